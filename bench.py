@@ -1,0 +1,334 @@
+"""Benchmark of the indirect INC par_loop on one GB300 (or N replicas).
+
+Workload: P1 tetrahedral Laplacian operator action y += K_e x_e on the unit
+cube, 128^3 hexes x 6 Kuhn tets = 12,582,912 cells, 2,146,689 vertices,
+lexicographic vertex numbering, FP64 (the second benchmark configuration;
+the first is the small CPU-runnable 2D case, used as a parity test).
+A step is one op2.par_loop over all cells.
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the CPU
+restatement of the reference's sequential backend instead (all host cores,
+one private output per thread as MPI ranks would have, summed at the end).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "INC par_loop cells/s + % of HBM peak; adjoint/forward time ratio vs plain GPU"
+N_CUBE = 128
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline(problem_np, threads=1, reps=3, max_cells=None):
+    """Time the oracle's sequential wrapper (the reference's CPU backend
+    restated in C, compiled with the reference's flags) on host cores."""
+    from oracle import op2 as O
+    coords, cells, x0 = problem_np
+    C = cells.shape[0] if max_cells is None else min(max_cells, cells.shape[0])
+    V = coords.shape[0]
+    verts = O.Set(V)
+    cset = O.Set(cells.shape[0])
+    c2v = O.Map(cset, verts, 4, cells)
+    X = O.Dat(O.DataSet(verts, 3), coords)
+    x = O.Dat(verts, x0)
+    y = O.Dat(verts, np.zeros(V))
+    from pyop2_gb300 import workloads
+    k = O.Kernel(workloads.P1_3D_LAPLACE_ACTION, "p1_laplace_3d")
+    loop = O.ParLoop(k, cset, y(O.INC, c2v), X(O.READ, c2v), x(O.READ, c2v), profile="timing")
+    ys = [np.zeros(V) for _ in range(threads)]
+    bounds = np.linspace(0, C, threads + 1).astype(np.int64)
+    best = None
+    for _ in range(reps):
+        for yy in ys:
+            yy[:] = 0
+        t0 = time.perf_counter()
+        if threads == 1:
+            loop.compute(0, C, overrides={0: ys[0]})
+        else:
+            ths = [threading.Thread(target=loop.compute,
+                                    args=(int(bounds[i]), int(bounds[i + 1])),
+                                    kwargs={"overrides": {0: ys[i]}}) for i in range(threads)]
+            for t in ths:
+                t.start()
+            for t in ths:
+                t.join()
+            total = ys[0]
+            for yy in ys[1:]:
+                total += yy
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return C / best, C, best
+
+
+def run_reference(args):
+    world, rank, local = _dist()
+    if rank != 0:
+        return 0
+    from pyop2_gb300 import meshes
+    coords, cells = meshes.unit_cube_tets(N_CUBE, permute=False, seed=0)
+    x0 = np.random.default_rng(1).uniform(-1, 1, coords.shape[0])
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline((coords, cells, x0), threads=threads, reps=1)
+    times = []
+    for _ in range(args.steps):
+        rate, C, dt = cpu_baseline((coords, cells, x0), threads=threads, reps=1)
+        times.append(dt)
+    tot = sum(times)
+    value = args.steps * cells.shape[0] / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "cells/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "p1_tet_laplace_action_128cube", "cells": int(cells.shape[0]),
+                   "vertices": int(coords.shape[0]), "numbering": "lexicographic"},
+        "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port",
+                         "sample": "full workload per step; oracle C wrapper, one thread per "
+                                   "contiguous cell range with a private y (rank emulation)"},
+        "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from pyop2_gb300.csrc import build as _b
+    _b.build()
+    from pyop2_gb300 import _lib, device, op2, workloads
+    from pyop2_gb300.configuration import configuration
+    configuration["device"] = local
+    if args.scatter:
+        configuration["scatter"] = args.scatter
+    device.require()
+    dev = device.device()
+
+    p = workloads.build_p1_3d(op2, n=N_CUBE, permute=args.permute, seed=0)
+    C = p["cells"].size
+    V = p["verts"].size
+    loop = op2.ParLoop(p["kernel"], p["cells"], p["y"](op2.INC, p["c2v"]),
+                       p["X"](op2.READ, p["c2v"]), p["x"](op2.READ, p["c2v"]))
+    loop.compute()                         # compile + upload
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        loop.compute()
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        barrier()
+        t0 = time.perf_counter()
+        for e0, e1 in ev:
+            e0.record(st)
+            loop.compute()
+            e1.record(st)
+        barrier()
+        wall = time.perf_counter() - t0
+    kern_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(kern_ms)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps * C / (total_ms * 1e-3)
+
+    # end to end through the public API with host buffers: x in from pinned
+    # host memory, par_loop, y back to host, every step
+    x_host = torch.from_numpy(p["x"].data_ro.copy()).pin_memory()
+    y_host = torch.empty(V, dtype=torch.float64).pin_memory()
+    xt, yt = p["x"].tensor, p["y"].tensor
+    for _ in range(2):
+        xt.copy_(x_host, non_blocking=True)
+        p["x"].mark_device_modified()
+        loop.compute()
+        y_host.copy_(yt, non_blocking=True)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        xt.copy_(x_host, non_blocking=True)
+        p["x"].mark_device_modified()
+        loop.compute()
+        y_host.copy_(yt, non_blocking=True)
+    e1.record(st)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = world * args.steps * C / (e2e_ms * 1e-3)
+
+    # FP64 ceiling: measured DFMA throughput of this GPU
+    import ctypes
+    fl = ctypes.c_double()
+    _lib.call("op2g_probe_fp64_peak", ctypes.byref(fl), device.stream_handle())
+    fp64_peak = fl.value / 1e12
+
+    if rank != 0:
+        return 0
+    peak, peak_kind = _peaks()
+    per_launch_ms = total_ms / args.steps
+    alg_bytes = workloads.bytes_c2a(C, V)
+    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
+    flops = workloads.P1_3D_FLOPS * C
+    fp64_achieved = flops / (per_launch_ms * 1e-3) / 1e12
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic_p1_laplace_3d_128cube.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    cpu = None
+    if not args.no_cpu_baseline:
+        coords = p["coords"]
+        cells = p["cellmap"]
+        x0 = p["x"].data_ro.copy()
+        rate, ncells, dt = cpu_baseline((coords, cells, x0), threads=1, reps=2)
+        cpu = {"value": rate, "unit": "cells/s", "cores": 1, "kind": "port",
+               "sample": "all %d cells, best of 2 passes, 1 core, oracle C wrapper built with "
+                         "the reference's -O3 -march=native -ffast-math" % ncells}
+    line = {
+        "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_launch_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "p1_tet_laplace_action_128cube", "cells": C, "vertices": V,
+                   "numbering": "random_permutation" if args.permute else "lexicographic",
+                   "scatter": configuration["scatter"], "l2": "working set %.0f MB > 129 MB L2, "
+                   "no flush" % (alg_bytes / 1e6), "parallelism": "replicas" if world > 1 else "1gpu"},
+        "pct_hbm_peak": 100.0 * achieved / peak,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "alg_bytes_per_launch": alg_bytes},
+        "roofline_fp64": {"achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                          "frac": fp64_achieved / fp64_peak, "flops_per_cell": workloads.P1_3D_FLOPS,
+                          "peak_source": "measured live (DFMA probe)"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": "cells/s", "h2d_bytes_per_step": 8 * V,
+                "d2h_bytes_per_step": 8 * V},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+        "wall_s_timed": wall,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--permute", action="store_true", help="random vertex numbering")
+    ap.add_argument("--scatter", default=None, choices=["atomic", "warp", "colour"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

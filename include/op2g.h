@@ -1,0 +1,280 @@
+/*
+ * op2g.h -- C ABI of libop2g, the GB300 (sm_103a) execution engine behind the
+ * PyOP2-compatible Python package `pyop2_gb300`.
+ *
+ * Everything here is plain C: integers, sizes and raw pointers.  Device
+ * pointers are CUDA global-memory addresses on the current device; "stream"
+ * is a cudaStream_t passed as void* (NULL = legacy default stream).  No call
+ * allocates device memory except where stated; callers own every buffer.
+ *
+ * Every entry point returns an op2g_status (0 = success).  On failure the
+ * thread-local message returned by op2g_last_error() says why.
+ *
+ * Which reference interface each group replaces (paths inside PyOP2 0.12.0):
+ *   op2g_kernel_*      the JIT-compiled, ctypes-called sequential wrapper
+ *                      `wrap_<name>(start, end, [layers], [subset], args..., maps...)`
+ *                      produced by pyop2/global_kernel.py:364-417 (compile/argtypes)
+ *                      from pyop2/codegen/builder.py:683-989 (WrapperBuilder) and
+ *                      called at pyop2/global_kernel.py:322-331.
+ *   op2g_sparsity_*    pyop2/sparsity.pyx:121-175 (build_sparsity) and
+ *                      pyop2/sparsity.pyx:178-405 (fill_with_zeros), which walk
+ *                      Map pairs into a PETSc MATPREALLOCATOR.
+ *   op2g_mat_*         the PETSc calls behind pyop2/types/mat.py: zeroEntries
+ *                      (:786-790), zeroRowsLocal (:792-801), setValuesLocalRCV
+ *                      for set_local_diagonal_entries (:806-827), MatMult for
+ *                      Mat * vector (:850-855 in the abstract interface).
+ *   op2g_colour_*      the two-level greedy colouring "plan" of the historical
+ *                      OP2 CUDA backend, documented in doc/sphinx/source/plan.rst:43-80
+ *                      (no code counterpart in this checkout).
+ */
+#ifndef OP2G_H
+#define OP2G_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OP2G_ABI_VERSION 1
+
+/* ---------------------------------------------------------------- status */
+typedef int32_t op2g_status;
+enum {
+    OP2G_OK = 0,
+    OP2G_ERR_INVALID = 1,      /* bad argument / descriptor                     */
+    OP2G_ERR_COMPILE = 2,      /* NVRTC rejected the generated source           */
+    OP2G_ERR_CUDA = 3,         /* a CUDA runtime/driver call failed             */
+    OP2G_ERR_BOUNDS = 4,       /* a device-side check tripped (map out of range) */
+    OP2G_ERR_NEW_NONZERO = 5,  /* Mat insertion outside the sparsity pattern    */
+    OP2G_ERR_CAPACITY = 6,     /* a fixed device capacity was exceeded          */
+    OP2G_ERR_UNSUPPORTED = 7,  /* feature not implemented                       */
+    OP2G_ERR_TIMEOUT = 8       /* a bounded device wait gave up                 */
+};
+
+/* Device-side error word bits (written with atomicOr by generated kernels). */
+enum {
+    OP2G_DEVERR_MAP_BOUNDS = 1,   /* map value >= toset size (debug builds)  */
+    OP2G_DEVERR_NEW_NONZERO = 2,  /* (row, col) not in the Mat's pattern     */
+    OP2G_DEVERR_CAPACITY = 4      /* row candidate list above the capacity   */
+};
+
+/* Thread-local description of the last failure (never NULL). */
+const char *op2g_last_error(void);
+/* OP2G_ABI_VERSION of the loaded library. */
+int32_t op2g_abi_version(void);
+
+/* Make `device` current for this thread and initialise its primary context.
+ * Returns the SM count and compute capability through the out-pointers
+ * (either may be NULL). */
+op2g_status op2g_device_init(int32_t device, int32_t *sm_count, int32_t *cc_major,
+                             int32_t *cc_minor);
+
+/* ---------------------------------------------------- par_loop wrappers */
+/* Access descriptors: same integer values as pyop2/types/access.py:4-10. */
+enum { OP2G_READ = 1, OP2G_WRITE = 2, OP2G_RW = 3, OP2G_INC = 4, OP2G_MIN = 5, OP2G_MAX = 6 };
+/* Iteration regions: same values as pyop2/types/__init__.py:14-18. */
+enum { OP2G_ON_BOTTOM = 1, OP2G_ON_TOP = 2, OP2G_ON_INTERIOR_FACETS = 3, OP2G_ALL = 4 };
+/* Element types (numpy dtype -> C type, pyop2/datatypes.py:13-29). */
+enum {
+    OP2G_F64 = 0, OP2G_F32 = 1, OP2G_I32 = 2, OP2G_U32 = 3, OP2G_I64 = 4, OP2G_U64 = 5,
+    OP2G_I16 = 6, OP2G_U16 = 7, OP2G_I8 = 8, OP2G_U8 = 9
+};
+/* Argument kinds (pyop2/global_kernel.py:89-247). */
+enum { OP2G_ARG_DAT = 0, OP2G_ARG_GLOBAL = 1, OP2G_ARG_MAT = 2, OP2G_ARG_PASSTHROUGH = 3 };
+/* Map kinds (pyop2/types/map.py: Map :17, PermutedMap :171, ComposedMap :218). */
+enum { OP2G_MAP_PLAIN = 0, OP2G_MAP_PERMUTED = 1, OP2G_MAP_COMPOSED = 2 };
+/* How INC contributions to indirect Dats and Mats reach memory. */
+enum {
+    OP2G_SCATTER_ATOMIC = 0,   /* one hardware atomic (RED) per contribution          */
+    OP2G_SCATTER_WARP = 1,     /* __match_any_sync groups lanes on one target, one
+                                  shuffle-reduced atomic per group                    */
+    OP2G_SCATTER_PLAIN = 2     /* plain read-modify-write: only legal when the caller
+                                  launches one colour (conflict-free cell set) at a time */
+};
+
+#define OP2G_MAX_ARGS 32
+#define OP2G_MAX_MAPS 32
+#define OP2G_MAX_COMPOSED 8
+
+/* One map of the loop.  Host arrays are copied during op2g_kernel_create and
+ * baked into the generated code as constants (as the reference bakes map
+ * offsets as named literals, pyop2/codegen/builder.py:55-62). */
+typedef struct op2g_map_desc {
+    int32_t kind;          /* OP2G_MAP_*                                                */
+    int32_t arity;
+    int32_t base;          /* PERMUTED: index of the permuted map in this table         */
+    int32_t ncomposed;     /* COMPOSED: number of maps in `composed`                    */
+    int32_t composed[OP2G_MAX_COMPOSED]; /* COMPOSED: maps_[0..ncomposed) (outermost first) */
+    const int32_t *offset;          /* host, arity entries, or NULL (not extruded)     */
+    const int32_t *offset_quotient; /* host, arity entries, or NULL                    */
+    const int32_t *permutation;     /* host, arity entries (PERMUTED only)             */
+} op2g_map_desc;
+
+/* One argument of the loop, in kernel-argument order. */
+typedef struct op2g_arg_desc {
+    int32_t kind;     /* OP2G_ARG_*                                                  */
+    int32_t access;   /* OP2G_READ .. OP2G_MAX                                       */
+    int32_t dtype;    /* OP2G_F64 ..                                                 */
+    int32_t dim;      /* DAT/GLOBAL: values per entity (cdim)                        */
+    int32_t map;      /* DAT: map index or -1 (direct); MAT: row map index           */
+    int32_t cmap;     /* MAT: column map index                                       */
+    int32_t rdim;     /* MAT: rows per block                                          */
+    int32_t cdim;     /* MAT: columns per block                                       */
+} op2g_arg_desc;
+
+typedef struct op2g_loop_desc {
+    int32_t extruded;          /* iterate (entity, layer)                                 */
+    int32_t constant_layers;   /* layers array has one row                                */
+    int32_t extruded_periodic;
+    int32_t indexed;           /* iterate indices[start..end) (Subset, colour order)      */
+    int32_t iteration_region;  /* OP2G_ALL ..                                             */
+    int32_t pass_layer_arg;    /* append `int layer` to the kernel call                   */
+    int32_t scatter;           /* OP2G_SCATTER_*                                          */
+    int32_t block_size;        /* threads per CTA (0 = 256)                               */
+    int32_t debug_checks;      /* bounds-check every map value, report via error word     */
+    int32_t batched;           /* build the persistent multi-loop variant (see _batch)    */
+} op2g_loop_desc;
+
+typedef struct op2g_kernel op2g_kernel;
+
+/* Generate the CUDA wrapper around `user_src` (a C kernel whose entry point is
+ * `kernel_name`), compile it with NVRTC for `arch` ("sm_103a"; NULL = the
+ * current device) and return a handle.  `cache_dir` (may be NULL) holds
+ * compiled cubins keyed by a hash of source, options and arch.  No device is
+ * needed unless arch is NULL.  On OP2G_ERR_COMPILE op2g_last_error() holds
+ * the NVRTC log. */
+op2g_status op2g_kernel_create(const char *user_src, const char *kernel_name,
+                               const op2g_loop_desc *loop, const op2g_arg_desc *args,
+                               int32_t nargs, const op2g_map_desc *maps, int32_t nmaps,
+                               const char *arch, const char *cache_dir, op2g_kernel **out);
+void op2g_kernel_destroy(op2g_kernel *k);
+
+/* Copy the generated CUDA source into buf (NUL-terminated, truncated to len);
+ * *needed receives strlen+1. */
+op2g_status op2g_kernel_source(const op2g_kernel *k, char *buf, size_t len, size_t *needed);
+/* Number of device-pointer slots op2g_kernel_launch expects in `ptrs`:
+ *   per argument, in order: DAT 1 (data), GLOBAL 1 (data, or the zeroed
+ *   reduction temporary for INC), MAT 3 (values, rowptr int64, colidx int32),
+ *   PASSTHROUGH 1; then one slot per map of the map table (values, int32
+ *   [iterset total, arity], NULL for PERMUTED/COMPOSED entries). */
+int32_t op2g_kernel_num_ptrs(const op2g_kernel *k);
+/* Registers per thread of the loaded kernel (-1 before first launch). */
+int32_t op2g_kernel_num_regs(const op2g_kernel *k);
+
+typedef struct op2g_launch_desc {
+    int64_t start, end;        /* iteration range (entities; indices range if indexed)    */
+    const int32_t *layers;     /* device layers array [*, 2] (extruded) or NULL          */
+    const int32_t *indices;    /* device entity indices (indexed) or NULL                */
+    int32_t *err;              /* device error word (OP2G_DEVERR_* bits) or NULL         */
+    void *const *ptrs;         /* host array of op2g_kernel_num_ptrs device pointers     */
+    const int64_t *map_toset;  /* host array, toset size per map (bounds checks) or NULL */
+    int64_t layers_per_entity; /* constant-layer extrusion: layers iterated per entity,
+                                  used only to size the grid (0 = 1)                     */
+    int32_t grid;              /* CTAs (0 = derived from occupancy and the range)        */
+} op2g_launch_desc;
+
+/* Launch the wrapper over [start, end) on `stream`.  Asynchronous. */
+op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *stream);
+
+/* Persistent batched launch of a kernel built with loop->batched = 1: one
+ * launch runs nloops loops of the same signature.  `params` is a DEVICE array
+ * of nloops records, each op2g_kernel_param_bytes(k) bytes, laid out as
+ * op2g_kernel_pack_params writes them; `work` is a DEVICE array of nwork
+ * (loop index, start, end) int64 triples.  CTAs take work items round robin. */
+int32_t op2g_kernel_param_bytes(const op2g_kernel *k);
+op2g_status op2g_kernel_pack_params(const op2g_kernel *k, const op2g_launch_desc *d,
+                                    void *out_host_record);
+op2g_status op2g_kernel_launch_batched(op2g_kernel *k, const void *params_dev,
+                                       const int64_t *work_dev, int64_t nwork,
+                                       int32_t grid, void *stream);
+
+/* ------------------------------------------------------------- sparsity */
+/* One (row map, column map, iteration region) triple of a Sparsity
+ * (pyop2/types/mat.py:118-176).  Map arrays are device int32
+ * [nent_total, arity]; composed chains are device pointers to arity-1 maps,
+ * applied innermost-last as in pyop2/sparsity.pyx:249-259. */
+typedef struct op2g_sparsity_pair {
+    const int32_t *rmap, *cmap;
+    int32_t rarity, carity;
+    int64_t nent;                 /* entities iterated (iterset.size)                 */
+    int32_t region;               /* OP2G_ALL ..                                      */
+    int32_t nrcomposed, nccomposed;
+    const int32_t *rcomposed[OP2G_MAX_COMPOSED];
+    const int32_t *ccomposed[OP2G_MAX_COMPOSED];
+    const int32_t *roffset, *coffset;                   /* host, or NULL          */
+    const int32_t *roffset_quotient, *coffset_quotient; /* host, or NULL          */
+} op2g_sparsity_pair;
+
+typedef struct op2g_sparsity_desc {
+    int64_t nrows, ncols;         /* block rows / block columns                      */
+    int32_t set_diag;             /* add (i, i) for i < min(nrows, ncols)            */
+    int32_t extruded, constant_layers, extruded_periodic;
+    const int32_t *layers;        /* device layers array of the iterset (extruded)   */
+    int32_t layer_slots;          /* extruded: max over entities of layers[e,1] - layers[e,0]
+                                     (an upper bound of cells per column)             */
+    int32_t npairs;
+    const op2g_sparsity_pair *pairs;
+} op2g_sparsity_desc;
+
+/* Bytes of device workspace op2g_sparsity_build needs for `d`. */
+op2g_status op2g_sparsity_workspace(const op2g_sparsity_desc *d, size_t *bytes);
+/* Phase 1: rowptr[nrows+1] (int64, device) gets the exclusive prefix sum of
+ * the per-row counts of distinct columns; *nnz (host) the total.  The call
+ * synchronises `stream` to return nnz. */
+op2g_status op2g_sparsity_count(const op2g_sparsity_desc *d, void *workspace, size_t ws_bytes,
+                                int64_t *rowptr, int64_t *nnz, void *stream);
+/* Phase 2: colidx[nnz] (int32, device) receives each row's columns, sorted
+ * ascending and unique.  Must follow op2g_sparsity_count with the same
+ * workspace (it reuses the row->entity transpose kept there). */
+op2g_status op2g_sparsity_fill(const op2g_sparsity_desc *d, void *workspace, size_t ws_bytes,
+                               const int64_t *rowptr, int32_t *colidx, void *stream);
+
+/* ----------------------------------------------------------- matrices */
+/* Block-CSR matrix with rdim x cdim row-major blocks (rdim = cdim = 1 is CSR). */
+typedef struct op2g_bcsr {
+    int64_t nrows, ncols;      /* block rows / block columns */
+    int32_t rdim, cdim;
+    const int64_t *rowptr;     /* device [nrows + 1] */
+    const int32_t *colidx;     /* device [nnz]       */
+    double *values;            /* device [nnz * rdim * cdim] */
+} op2g_bcsr;
+
+/* Zero the given dof rows (rows are dof indices: block_row * rdim + r) keeping
+ * the pattern, and put diag_val on their diagonal (zeroRowsLocal). */
+op2g_status op2g_mat_zero_rows(const op2g_bcsr *m, const int32_t *rows_dev, int64_t nrows_zero,
+                               double diag_val, void *stream);
+/* Set (INSERT) diag_val on the diagonal of the given dof rows. */
+op2g_status op2g_mat_set_diagonal(const op2g_bcsr *m, const int32_t *rows_dev, int64_t n,
+                                  double diag_val, int32_t *err, void *stream);
+/* y = A x (transpose = 0) or y = A^T x (transpose = 1; y must be zeroed, uses atomics). */
+op2g_status op2g_mat_spmv(const op2g_bcsr *m, const double *x, double *y, int32_t transpose,
+                          void *stream);
+
+/* ------------------------------------------------------------ colouring */
+/* Greedy colouring of `ncells` entities so that no two entities of one colour
+ * share a target through any of the `nmaps` maps (device int32 [ncells, arity_k],
+ * negative values ignored).  Each target set has `target_size[k]` entries.
+ * Outputs (device): colour[ncells] int32, order[ncells] int32 (entities sorted
+ * by colour, stable), colour_ptr[max_colours + 1] int64 (segment offsets).
+ * *ncolours (host) receives the colour count; the call synchronises.  Fails
+ * with OP2G_ERR_CAPACITY if more than max_colours colours are needed.
+ * workspace: op2g_colour_workspace bytes of device memory. */
+op2g_status op2g_colour_workspace(int64_t ncells, int32_t nmaps, const int64_t *target_size,
+                                  size_t *bytes);
+op2g_status op2g_colour(int64_t ncells, int32_t nmaps, const int32_t *const *maps,
+                        const int32_t *arity, const int64_t *target_size, int32_t max_colours,
+                        void *workspace, size_t ws_bytes, int32_t *colour, int32_t *order,
+                        int64_t *colour_ptr, int32_t *ncolours, void *stream);
+
+/* --------------------------------------------------------- measurement */
+/* Time a register-resident FP64 FMA loop over the whole GPU and return the
+ * achieved FP64 rate (flop/s, FMA = 2) -- the second roofline ceiling of the
+ * element kernels.  Synchronous. */
+op2g_status op2g_probe_fp64_peak(double *flops_per_s, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OP2G_H */

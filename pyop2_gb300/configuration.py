@@ -1,0 +1,83 @@
+"""Runtime configuration, mirroring pyop2/configuration.py:43-172.
+
+Kept keys use the reference's ``PYOP2_*`` environment variables; keys that
+only exist here use ``OP2G_*``.
+"""
+import os
+from tempfile import gettempdir
+
+from pyop2_gb300.exceptions import ConfigurationError
+
+
+def _bool(v):
+    if isinstance(v, str):
+        return v.strip().lower() not in ("", "0", "false", "no", "off")
+    return bool(v)
+
+
+class Configuration(dict):
+    # name: (environment variable, type, default)
+    DEFAULTS = {
+        "debug": ("PYOP2_DEBUG", bool, False),
+        "type_check": ("PYOP2_TYPE_CHECK", bool, True),
+        "log_level": ("PYOP2_LOG_LEVEL", (str, int), "WARNING"),
+        "cache_dir": ("PYOP2_CACHE_DIR", str,
+                      os.path.join(gettempdir(), "pyop2_gb300-cache-uid%s" % os.getuid())),
+        "block_sparsity": ("PYOP2_BLOCK_SPARSITY", bool, True),
+        "matnest": ("PYOP2_MATNEST", bool, True),
+        "compute_kernel_flops": ("PYOP2_COMPUTE_KERNEL_FLOPS", bool, False),
+        "print_cache_info": ("PYOP2_CACHE_INFO", bool, False),
+        # INC conflict resolution: "atomic", "warp", "colour" or "auto" (autotuner)
+        "scatter": ("OP2G_SCATTER", str, "atomic"),
+        # threads per CTA of generated wrappers
+        "block_size": ("OP2G_BLOCK_SIZE", int, 256),
+        # let the autotuner pick scatter strategy and block size per kernel
+        "autotune": ("OP2G_AUTOTUNE", bool, False),
+        # CUDA device used by this process
+        "device": ("OP2G_DEVICE", int, 0),
+    }
+
+    def __init__(self):
+        super().__init__()
+        self._set = set()
+        self.reset()
+
+    def reset(self):
+        for k, (env, typ, default) in self.DEFAULTS.items():
+            v = os.environ.get(env)
+            if v is None:
+                self[k] = default
+            else:
+                self[k] = self._convert(k, v)
+
+    def _convert(self, key, value):
+        typ = self.DEFAULTS[key][1]
+        if typ is bool:
+            return _bool(value)
+        if typ is int:
+            return int(value)
+        if isinstance(typ, tuple):
+            return value
+        return typ(value)
+
+    def reconfigure(self, **kwargs):
+        for k, v in kwargs.items():
+            self[k] = v
+
+    def __setitem__(self, key, value):
+        if key not in self.DEFAULTS:
+            raise ConfigurationError("Unknown configuration option %r" % key)
+        typ = self.DEFAULTS[key][1]
+        if typ is bool:
+            value = _bool(value)
+        elif typ is int and not isinstance(value, int):
+            try:
+                value = int(value)
+            except (TypeError, ValueError):
+                raise ConfigurationError("Option %r needs an int" % key)
+        if key == "scatter" and value not in ("atomic", "warp", "colour", "auto"):
+            raise ConfigurationError("scatter must be atomic, warp, colour or auto")
+        super().__setitem__(key, value)
+
+
+configuration = Configuration()

@@ -1,0 +1,643 @@
+// op2g_codegen.cpp -- writes the CUDA wrapper for one par_loop signature.
+//
+// The reference generates, per (local kernel, argument signature), a C loop
+// that packs each argument, calls the kernel and unpacks
+// (pyop2/codegen/builder.py:683-989, lowered by rep2loopy.py).  Here the same
+// contract is written directly as CUDA: one thread per iteration entity (or
+// per (entity, layer) for constant-layer extrusion), packs in registers, the
+// user's kernel inlined as a __device__ function, and conflict handling for
+// INC/MIN/MAX by atomics, warp aggregation, or plain stores when the caller
+// iterates one colour at a time.
+#include "op2g_internal.h"
+
+#include <sstream>
+
+namespace op2g {
+
+static const char *ctype_of(int dt) {
+    switch (dt) {
+        case OP2G_F64: return "double";
+        case OP2G_F32: return "float";
+        case OP2G_I32: return "int";
+        case OP2G_U32: return "unsigned";
+        case OP2G_I64: return "long long";
+        case OP2G_U64: return "unsigned long long";
+        case OP2G_I16: return "short";
+        case OP2G_U16: return "unsigned short";
+        case OP2G_I8: return "signed char";
+        case OP2G_U8: return "unsigned char";
+    }
+    return nullptr;
+}
+
+static bool atomic_capable(int dt) {
+    return dt == OP2G_F64 || dt == OP2G_F32 || dt == OP2G_I32 || dt == OP2G_U32 ||
+           dt == OP2G_I64 || dt == OP2G_U64;
+}
+
+// Strip `#include <...>` lines of C system headers: NVRTC has no host system
+// headers, and the device math library and fixed-width integer types they
+// would declare are provided by NVRTC and op2g_device.cuh.  Any other include
+// is kept (and fails to compile if it cannot be found, as it should).
+static std::string strip_system_includes(const std::string &src) {
+    static const char *known[] = {"math.h", "stdio.h", "stdlib.h", "string.h", "stdint.h",
+                                  "stdbool.h", "complex.h", "petsc.h", "inttypes.h",
+                                  "float.h", "limits.h", "cmath", "cstdio", "cstdlib",
+                                  "cstring", "cstdint", "algorithm"};
+    std::istringstream in(src);
+    std::ostringstream out;
+    std::string line;
+    while (std::getline(in, line)) {
+        size_t p = line.find_first_not_of(" \t");
+        bool drop = false;
+        if (p != std::string::npos && line[p] == '#') {
+            size_t q = line.find("include", p);
+            if (q != std::string::npos) {
+                size_t lt = line.find('<', q), gt = line.find('>', q);
+                if (lt != std::string::npos && gt != std::string::npos && gt > lt) {
+                    std::string h = line.substr(lt + 1, gt - lt - 1);
+                    for (const char *k : known)
+                        if (h == k) drop = true;
+                }
+            }
+        }
+        out << (drop ? std::string("// (system include supplied by op2g) ") + line : line)
+            << "\n";
+    }
+    return out.str();
+}
+
+// ---------------------------------------------------------------------------
+struct Gen {
+    const Signature &S;
+    std::ostringstream o;
+    int nf = 1;  // 2 for ON_INTERIOR_FACETS (packs span two cells of a column)
+
+    explicit Gen(const Signature &s) : S(s) {
+        nf = (S.loop.extruded && S.loop.iteration_region == OP2G_ON_INTERIOR_FACETS) ? 2 : 1;
+    }
+
+    // Map used for the outermost indexing of map m (PERMUTED -> its base).
+    int root_of(int m) const {
+        const MapInfo &mi = S.maps[m];
+        return mi.kind == OP2G_MAP_PERMUTED ? mi.base : m;
+    }
+
+    // Names of the per-iteration base rows.
+    std::string base_row(int m) const { return "mv" + std::to_string(m); }
+    std::string idx_arr(int m, int f) const {
+        return "mi" + std::to_string(m) + "_" + std::to_string(f);
+    }
+
+    void emit_constants() {
+        for (size_t m = 0; m < S.maps.size(); ++m) {
+            const MapInfo &mi = S.maps[m];
+            auto arr = [&](const char *nm, const std::vector<int> &v) {
+                o << "__device__ const int op2g_" << nm << m << "[" << v.size() << "] = {";
+                for (size_t i = 0; i < v.size(); ++i) o << (i ? ", " : "") << v[i];
+                o << "};\n";
+            };
+            if (!mi.offset.empty()) arr("off", mi.offset);
+            if (!mi.offset_quotient.empty()) arr("offq", mi.offset_quotient);
+            if (!mi.permutation.empty()) arr("perm", mi.permutation);
+        }
+    }
+
+    // Which maps need per-iteration index arrays.
+    std::vector<bool> used_maps() const {
+        std::vector<bool> used(S.maps.size(), false);
+        for (const ArgInfo &a : S.args) {
+            if (a.d.kind == OP2G_ARG_DAT && a.d.map >= 0) used[a.d.map] = true;
+            if (a.d.kind == OP2G_ARG_MAT) {
+                used[a.d.map] = true;
+                used[a.d.cmap] = true;
+            }
+        }
+        return used;
+    }
+
+    // Emit loading of the base row for plain map m at entity expression `ent`.
+    void emit_plain_row(int m, const std::string &ent, const std::string &ind) {
+        const MapInfo &mi = S.maps[m];
+        o << ind << "int " << base_row(m) << "[" << mi.arity << "];\n";
+        o << ind << "{ const int *r_ = (const int *)p.ptr[" << S.map_slot(m) << "] + (" << ent
+          << ") * " << mi.arity << ";\n";
+        o << ind << "#pragma unroll\n";
+        o << ind << "  for (int i = 0; i < " << mi.arity << "; ++i) " << base_row(m)
+          << "[i] = r_[i]; }\n";
+    }
+
+    // Emit index arrays mi<m>_<f>[arity] for map m (after base rows exist).
+    void emit_index_arrays(int m, const std::string &ind) {
+        const MapInfo &mi = S.maps[m];
+        // Resolve: outermost plain map supplying the values, and the row it reads.
+        std::string rowname;
+        int src = m;
+        if (mi.kind == OP2G_MAP_PLAIN) {
+            rowname = base_row(m);
+        } else if (mi.kind == OP2G_MAP_PERMUTED) {
+            rowname = base_row(mi.base);
+            src = mi.base;
+        } else {  // COMPOSED: chain maps_[k-1] .. maps_[1] (arity 1), then maps_[0]
+            const int outer = mi.composed[0];
+            const MapInfo &om = S.maps[outer];
+            int oroot = outer;
+            std::string operm;
+            if (om.kind == OP2G_MAP_PERMUTED) {
+                oroot = om.base;
+                operm = "op2g_perm" + std::to_string(outer);
+            }
+            o << ind << "int " << base_row(m) << "[" << mi.arity << "];\n";
+            o << ind << "{ long long c_ = n;\n";
+            for (int k = mi.ncomposed - 1; k >= 1; --k) {
+                int cm = mi.composed[k];
+                int croot = root_of(cm);
+                o << ind << "  if (c_ >= 0) c_ = ((const int *)p.ptr[" << S.map_slot(croot)
+                  << "])[c_ * " << S.maps[croot].arity << "];\n";
+            }
+            o << ind << "#pragma unroll\n";
+            o << ind << "  for (int i = 0; i < " << mi.arity << "; ++i) " << base_row(m)
+              << "[i] = c_ >= 0 ? ((const int *)p.ptr[" << S.map_slot(oroot) << "])[c_ * "
+              << S.maps[oroot].arity << " + " << (operm.empty() ? "i" : operm + "[i]")
+              << "] : -1; }\n";
+            rowname = base_row(m);
+            src = outer;  // offsets come from maps_[0] (pyop2/types/map.py:271)
+            if (om.kind == OP2G_MAP_PERMUTED) src = om.base;
+        }
+        const MapInfo &sm = S.maps[src];
+        const bool perm = (mi.kind == OP2G_MAP_PERMUTED);
+        const std::string pidx = perm ? "op2g_perm" + std::to_string(m) + "[i]" : "i";
+        // Index into the offset arrays of `src`: the permutation applies to the
+        // offsets as well (pyop2/codegen/builder.py:160-166).
+        std::string oidx = pidx;
+        if (mi.kind == OP2G_MAP_COMPOSED) {
+            const MapInfo &om = S.maps[mi.composed[0]];
+            oidx = om.kind == OP2G_MAP_PERMUTED ? "op2g_perm" + std::to_string(mi.composed[0]) + "[i]"
+                                                 : "i";
+        }
+        const bool extr = S.loop.extruded && !sm.offset.empty();
+        for (int f = 0; f < nf; ++f) {
+            o << ind << "int " << idx_arr(m, f) << "[" << mi.arity << "];\n";
+            o << ind << "#pragma unroll\n";
+            o << ind << "for (int i = 0; i < " << mi.arity << "; ++i) {\n";
+            o << ind << "  int b_ = " << rowname << "[" << (mi.kind == OP2G_MAP_COMPOSED ? "i" : pidx)
+              << "];\n";
+            if (extr) {
+                // pyop2/codegen/builder.py:81-125: base + offset * (layer - bottom + f),
+                // with the periodic remainder of :27-30 / :109-121.
+                std::string offi = "op2g_off" + std::to_string(src) + "[" + oidx + "]";
+                std::string e = "(layer - bottom + " + std::to_string(f) + ")";
+                if (S.loop.extruded_periodic) {
+                    if (!sm.offset_quotient.empty()) {
+                        std::string q = "op2g_offq" + std::to_string(src) + "[" + oidx + "]";
+                        e = "(op2g::rem(" + e + " + " + q + ", nlay) - op2g::rem(" + q + ", nlay))";
+                    } else {
+                        e = "op2g::rem(" + e + ", nlay)";
+                    }
+                }
+                o << ind << "  if (b_ >= 0) b_ += " << offi << " * " << e << ";\n";
+            }
+            if (S.loop.debug_checks) {
+                o << ind << "  if (b_ >= p.toset[" << m
+                  << "]) { op2g::set_err(p.err, OP2G_DEVERR_MAP_BOUNDS); b_ = -1; }\n";
+            }
+            o << ind << "  " << idx_arr(m, f) << "[i] = b_;\n";
+            o << ind << "}\n";
+        }
+    }
+
+    std::string emit() {
+        std::ostringstream &O = o;
+        O << "// generated by op2g_codegen.cpp for kernel '" << S.kernel_name << "'\n";
+        O << "#include \"op2g_device.cuh\"\n";
+        O << "#define OP2G_DEVERR_MAP_BOUNDS " << OP2G_DEVERR_MAP_BOUNDS << "\n";
+        O << "#define OP2G_DEVERR_NEW_NONZERO " << OP2G_DEVERR_NEW_NONZERO << "\n";
+        O << "namespace op2g { __device__ __forceinline__ int rem(int a, int b) { return a < b ? a : a - b; } }\n";
+        O << "#define restrict __restrict__\n";
+        O << "// ---- user kernel ----\n";
+        O << strip_system_includes(S.user_src) << "\n";
+        O << "// ---- end of user kernel ----\n";
+        O << "#undef restrict\n";
+        emit_constants();
+        const int nptr = S.nptrs;
+        const int nmaps = (int)S.maps.size();
+        O << "struct op2g_params_t {\n"
+          << "  long long start, end;\n"
+          << "  const int *layers;\n"
+          << "  const int *indices;\n"
+          << "  int *err;\n"
+          << "  void *ptr[" << (nptr > 0 ? nptr : 1) << "];\n"
+          << "  long long toset[" << (nmaps > 0 ? nmaps : 1) << "];\n"
+          << "};\n";
+
+        const int BS = S.block_size;
+        const bool warp = S.loop.scatter == OP2G_SCATTER_WARP;
+        const bool plain = S.loop.scatter == OP2G_SCATTER_PLAIN;
+        const bool extr = S.loop.extruded != 0;
+        const bool varlay = extr && !S.loop.constant_layers;
+
+        // ----- the run function: a strided sweep of [start, end) plus reductions
+        O << "__device__ __forceinline__ void op2g_run(const op2g_params_t &p, long long start, "
+             "long long end, long long first, long long stride) {\n";
+        // Global accumulators
+        for (size_t a = 0; a < S.args.size(); ++a) {
+            const ArgInfo &A = S.args[a];
+            if (A.d.kind != OP2G_ARG_GLOBAL) continue;
+            const char *T = ctype_of(A.d.dtype);
+            if (A.d.access == OP2G_INC) {
+                O << "  " << T << " gacc" << a << "[" << A.d.dim << "];\n";
+                O << "  for (int j = 0; j < " << A.d.dim << "; ++j) gacc" << a << "[j] = (" << T
+                  << ")0;\n";
+            } else if (A.d.access == OP2G_MIN || A.d.access == OP2G_MAX) {
+                O << "  " << T << " gacc" << a << "[" << A.d.dim << "];\n";
+                O << "  for (int j = 0; j < " << A.d.dim << "; ++j) gacc" << a << "[j] = ((const "
+                  << T << " *)p.ptr[" << A.slot << "])[j];\n";
+            }
+        }
+        if (extr) {
+            // pyop2/codegen/builder.py:771-812 (layer extents per iteration region)
+            O << "  const int *lay_ = p.layers;\n";
+        }
+        std::string ent_expr = "n";
+        if (extr && !varlay) {
+            O << "  const int cs_ = lay_[0], ce_ = lay_[1] - 1;  // cellStart, cellEnd\n";
+            emit_layer_extents("cs_", "ce_", "ls_", "le_", "  ");
+            O << "  const long long nl_ = le_ > ls_ ? (long long)(le_ - ls_) : 0;\n";
+            O << "  const long long i0_ = start * nl_, i1_ = end * nl_;\n";
+        } else {
+            O << "  const long long i0_ = start, i1_ = end;\n";
+        }
+        O << "  for (long long base_ = i0_ + first; base_ < i1_; base_ += stride) {\n";
+        O << "    const long long it = base_ + threadIdx.x;\n";
+        O << "    const bool active = it < i1_;\n";
+        // Pack declarations visible to the warp-aggregated unpack.
+        std::string I = "    ";
+        // Per-iteration declarations that warp scatter needs outside `if (active)`.
+        if (warp) {
+            for (size_t a = 0; a < S.args.size(); ++a) {
+                const ArgInfo &A = S.args[a];
+                if (A.d.kind == OP2G_ARG_DAT && A.d.map >= 0 && A.d.access == OP2G_INC) {
+                    const int ar = S.maps[A.d.map].arity;
+                    O << I << ctype_of(A.d.dtype) << " t" << a << "[" << nf * ar * A.d.dim
+                      << "];\n";
+                    O << I << "int ti" << a << "[" << nf * ar << "];\n";
+                }
+            }
+        }
+        O << I << "if (active) {\n";
+        std::string J = "      ";
+        // entity / layer
+        if (extr && !varlay) {
+            O << J << "const long long it_ent = it / nl_;\n";
+            O << J << "const int layer = ls_ + (int)(it - it_ent * nl_);\n";
+            O << J << "const long long n = " << (S.loop.indexed ? "p.indices[it_ent]" : "it_ent")
+              << ";\n";
+            O << J << "const int bottom = " << (S.loop.iteration_region == OP2G_ON_TOP ? "cs_" : "ls_")
+              << ";\n";
+            O << J << "const int nlay = ce_ - cs_; (void)nlay; (void)bottom;\n";
+            emit_body(J, warp, plain);
+        } else if (varlay) {
+            O << J << "const long long n = " << (S.loop.indexed ? "p.indices[it]" : "it") << ";\n";
+            O << J << "const int cs_ = lay_[2 * n], ce_ = lay_[2 * n + 1] - 1;\n";
+            emit_layer_extents("cs_", "ce_", "ls_", "le_", J);
+            O << J << "const int bottom = " << (S.loop.iteration_region == OP2G_ON_TOP ? "cs_" : "ls_")
+              << ";\n";
+            O << J << "const int nlay = ce_ - cs_; (void)nlay; (void)bottom;\n";
+            O << J << "for (int layer = ls_; layer < le_; ++layer) {\n";
+            emit_body(J + "  ", false, plain);
+            O << J << "}\n";
+        } else {
+            O << J << "const long long n = " << (S.loop.indexed ? "p.indices[it]" : "it") << ";\n";
+            emit_body(J, warp, plain);
+        }
+        O << I << "}\n";
+        if (warp) {
+            for (size_t a = 0; a < S.args.size(); ++a) {
+                const ArgInfo &A = S.args[a];
+                if (A.d.kind == OP2G_ARG_DAT && A.d.map >= 0 && A.d.access == OP2G_INC) {
+                    const int ar = S.maps[A.d.map].arity;
+                    const int D = A.d.dim;
+                    const char *T = ctype_of(A.d.dtype);
+                    O << I << "{ " << T << " *d_ = (" << T << " *)p.ptr[" << A.slot << "];\n";
+                    O << I << "#pragma unroll\n";
+                    O << I << "  for (int i = 0; i < " << nf * ar << "; ++i) {\n";
+                    O << I << "    const bool v_ = active && ti" << a << "[i] >= 0;\n";
+                    O << I << "    const long long o_ = v_ ? (long long)ti" << a << "[i] * " << D
+                      << " : 0;\n";
+                    O << I << "#pragma unroll\n";
+                    O << I << "    for (int j = 0; j < " << D << "; ++j) op2g::warp_agg_inc(d_ + o_ + j, t"
+                      << a << "[i * " << D << " + j], v_);\n";
+                    O << I << "  } }\n";
+                }
+            }
+        }
+        O << "  }\n";  // sweep loop
+        // Global reductions (pyop2/parloop.py:409-452 semantics on one device:
+        // INC goes to the zeroed temporary, MIN/MAX straight into the Global).
+        for (size_t a = 0; a < S.args.size(); ++a) {
+            const ArgInfo &A = S.args[a];
+            if (A.d.kind != OP2G_ARG_GLOBAL || A.d.access == OP2G_READ) continue;
+            const char *T = ctype_of(A.d.dtype);
+            const char *red = A.d.access == OP2G_INC ? "warp_sum"
+                              : A.d.access == OP2G_MIN ? "warp_min" : "warp_max";
+            const char *atom = A.d.access == OP2G_INC ? "atomic_inc"
+                               : A.d.access == OP2G_MIN ? "atomic_min" : "atomic_max";
+            O << "  for (int j = 0; j < " << A.d.dim << "; ++j) {\n";
+            O << "    " << T << " v_ = op2g::" << red << "(gacc" << a << "[j]);\n";
+            O << "    if ((threadIdx.x & 31) == 0) op2g::" << atom << "(((" << T << " *)p.ptr["
+              << A.slot << "]) + j, v_);\n";
+            O << "  }\n";
+        }
+        O << "}\n\n";
+
+        // ----- the entry points
+        O << "extern \"C\" __global__ void __launch_bounds__(" << BS
+          << ") op2g_wrap(const __grid_constant__ op2g_params_t p) {\n"
+          << "  op2g_run(p, p.start, p.end, (long long)blockIdx.x * " << BS
+          << ", (long long)gridDim.x * " << BS << ");\n}\n";
+        O << "extern \"C\" __global__ void __launch_bounds__(" << BS
+          << ") op2g_wrap_batched(const op2g_params_t *__restrict__ P, const long long "
+             "*__restrict__ work, long long nwork) {\n"
+          << "  for (long long w = blockIdx.x; w < nwork; w += gridDim.x) {\n"
+          << "    const op2g_params_t &p = P[work[3 * w]];\n"
+          << "    op2g_run(p, work[3 * w + 1], work[3 * w + 2], 0, " << BS << ");\n"
+          << "  }\n}\n";
+        return O.str();
+    }
+
+    // Layer range for the iteration region (pyop2/codegen/builder.py:771-800).
+    void emit_layer_extents(const std::string &cs, const std::string &ce, const std::string &ls,
+                            const std::string &le, const std::string &ind) {
+        switch (S.loop.iteration_region) {
+            case OP2G_ON_BOTTOM:
+                o << ind << "const int " << ls << " = " << cs << ", " << le << " = " << cs << " + 1;\n";
+                break;
+            case OP2G_ON_TOP:
+                o << ind << "const int " << ls << " = " << ce << " - 1, " << le << " = " << ce << ";\n";
+                break;
+            case OP2G_ON_INTERIOR_FACETS:
+                if (S.loop.extruded_periodic)
+                    o << ind << "const int " << ls << " = " << cs << ", " << le << " = " << ce << ";\n";
+                else
+                    o << ind << "const int " << ls << " = " << cs << ", " << le << " = " << ce
+                      << " - 1;\n";
+                break;
+            default:
+                o << ind << "const int " << ls << " = " << cs << ", " << le << " = " << ce << ";\n";
+        }
+    }
+
+    // Pack, call, unpack for one iteration (entity n, and layer when extruded).
+    void emit_body(const std::string &J, bool warp, bool plain) {
+        std::ostringstream &O = o;
+        std::vector<bool> used = used_maps();
+        // expand used to the plain maps that supply rows
+        std::vector<bool> need_row(S.maps.size(), false);
+        for (size_t m = 0; m < S.maps.size(); ++m) {
+            if (!used[m]) continue;
+            const MapInfo &mi = S.maps[m];
+            if (mi.kind == OP2G_MAP_PLAIN) need_row[m] = true;
+            else if (mi.kind == OP2G_MAP_PERMUTED) need_row[mi.base] = true;
+        }
+        for (size_t m = 0; m < S.maps.size(); ++m)
+            if (need_row[m]) emit_plain_row((int)m, "n", J);
+        for (size_t m = 0; m < S.maps.size(); ++m)
+            if (used[m]) emit_index_arrays((int)m, J);
+
+        // Packs (pyop2/codegen/builder.py:240-300, 303-365, 531-552)
+        std::vector<std::string> kargs;
+        for (size_t a = 0; a < S.args.size(); ++a) {
+            const ArgInfo &A = S.args[a];
+            const char *T = ctype_of(A.d.dtype);
+            const std::string an = std::to_string(a);
+            if (A.d.kind == OP2G_ARG_PASSTHROUGH) {
+                kargs.push_back("op2g::ptr((" + std::string(T) + " *)p.ptr[" +
+                                std::to_string(A.slot) + "])");
+            } else if (A.d.kind == OP2G_ARG_GLOBAL) {
+                if (A.d.access == OP2G_READ) {
+                    kargs.push_back("op2g::ptr((" + std::string(T) + " *)p.ptr[" +
+                                    std::to_string(A.slot) + "])");
+                } else {
+                    O << J << T << " g" << an << "[" << A.d.dim << "];\n";
+                    if (A.d.access == OP2G_INC)
+                        O << J << "for (int j = 0; j < " << A.d.dim << "; ++j) g" << an << "[j] = ("
+                          << T << ")0;\n";
+                    else
+                        O << J << "for (int j = 0; j < " << A.d.dim << "; ++j) g" << an
+                          << "[j] = gacc" << an << "[j];\n";
+                    kargs.push_back("op2g::ptr(g" + an + ")");
+                }
+            } else if (A.d.kind == OP2G_ARG_DAT) {
+                const int D = A.d.dim;
+                if (A.d.map < 0) {
+                    // direct: pointer into the Dat (pyop2/codegen/builder.py:367-377)
+                    kargs.push_back("op2g::ptr((" + std::string(T) + " *)p.ptr[" +
+                                    std::to_string(A.slot) + "] + n * " + std::to_string(D) + ")");
+                    continue;
+                }
+                const int ar = S.maps[A.d.map].arity;
+                const int tot = nf * ar * D;
+                const bool decl_outside = warp && A.d.access == OP2G_INC;
+                if (!decl_outside) O << J << T << " t" << an << "[" << tot << "];\n";
+                if (A.d.access == OP2G_INC || A.d.access == OP2G_WRITE) {
+                    O << J << "#pragma unroll\n";
+                    O << J << "for (int k = 0; k < " << tot << "; ++k) t" << an << "[k] = (" << T
+                      << ")0;\n";
+                } else {
+                    O << J << "{ const " << T << " *d_ = (const " << T << " *)p.ptr[" << A.slot
+                      << "];\n";
+                    for (int f = 0; f < nf; ++f) {
+                        O << J << "#pragma unroll\n";
+                        O << J << "  for (int i = 0; i < " << ar << "; ++i) {\n";
+                        O << J << "    const int x_ = " << idx_arr(A.d.map, f) << "[i];\n";
+                        O << J << "#pragma unroll\n";
+                        O << J << "    for (int j = 0; j < " << D << "; ++j) t" << an << "[("
+                          << f * ar << " + i) * " << D << " + j] = x_ >= 0 ? d_[(long long)x_ * "
+                          << D << " + j] : (" << T << ")0;\n";
+                        O << J << "  }\n";
+                    }
+                    O << J << "}\n";
+                }
+                kargs.push_back("op2g::ptr(t" + an + ")");
+            } else if (A.d.kind == OP2G_ARG_MAT) {
+                const int ra = S.maps[A.d.map].arity, ca = S.maps[A.d.cmap].arity;
+                const int tot = nf * ra * A.d.rdim * nf * ca * A.d.cdim;
+                O << J << T << " t" << an << "[" << tot << "];\n";
+                O << J << "#pragma unroll\n";
+                O << J << "for (int k = 0; k < " << tot << "; ++k) t" << an << "[k] = (" << T
+                  << ")0;\n";
+                kargs.push_back("op2g::ptr(t" + an + ")");
+            }
+        }
+        if (S.loop.pass_layer_arg) kargs.push_back("layer");
+        // Call (pyop2/codegen/builder.py:964-977)
+        O << J << S.kernel_name << "(";
+        for (size_t i = 0; i < kargs.size(); ++i) O << (i ? ", " : "") << kargs[i];
+        O << ");\n";
+
+        // Unpacks (pyop2/codegen/builder.py:283-300, 386-410, 554-606)
+        for (size_t a = 0; a < S.args.size(); ++a) {
+            const ArgInfo &A = S.args[a];
+            const char *T = ctype_of(A.d.dtype);
+            const std::string an = std::to_string(a);
+            if (A.d.kind == OP2G_ARG_GLOBAL) {
+                if (A.d.access == OP2G_INC)
+                    O << J << "for (int j = 0; j < " << A.d.dim << "; ++j) gacc" << an << "[j] += g"
+                      << an << "[j];\n";
+                else if (A.d.access == OP2G_MIN)
+                    O << J << "for (int j = 0; j < " << A.d.dim << "; ++j) gacc" << an
+                      << "[j] = op2g::vmin(gacc" << an << "[j], g" << an << "[j]);\n";
+                else if (A.d.access == OP2G_MAX)
+                    O << J << "for (int j = 0; j < " << A.d.dim << "; ++j) gacc" << an
+                      << "[j] = op2g::vmax(gacc" << an << "[j], g" << an << "[j]);\n";
+            } else if (A.d.kind == OP2G_ARG_DAT && A.d.map >= 0 && A.d.access != OP2G_READ) {
+                const int ar = S.maps[A.d.map].arity;
+                const int D = A.d.dim;
+                if (warp && A.d.access == OP2G_INC) {
+                    for (int f = 0; f < nf; ++f)
+                        O << J << "for (int i = 0; i < " << ar << "; ++i) ti" << an << "[" << f * ar
+                          << " + i] = " << idx_arr(A.d.map, f) << "[i];\n";
+                    continue;  // scattered after the active block
+                }
+                O << J << "{ " << T << " *d_ = (" << T << " *)p.ptr[" << A.slot << "];\n";
+                for (int f = 0; f < nf; ++f) {
+                    O << J << "#pragma unroll\n";
+                    O << J << "  for (int i = 0; i < " << ar << "; ++i) {\n";
+                    O << J << "    const int x_ = " << idx_arr(A.d.map, f) << "[i];\n";
+                    O << J << "    if (x_ < 0) continue;\n";
+                    O << J << "#pragma unroll\n";
+                    O << J << "    for (int j = 0; j < " << D << "; ++j) {\n";
+                    std::string dst = "d_[(long long)x_ * " + std::to_string(D) + " + j]";
+                    std::string src = "t" + an + "[(" + std::to_string(f * ar) + " + i) * " +
+                                      std::to_string(D) + " + j]";
+                    switch (A.d.access) {
+                        case OP2G_INC:
+                            if (plain) O << J << "      " << dst << " += " << src << ";\n";
+                            else O << J << "      op2g::atomic_inc(&" << dst << ", " << src << ");\n";
+                            break;
+                        case OP2G_MIN:
+                            if (plain) O << J << "      " << dst << " = op2g::vmin(" << dst << ", " << src << ");\n";
+                            else O << J << "      op2g::atomic_min(&" << dst << ", " << src << ");\n";
+                            break;
+                        case OP2G_MAX:
+                            if (plain) O << J << "      " << dst << " = op2g::vmax(" << dst << ", " << src << ");\n";
+                            else O << J << "      op2g::atomic_max(&" << dst << ", " << src << ");\n";
+                            break;
+                        default:  // WRITE, RW
+                            O << J << "      " << dst << " = " << src << ";\n";
+                    }
+                    O << J << "    }\n";
+                    O << J << "  }\n";
+                }
+                O << J << "}\n";
+            } else if (A.d.kind == OP2G_ARG_MAT) {
+                // MatSetValuesBlockedLocal(ADD|INSERT) on block-CSR storage.
+                const int ra = S.maps[A.d.map].arity, ca = S.maps[A.d.cmap].arity;
+                const int RD = A.d.rdim, CD = A.d.cdim;
+                const int ncolv = nf * ca * CD;
+                O << J << "{ " << T << " *v_ = (" << T << " *)p.ptr[" << A.slot << "];\n";
+                O << J << "  const long long *rp_ = (const long long *)p.ptr[" << A.slot + 1 << "];\n";
+                O << J << "  const int *ci_ = (const int *)p.ptr[" << A.slot + 2 << "];\n";
+                for (int fr = 0; fr < nf; ++fr)
+                    for (int fc = 0; fc < nf; ++fc) {
+                        O << J << "  for (int i = 0; i < " << ra << "; ++i) {\n";
+                        O << J << "    const int r_ = " << idx_arr(A.d.map, fr) << "[i];\n";
+                        O << J << "    if (r_ < 0) continue;\n";
+                        O << J << "    for (int j = 0; j < " << ca << "; ++j) {\n";
+                        O << J << "      const int c_ = " << idx_arr(A.d.cmap, fc) << "[j];\n";
+                        O << J << "      if (c_ < 0) continue;\n";
+                        O << J << "      const long long q_ = op2g::bcsr_find(rp_, ci_, r_, c_);\n";
+                        O << J << "      if (q_ < 0) { op2g::set_err(p.err, OP2G_DEVERR_NEW_NONZERO); continue; }\n";
+                        O << J << "#pragma unroll\n";
+                        O << J << "      for (int ri = 0; ri < " << RD << "; ++ri)\n";
+                        O << J << "#pragma unroll\n";
+                        O << J << "        for (int cj = 0; cj < " << CD << "; ++cj) {\n";
+                        O << J << "          const " << T << " w_ = t" << an << "[((" << fr * ra
+                          << " + i) * " << RD << " + ri) * " << ncolv << " + (" << fc * ca
+                          << " + j) * " << CD << " + cj];\n";
+                        std::string dst = "v_[q_ * " + std::to_string(RD * CD) + " + ri * " +
+                                          std::to_string(CD) + " + cj]";
+                        if (A.d.access == OP2G_INC) {
+                            if (plain) O << J << "          " << dst << " += w_;\n";
+                            else O << J << "          op2g::atomic_inc(&" << dst << ", w_);\n";
+                        } else {
+                            O << J << "          " << dst << " = w_;\n";
+                        }
+                        O << J << "        }\n";
+                        O << J << "    }\n";
+                        O << J << "  }\n";
+                    }
+                O << J << "}\n";
+            }
+        }
+    }
+};
+
+// Validate a signature; returns an error message or "".
+std::string validate_signature(const Signature &S) {
+    if (S.kernel_name.empty()) return "empty kernel name";
+    for (size_t m = 0; m < S.maps.size(); ++m) {
+        const MapInfo &mi = S.maps[m];
+        if (mi.arity <= 0) return "map " + std::to_string(m) + ": arity must be positive";
+        if (mi.kind == OP2G_MAP_PERMUTED) {
+            if (mi.base < 0 || mi.base >= (int)S.maps.size() || S.maps[mi.base].kind != OP2G_MAP_PLAIN)
+                return "map " + std::to_string(m) + ": permuted map must refer to a plain map";
+            if ((int)mi.permutation.size() != mi.arity) return "permutation length != arity";
+        } else if (mi.kind == OP2G_MAP_COMPOSED) {
+            if (mi.ncomposed < 2 || mi.ncomposed > OP2G_MAX_COMPOSED) return "bad composed chain";
+            for (int k = 0; k < mi.ncomposed; ++k) {
+                int c = mi.composed[k];
+                if (c < 0 || c >= (int)S.maps.size() || S.maps[c].kind == OP2G_MAP_COMPOSED)
+                    return "composed chain must refer to plain or permuted maps (flatten first)";
+                if (k >= 1 && S.maps[c].arity != 1) return "inner maps of a composition need arity 1";
+            }
+        } else if (mi.kind != OP2G_MAP_PLAIN) {
+            return "unknown map kind";
+        }
+    }
+    for (size_t a = 0; a < S.args.size(); ++a) {
+        const op2g_arg_desc &d = S.args[a].d;
+        std::string an = "argument " + std::to_string(a) + ": ";
+        if (!ctype_of(d.dtype)) return an + "unknown dtype";
+        if (d.access < OP2G_READ || d.access > OP2G_MAX) return an + "unknown access";
+        switch (d.kind) {
+            case OP2G_ARG_DAT:
+                if (d.dim <= 0) return an + "dim must be positive";
+                if (d.map >= (int)S.maps.size()) return an + "map index out of range";
+                if (d.map >= 0 && (d.access == OP2G_INC || d.access == OP2G_MIN || d.access == OP2G_MAX) &&
+                    !atomic_capable(d.dtype) && S.loop.scatter != OP2G_SCATTER_PLAIN)
+                    return an + "INC/MIN/MAX through a map needs a 32- or 64-bit element type";
+                break;
+            case OP2G_ARG_GLOBAL:
+                if (d.dim <= 0) return an + "dim must be positive";
+                if (d.access != OP2G_READ && d.access != OP2G_INC && d.access != OP2G_MIN &&
+                    d.access != OP2G_MAX)
+                    return an + "Globals take READ, INC, MIN or MAX";
+                if (d.access != OP2G_READ && !atomic_capable(d.dtype))
+                    return an + "Global reductions need a 32- or 64-bit element type";
+                break;
+            case OP2G_ARG_MAT:
+                if (d.access != OP2G_INC && d.access != OP2G_WRITE) return an + "Mats take INC or WRITE";
+                if (d.map < 0 || d.cmap < 0 || d.map >= (int)S.maps.size() || d.cmap >= (int)S.maps.size())
+                    return an + "Mat needs row and column maps";
+                if (d.rdim <= 0 || d.cdim <= 0) return an + "bad Mat block dims";
+                if (!atomic_capable(d.dtype)) return an + "Mat values need a 32- or 64-bit type";
+                break;
+            case OP2G_ARG_PASSTHROUGH:
+                break;
+            default:
+                return an + "unknown kind";
+        }
+    }
+    if (S.loop.extruded && !S.loop.constant_layers && S.loop.scatter == OP2G_SCATTER_WARP)
+        return "warp-aggregated scatter needs constant layers";
+    if (S.loop.pass_layer_arg && !S.loop.extruded) return "layer argument needs an extruded loop";
+    return "";
+}
+
+std::string generate_source(const Signature &S) {
+    Gen g(S);
+    return g.emit();
+}
+
+}  // namespace op2g

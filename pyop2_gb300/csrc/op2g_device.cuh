@@ -1,0 +1,182 @@
+// op2g_device.cuh -- device-side building blocks of the generated par_loop
+// wrappers.  This header is compiled by NVRTC together with the user's local
+// kernel and the per-signature glue that op2g_codegen.cpp writes.  It holds the
+// hand-written parts: typed pointers that convert to whatever pointer type the
+// user's C kernel declares, the INC/MIN/MAX atomics for every element type,
+// warp-level reductions for op2.Global arguments, warp-aggregated scatter and
+// the block-CSR insertion used for op2.Mat arguments.
+//
+// Semantics follow the reference's sequential wrapper: pack, call, unpack
+// (pyop2/codegen/builder.py:240-300 GlobalPack, :303-410 DatPack,
+// :501-606 MatPack).
+#pragma once
+
+typedef signed char int8_t;
+typedef unsigned char uint8_t;
+typedef short int16_t;
+typedef unsigned short uint16_t;
+typedef int int32_t;
+typedef unsigned int uint32_t;
+typedef long long int64_t;
+typedef unsigned long long uint64_t;
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+#ifndef NULL
+#define NULL 0
+#endif
+
+namespace op2g {
+
+// Kernel-argument pointer.  The reference passes every argument to the C
+// kernel through a void*-typed ctypes call (pyop2/global_kernel.py:410-417),
+// so a kernel may declare any pointer type for any argument; C++ would reject
+// the implicit conversions, so the wrapper passes this proxy instead.
+template <class T>
+struct anyptr {
+    T *p;
+    __device__ __forceinline__ explicit anyptr(T *q) : p(q) {}
+    template <class U>
+    __device__ __forceinline__ operator U *() const { return (U *)p; }
+};
+template <class T>
+__device__ __forceinline__ anyptr<T> ptr(T *p) { return anyptr<T>(p); }
+
+__device__ __forceinline__ void set_err(int *err, int bit) {
+    if (err) atomicOr(err, bit);
+}
+
+// ---------------------------------------------------------------- INC
+__device__ __forceinline__ void atomic_inc(double *a, double v) { atomicAdd(a, v); }
+__device__ __forceinline__ void atomic_inc(float *a, float v) { atomicAdd(a, v); }
+__device__ __forceinline__ void atomic_inc(int *a, int v) { atomicAdd(a, v); }
+__device__ __forceinline__ void atomic_inc(unsigned *a, unsigned v) { atomicAdd(a, v); }
+__device__ __forceinline__ void atomic_inc(long long *a, long long v) {
+    atomicAdd((unsigned long long *)a, (unsigned long long)v);
+}
+__device__ __forceinline__ void atomic_inc(unsigned long long *a, unsigned long long v) {
+    atomicAdd(a, v);
+}
+
+// ------------------------------------------------------------ MIN/MAX
+__device__ __forceinline__ void atomic_min(int *a, int v) { atomicMin(a, v); }
+__device__ __forceinline__ void atomic_max(int *a, int v) { atomicMax(a, v); }
+__device__ __forceinline__ void atomic_min(unsigned *a, unsigned v) { atomicMin(a, v); }
+__device__ __forceinline__ void atomic_max(unsigned *a, unsigned v) { atomicMax(a, v); }
+__device__ __forceinline__ void atomic_min(long long *a, long long v) { atomicMin(a, v); }
+__device__ __forceinline__ void atomic_max(long long *a, long long v) { atomicMax(a, v); }
+__device__ __forceinline__ void atomic_min(unsigned long long *a, unsigned long long v) {
+    atomicMin(a, v);
+}
+__device__ __forceinline__ void atomic_max(unsigned long long *a, unsigned long long v) {
+    atomicMax(a, v);
+}
+// Floating point MIN/MAX: compare-and-swap on the bit pattern.  The loop ends
+// as soon as the stored value is already no larger (smaller) than v, so it
+// performs at most one successful swap per distinct improvement.
+__device__ __forceinline__ void atomic_min(double *a, double v) {
+    unsigned long long *p = (unsigned long long *)a;
+    unsigned long long old = *p;
+    while (__longlong_as_double(old) > v) {
+        unsigned long long seen = atomicCAS(p, old, __double_as_longlong(v));
+        if (seen == old) break;
+        old = seen;
+    }
+}
+__device__ __forceinline__ void atomic_max(double *a, double v) {
+    unsigned long long *p = (unsigned long long *)a;
+    unsigned long long old = *p;
+    while (__longlong_as_double(old) < v) {
+        unsigned long long seen = atomicCAS(p, old, __double_as_longlong(v));
+        if (seen == old) break;
+        old = seen;
+    }
+}
+__device__ __forceinline__ void atomic_min(float *a, float v) {
+    int *p = (int *)a;
+    int old = *p;
+    while (__int_as_float(old) > v) {
+        int seen = atomicCAS(p, old, __float_as_int(v));
+        if (seen == old) break;
+        old = seen;
+    }
+}
+__device__ __forceinline__ void atomic_max(float *a, float v) {
+    int *p = (int *)a;
+    int old = *p;
+    while (__int_as_float(old) < v) {
+        int seen = atomicCAS(p, old, __float_as_int(v));
+        if (seen == old) break;
+        old = seen;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ T vmin(T a, T b) { return b < a ? b : a; }
+template <class T>
+__device__ __forceinline__ T vmax(T a, T b) { return a < b ? b : a; }
+
+// ------------------------------------------------- warp reductions (Globals)
+template <class T>
+__device__ __forceinline__ T shfl_xor(T v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) v += shfl_xor(v, m);
+    return v;
+}
+template <class T>
+__device__ __forceinline__ T warp_min(T v) {
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) v = vmin(v, shfl_xor(v, m));
+    return v;
+}
+template <class T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) v = vmax(v, shfl_xor(v, m));
+    return v;
+}
+
+// ------------------------------------------- warp-aggregated INC scatter
+// All 32 lanes call this together (inactive lanes pass valid = false).  Lanes
+// whose target address is equal form a group (__match_any_sync); the group's
+// lowest lane sums the members' values in lane order with shuffles and issues
+// one atomic.  The number of shuffle rounds is the size of the largest group.
+template <class T>
+__device__ __forceinline__ void warp_agg_inc(T *addr, T v, bool valid) {
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned long long key = valid ? (unsigned long long)addr : 0ull;
+    unsigned peers = __match_any_sync(0xffffffffu, key);
+    const unsigned leader = __ffs(peers) - 1;
+    const int gsize = __popc(peers);
+    const int rounds = __reduce_max_sync(0xffffffffu, (unsigned)gsize);
+    T acc = v;
+    unsigned rest = peers & ~(1u << lane);   // members other than me
+    for (int r = 1; r < rounds; ++r) {
+        int src = rest ? (__ffs(rest) - 1) : (int)lane;
+        T w = __shfl_sync(0xffffffffu, v, src);
+        if (lane == leader && rest) acc += w;
+        rest &= rest - 1u;
+    }
+    if (valid && lane == leader) atomic_inc(addr, acc);
+}
+
+// ------------------------------------------------------- block-CSR insertion
+// Position of column `col` in block row `row` (binary search over the sorted
+// unique column list), or -1 if absent.
+__device__ __forceinline__ long long bcsr_find(const long long *__restrict__ rowptr,
+                                               const int *__restrict__ colidx, int row, int col) {
+    long long lo = rowptr[row], hi = rowptr[row + 1] - 1;
+    while (lo <= hi) {
+        long long mid = (lo + hi) >> 1;
+        int c = colidx[mid];
+        if (c == col) return mid;
+        if (c < col) lo = mid + 1; else hi = mid - 1;
+    }
+    return -1;
+}
+
+}  // namespace op2g

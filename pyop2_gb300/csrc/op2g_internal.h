@@ -1,0 +1,47 @@
+// op2g_internal.h -- shared declarations of libop2g's C++ translation units.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "../../include/op2g.h"
+
+namespace op2g {
+
+// Thread-local error reporting behind op2g_last_error().
+op2g_status fail(op2g_status code, const std::string &msg);
+op2g_status cuda_fail(int err, const char *what);
+
+struct MapInfo {
+    int kind = OP2G_MAP_PLAIN;
+    int arity = 0;
+    int base = -1;
+    int ncomposed = 0;
+    int composed[OP2G_MAX_COMPOSED] = {0};
+    std::vector<int> offset, offset_quotient, permutation;
+};
+
+struct ArgInfo {
+    op2g_arg_desc d;
+    int slot = 0;  // first device-pointer slot
+};
+
+// Everything that determines the generated code of one wrapper.
+struct Signature {
+    std::string user_src, kernel_name;
+    op2g_loop_desc loop;
+    std::vector<ArgInfo> args;
+    std::vector<MapInfo> maps;
+    int nptrs = 0;          // argument slots + one slot per map
+    int map_slot0 = 0;      // first map slot
+    int block_size = 256;
+    int map_slot(int m) const { return map_slot0 + m; }
+};
+
+std::string validate_signature(const Signature &S);
+std::string generate_source(const Signature &S);
+
+// Text of op2g_device.cuh, embedded at build time.
+extern const char *const device_header_src;
+
+}  // namespace op2g

@@ -1,0 +1,946 @@
+// op2g_kernels.cu -- hand-written sm_103a kernels behind the non-par_loop parts
+// of the C ABI: the Map -> block-CSR sparsity build, block-CSR matrix
+// utilities, greedy colouring, a prefix scan shared by them, and the FP64
+// throughput probe used as the second roofline ceiling.
+//
+// Sparsity semantics restate pyop2/sparsity.pyx:178-405 (fill_with_zeros):
+// every (row map, column map, iteration region) triple inserts the block
+// rmap[e,:] x cmap[e,:] for every iterated entity (and layer), composed maps
+// are resolved innermost-last and skipped when negative (:249-259, :270-281),
+// extruded maps add offset * ((layer + k + q) % nl - q % nl) (:361-374), the
+// diagonal (i, i) is added for i < min(nrows, ncols) when requested
+// (:214-219), and negative indices are ignored as PETSc's MatSetValues does.
+// The result is PETSc's preallocated pattern: per row, the sorted set of
+// distinct columns.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstring>
+#include <vector>
+
+#include "op2g_internal.h"
+
+namespace {
+
+constexpr int MAXAR = 128;  // arity bound for extruded offset tables
+
+struct PairDev {
+    const int *rmap, *cmap;
+    int rarity, carity;
+    long long nent;
+    int region;
+    int nrc, ncc;
+    const int *rc[OP2G_MAX_COMPOSED];
+    const int *cc[OP2G_MAX_COMPOSED];
+    int has_roff, has_coff;
+    int tr, tc;          // rows / columns of one virtual cell (x2 for interior facets)
+    long long nvirt;     // virtual cells (entities x layer slots)
+    int roff[MAXAR], coff[MAXAR], rq[MAXAR], cq[MAXAR];
+};
+
+struct SpDev {
+    long long nrows, ncols;
+    int set_diag, extruded, constant_layers, periodic;
+    const int *layers;
+    int slots;
+    int *err;
+};
+
+#define CK(call)                                                   \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return op2g::cuda_fail(e_, #call); \
+    } while (0)
+
+__device__ __forceinline__ bool vcell(const SpDev &S, const PairDev &P, long long v,
+                                      long long &rent, long long &cent, int &layer, int &nl) {
+    const long long e = S.extruded ? v / S.slots : v;
+    const int l = S.extruded ? (int)(v - e * S.slots) : 0;
+    rent = e;
+    cent = e;
+    for (int i = 0; i < P.nrc; ++i) {
+        rent = P.rc[P.nrc - 1 - i][rent];
+        if (rent < 0) return false;
+    }
+    for (int i = 0; i < P.ncc; ++i) {
+        cent = P.cc[P.ncc - 1 - i][cent];
+        if (cent < 0) return false;
+    }
+    layer = 0;
+    nl = 1;
+    if (S.extruded) {
+        const int *L = S.constant_layers ? S.layers : S.layers + 2 * e;
+        int ls = L[0], le = L[1] - 1;
+        nl = le - ls;
+        if (P.region == OP2G_ON_BOTTOM) le = ls + 1;
+        else if (P.region == OP2G_ON_TOP) ls = le - 1;
+        else if (P.region == OP2G_ON_INTERIOR_FACETS && !S.periodic) le = le - 1;
+        layer = ls + l;
+        if (layer >= le) return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ int ext_term(int layer, int k, int q, int nl) {
+    const int eff = layer + k + q;
+    return nl > 0 ? (eff % nl - q % nl) : (eff - q);
+}
+
+__device__ __forceinline__ int row_of(const SpDev &S, const PairDev &P, long long rent, int i,
+                                      int layer, int nl) {
+    const int k = i / P.rarity, ir = i - k * P.rarity;
+    int b = P.rmap[rent * P.rarity + ir];
+    if (S.extruded && P.has_roff) b += P.roff[ir] * ext_term(layer, k, P.rq[ir], nl);
+    return b;
+}
+
+__device__ __forceinline__ int col_of(const SpDev &S, const PairDev &P, long long cent, int j,
+                                      int layer, int nl) {
+    const int k = j / P.carity, jr = j - k * P.carity;
+    int b = P.cmap[cent * P.carity + jr];
+    if (S.extruded && P.has_coff) b += P.coff[jr] * ext_term(layer, k, P.cq[jr], nl);
+    return b;
+}
+
+// Row -> virtual-cell incidence: counts (pass 0) or fills (pass 1).
+__global__ void k_incidence(SpDev S, const PairDev *__restrict__ pairs, int p, int pass,
+                            long long *__restrict__ cnt, int *__restrict__ cand,
+                            int *__restrict__ fillpos, long long *__restrict__ tlist) {
+    const PairDev &P = pairs[p];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < P.nvirt; v += stride) {
+        long long rent, cent;
+        int layer, nl;
+        if (!vcell(S, P, v, rent, cent, layer, nl)) continue;
+        for (int i = 0; i < P.tr; ++i) {
+            const int r = row_of(S, P, rent, i, layer, nl);
+            if (r < 0) continue;
+            if (r >= S.nrows) {
+                atomicOr(S.err, OP2G_DEVERR_MAP_BOUNDS);
+                continue;
+            }
+            if (pass == 0) {
+                atomicAdd((unsigned long long *)&cnt[r], 1ull);
+                atomicAdd(&cand[r], P.tc);
+            } else {
+                const long long pos = cnt[r] + atomicAdd(&fillpos[r], 1);
+                tlist[pos] = ((long long)p << 56) | v;
+            }
+        }
+    }
+}
+
+__global__ void k_max_cand(const int *__restrict__ cand, long long n, int diag, int *out) {
+    int m = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        m = max(m, cand[i] + diag);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// One warp per row: gather candidate columns of every incident virtual cell
+// into shared memory, bitonic-sort them, count (pass 0) or write (pass 1) the
+// distinct ones.
+__global__ void k_rows(SpDev S, const PairDev *__restrict__ pairs,
+                       const long long *__restrict__ tptr, const long long *__restrict__ tlist,
+                       int cap, int pass, long long *__restrict__ rowcount,
+                       const long long *__restrict__ rowptr, int *__restrict__ colidx) {
+    extern __shared__ int smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    int *s = smem + warp * cap;
+    for (long long r = (long long)blockIdx.x * wpb + warp; r < S.nrows;
+         r += (long long)gridDim.x * wpb) {
+        const long long e0 = tptr[r], e1 = tptr[r + 1];
+        int n = 0;  // warp-uniform candidate count
+        for (long long eb = e0; eb < e1; eb += 32) {
+            const long long e = eb + lane;
+            int cnt = 0;
+            long long cent = 0;
+            int layer = 0, nl = 1;
+            const PairDev *P = nullptr;
+            if (e < e1) {
+                const long long code = tlist[e];
+                P = &pairs[(int)(code >> 56)];
+                long long rent;
+                if (vcell(S, *P, code & ((1ll << 56) - 1), rent, cent, layer, nl)) cnt = P->tc;
+            }
+            int off = cnt;  // inclusive warp scan
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, off, o);
+                if (lane >= o) off += t;
+            }
+            const int tot = __shfl_sync(0xffffffffu, off, 31);
+            off -= cnt;
+            for (int j = 0; j < cnt; ++j) {
+                int c = col_of(S, *P, cent, j, layer, nl);
+                if (c >= S.ncols) {
+                    atomicOr(S.err, OP2G_DEVERR_MAP_BOUNDS);
+                    c = -1;
+                }
+                if (n + off + j < cap) s[n + off + j] = c < 0 ? INT_MAX : c;
+            }
+            n += tot;
+        }
+        if (S.set_diag && r < S.ncols) {
+            if (lane == 0 && n < cap) s[n] = (int)r;
+            n += 1;
+        }
+        if (n > cap) {  // cannot happen: cap >= the largest candidate count
+            if (lane == 0) atomicOr(S.err, OP2G_DEVERR_CAPACITY);
+            continue;
+        }
+        int P2 = 1;
+        while (P2 < n) P2 <<= 1;
+        for (int i = n + lane; i < P2; i += 32) s[i] = INT_MAX;
+        __syncwarp();
+        for (int k = 2; k <= P2; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = lane; i < P2; i += 32) {
+                    const int ixj = i ^ j;
+                    if (ixj > i) {
+                        const int a = s[i], b = s[ixj];
+                        const bool up = (i & k) == 0;
+                        if ((a > b) == up) {
+                            s[i] = b;
+                            s[ixj] = a;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        long long run = 0;
+        const long long out0 = pass ? rowptr[r] : 0;
+        for (int i0 = 0; i0 < P2; i0 += 32) {
+            const int i = i0 + lane;
+            const int x = i < P2 ? s[i] : INT_MAX;
+            const bool keep = x != INT_MAX && (i == 0 || s[i - 1] != x);
+            const unsigned b = __ballot_sync(0xffffffffu, keep);
+            if (pass && keep) colidx[out0 + run + __popc(b & ((1u << lane) - 1u))] = x;
+            run += __popc(b);
+        }
+        if (!pass && lane == 0) rowcount[r] = run;
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------- scan
+constexpr int SCAN_T = 1024, SCAN_V = 4, SCAN_B = SCAN_T * SCAN_V;
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_block(long long *__restrict__ d, long long n,
+                                                       long long *__restrict__ sums) {
+    __shared__ long long ws[32];
+    const long long b0 = (long long)blockIdx.x * SCAN_B + (long long)threadIdx.x * SCAN_V;
+    long long v[SCAN_V], t = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_V; ++k) {
+        v[k] = (b0 + k < n) ? d[b0 + k] : 0;
+        t += v[k];
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    long long inc = t;
+    for (int o = 1; o < 32; o <<= 1) {
+        long long y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) ws[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        long long x = ws[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        ws[lane] = x;
+    }
+    __syncthreads();
+    long long run = inc - t + (w ? ws[w - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < SCAN_V; ++k) {
+        if (b0 + k < n) d[b0 + k] = run;
+        run += v[k];
+    }
+    if (sums && threadIdx.x == SCAN_T - 1) sums[blockIdx.x] = run;
+}
+
+__global__ void k_scan_add(long long *__restrict__ d, long long n, const long long *__restrict__ offs) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) d[i] += offs[i / SCAN_B];
+}
+
+size_t scan_tmp_elems(long long n) {
+    size_t tot = 0;
+    while (n > SCAN_B) {
+        n = (n + SCAN_B - 1) / SCAN_B;
+        tot += (size_t)n;
+    }
+    return tot + 1;
+}
+
+// Exclusive in-place scan of d[0..n); tmp needs scan_tmp_elems(n) elements.
+op2g_status scan_exclusive(long long *d, long long n, long long *tmp, cudaStream_t st) {
+    if (n <= 0) return OP2G_OK;
+    if (n <= SCAN_B) {
+        k_scan_block<<<1, SCAN_T, 0, st>>>(d, n, nullptr);
+        CK(cudaGetLastError());
+        return OP2G_OK;
+    }
+    const long long nb = (n + SCAN_B - 1) / SCAN_B;
+    k_scan_block<<<(unsigned)nb, SCAN_T, 0, st>>>(d, n, tmp);
+    CK(cudaGetLastError());
+    op2g_status s = scan_exclusive(tmp, nb, tmp + nb, st);
+    if (s != OP2G_OK) return s;
+    k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, n, tmp);
+    CK(cudaGetLastError());
+    return OP2G_OK;
+}
+
+// ------------------------------------------------------- sparsity driver
+struct SpLayout {
+    size_t off_cnt, off_cand, off_fill, off_tlist, off_scan, off_pairs, off_misc, total;
+    long long ninc;
+};
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+op2g_status sp_prepare(const op2g_sparsity_desc *d, std::vector<PairDev> &pairs, SpDev &S,
+                       SpLayout &L) {
+    if (!d || d->npairs < 0 || (d->npairs && !d->pairs))
+        return op2g::fail(OP2G_ERR_INVALID, "bad sparsity descriptor");
+    if (d->nrows < 0 || d->ncols < 0 || d->nrows > INT_MAX || d->ncols > INT_MAX)
+        return op2g::fail(OP2G_ERR_INVALID, "row/column counts must fit int32");
+    if (d->npairs > 255) return op2g::fail(OP2G_ERR_INVALID, "at most 255 map pairs");
+    memset(&S, 0, sizeof S);
+    S.nrows = d->nrows;
+    S.ncols = d->ncols;
+    S.set_diag = d->set_diag;
+    S.extruded = d->extruded;
+    S.constant_layers = d->constant_layers;
+    S.periodic = d->extruded_periodic;
+    S.layers = d->layers;
+    S.slots = d->extruded ? (d->layer_slots > 0 ? d->layer_slots : 1) : 1;
+    if (d->extruded && !d->layers) return op2g::fail(OP2G_ERR_INVALID, "extruded sparsity needs layers");
+    L.ninc = 0;
+    pairs.resize(d->npairs);
+    for (int p = 0; p < d->npairs; ++p) {
+        const op2g_sparsity_pair &q = d->pairs[p];
+        PairDev &P = pairs[p];
+        memset(&P, 0, sizeof P);
+        if (!q.rmap || !q.cmap || q.rarity <= 0 || q.carity <= 0 || q.nent < 0)
+            return op2g::fail(OP2G_ERR_INVALID, "bad map pair");
+        if (q.nrcomposed < 0 || q.nrcomposed > OP2G_MAX_COMPOSED || q.nccomposed < 0 ||
+            q.nccomposed > OP2G_MAX_COMPOSED)
+            return op2g::fail(OP2G_ERR_INVALID, "bad composed chain");
+        P.rmap = q.rmap;
+        P.cmap = q.cmap;
+        P.rarity = q.rarity;
+        P.carity = q.carity;
+        P.nent = q.nent;
+        P.region = q.region ? q.region : OP2G_ALL;
+        P.nrc = q.nrcomposed;
+        P.ncc = q.nccomposed;
+        for (int k = 0; k < OP2G_MAX_COMPOSED; ++k) {
+            P.rc[k] = q.rcomposed[k];
+            P.cc[k] = q.ccomposed[k];
+        }
+        const int ih = (d->extruded && P.region == OP2G_ON_INTERIOR_FACETS) ? 2 : 1;
+        P.tr = ih * q.rarity;
+        P.tc = ih * q.carity;
+        if (d->extruded) {
+            if (q.rarity > MAXAR || q.carity > MAXAR)
+                return op2g::fail(OP2G_ERR_UNSUPPORTED, "extruded sparsity supports arity <= 128");
+            if (!q.roffset || !q.coffset)
+                return op2g::fail(OP2G_ERR_INVALID, "extruded sparsity needs map offsets");
+            P.has_roff = P.has_coff = 1;
+            for (int i = 0; i < q.rarity; ++i) {
+                P.roff[i] = q.roffset[i];
+                P.rq[i] = q.roffset_quotient ? q.roffset_quotient[i] : 0;
+            }
+            for (int i = 0; i < q.carity; ++i) {
+                P.coff[i] = q.coffset[i];
+                P.cq[i] = q.coffset_quotient ? q.coffset_quotient[i] : 0;
+            }
+        }
+        P.nvirt = q.nent * S.slots;
+        L.ninc += P.nvirt * P.tr;
+    }
+    const long long n1 = d->nrows + 1;
+    size_t off = 0;
+    L.off_cnt = off; off = align256(off + sizeof(long long) * n1);
+    L.off_cand = off; off = align256(off + sizeof(int) * (d->nrows + 1));
+    L.off_fill = off; off = align256(off + sizeof(int) * (d->nrows + 1));
+    L.off_tlist = off; off = align256(off + sizeof(long long) * (L.ninc > 0 ? L.ninc : 1));
+    L.off_scan = off; off = align256(off + sizeof(long long) * scan_tmp_elems(n1));
+    L.off_pairs = off; off = align256(off + sizeof(PairDev) * (d->npairs ? d->npairs : 1));
+    L.off_misc = off; off = align256(off + 64);
+    L.total = off;
+    return OP2G_OK;
+}
+
+int sms_of_current() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+op2g_status sp_rows_launch(const SpDev &S, const PairDev *pd, const long long *tptr,
+                           const long long *tlist, int cap, int pass, long long *rowcount,
+                           const long long *rowptr, int *colidx, cudaStream_t st) {
+    if (S.nrows == 0) return OP2G_OK;
+    const size_t per = (size_t)cap * sizeof(int);
+    int wpb = (int)((48 * 1024) / per);
+    if (wpb > 8) wpb = 8;
+    if (wpb < 1) wpb = 1;
+    const size_t smem = per * wpb;
+    if (smem > 227 * 1024)
+        return op2g::fail(OP2G_ERR_CAPACITY, "a sparsity row has more than 58,000 candidate columns");
+    if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    long long blocks = (S.nrows + wpb - 1) / wpb;
+    const long long capb = (long long)sms_of_current() * 32;
+    if (blocks > capb) blocks = capb;
+    k_rows<<<(unsigned)blocks, 32 * wpb, smem, st>>>(S, pd, tptr, tlist, cap, pass, rowcount, rowptr,
+                                                     colidx);
+    CK(cudaGetLastError());
+    return OP2G_OK;
+}
+
+// State kept in the workspace between count and fill (the candidate capacity).
+struct SpMisc {
+    int max_cand;
+    int err;
+    int cap;
+};
+
+}  // namespace
+
+extern "C" {
+
+op2g_status op2g_sparsity_workspace(const op2g_sparsity_desc *d, size_t *bytes) {
+    std::vector<PairDev> pairs;
+    SpDev S;
+    SpLayout L;
+    op2g_status s = sp_prepare(d, pairs, S, L);
+    if (s != OP2G_OK) return s;
+    if (bytes) *bytes = L.total;
+    return OP2G_OK;
+}
+
+op2g_status op2g_sparsity_count(const op2g_sparsity_desc *d, void *ws, size_t ws_bytes,
+                                int64_t *rowptr, int64_t *nnz, void *stream) {
+    std::vector<PairDev> pairs;
+    SpDev S;
+    SpLayout L;
+    op2g_status s = sp_prepare(d, pairs, S, L);
+    if (s != OP2G_OK) return s;
+    if (!ws || ws_bytes < L.total) return op2g::fail(OP2G_ERR_INVALID, "workspace too small");
+    if (!rowptr) return op2g::fail(OP2G_ERR_INVALID, "rowptr is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    char *w = (char *)ws;
+    long long *cnt = (long long *)(w + L.off_cnt);
+    int *cand = (int *)(w + L.off_cand);
+    int *fill = (int *)(w + L.off_fill);
+    long long *tlist = (long long *)(w + L.off_tlist);
+    long long *scan = (long long *)(w + L.off_scan);
+    PairDev *pd = (PairDev *)(w + L.off_pairs);
+    SpMisc *misc = (SpMisc *)(w + L.off_misc);
+    S.err = &misc->err;
+    const long long n1 = d->nrows + 1;
+    CK(cudaMemsetAsync(cnt, 0, sizeof(long long) * n1, st));
+    CK(cudaMemsetAsync(cand, 0, sizeof(int) * n1, st));
+    CK(cudaMemsetAsync(fill, 0, sizeof(int) * n1, st));
+    CK(cudaMemsetAsync(misc, 0, sizeof(SpMisc), st));
+    if (!pairs.empty())
+        CK(cudaMemcpyAsync(pd, pairs.data(), sizeof(PairDev) * pairs.size(), cudaMemcpyHostToDevice, st));
+    const long long capb = (long long)sms_of_current() * 16;
+    for (int pass = 0; pass < 2; ++pass) {
+        for (size_t p = 0; p < pairs.size(); ++p) {
+            long long nb = (pairs[p].nvirt + 255) / 256;
+            if (nb == 0) continue;
+            if (nb > capb) nb = capb;
+            k_incidence<<<(unsigned)nb, 256, 0, st>>>(S, pd, (int)p, pass, cnt, cand, fill, tlist);
+            CK(cudaGetLastError());
+        }
+        if (pass == 0) {
+            s = scan_exclusive(cnt, n1, scan, st);
+            if (s != OP2G_OK) return s;
+        }
+    }
+    if (d->nrows > 0) {
+        long long nb = (d->nrows + 255) / 256;
+        if (nb > capb) nb = capb;
+        k_max_cand<<<(unsigned)nb, 256, 0, st>>>(cand, d->nrows, d->set_diag ? 1 : 0, &misc->max_cand);
+        CK(cudaGetLastError());
+    }
+    SpMisc hm;
+    CK(cudaMemcpyAsync(&hm, misc, sizeof hm, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (hm.err & OP2G_DEVERR_MAP_BOUNDS)
+        return op2g::fail(OP2G_ERR_BOUNDS, "a map value is outside the row or column set");
+    int cap = 32;
+    while (cap < hm.max_cand) cap <<= 1;
+    CK(cudaMemcpyAsync(&misc->cap, &cap, sizeof(int), cudaMemcpyHostToDevice, st));
+    s = sp_rows_launch(S, pd, cnt, tlist, cap, 0, (long long *)rowptr, nullptr, nullptr, st);
+    if (s != OP2G_OK) return s;
+    CK(cudaMemsetAsync(rowptr + d->nrows, 0, sizeof(long long), st));
+    s = scan_exclusive((long long *)rowptr, n1, scan, st);
+    if (s != OP2G_OK) return s;
+    long long total = 0;
+    int err = 0;
+    CK(cudaMemcpyAsync(&total, rowptr + d->nrows, sizeof total, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&err, &misc->err, sizeof err, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (err & OP2G_DEVERR_MAP_BOUNDS)
+        return op2g::fail(OP2G_ERR_BOUNDS, "a map value is outside the row or column set");
+    if (err & OP2G_DEVERR_CAPACITY)
+        return op2g::fail(OP2G_ERR_CAPACITY, "sparsity row candidate capacity exceeded");
+    if (nnz) *nnz = total;
+    return OP2G_OK;
+}
+
+op2g_status op2g_sparsity_fill(const op2g_sparsity_desc *d, void *ws, size_t ws_bytes,
+                               const int64_t *rowptr, int32_t *colidx, void *stream) {
+    std::vector<PairDev> pairs;
+    SpDev S;
+    SpLayout L;
+    op2g_status s = sp_prepare(d, pairs, S, L);
+    if (s != OP2G_OK) return s;
+    if (!ws || ws_bytes < L.total) return op2g::fail(OP2G_ERR_INVALID, "workspace too small");
+    if (!rowptr || (!colidx && d->nrows > 0)) return op2g::fail(OP2G_ERR_INVALID, "NULL output");
+    cudaStream_t st = (cudaStream_t)stream;
+    char *w = (char *)ws;
+    long long *cnt = (long long *)(w + L.off_cnt);
+    long long *tlist = (long long *)(w + L.off_tlist);
+    PairDev *pd = (PairDev *)(w + L.off_pairs);
+    SpMisc *misc = (SpMisc *)(w + L.off_misc);
+    S.err = &misc->err;
+    int cap = 0;
+    CK(cudaMemcpyAsync(&cap, &misc->cap, sizeof cap, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (cap < 32) return op2g::fail(OP2G_ERR_INVALID, "op2g_sparsity_fill before op2g_sparsity_count");
+    return sp_rows_launch(S, pd, cnt, tlist, cap, 1, nullptr, (const long long *)rowptr, colidx, st);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- matrices
+namespace {
+
+__device__ __forceinline__ long long find_col(const int64_t *rp, const int *ci, long long row,
+                                              int col) {
+    long long lo = rp[row], hi = rp[row + 1] - 1;
+    while (lo <= hi) {
+        const long long mid = (lo + hi) >> 1;
+        const int c = ci[mid];
+        if (c == col) return mid;
+        if (c < col) lo = mid + 1;
+        else hi = mid - 1;
+    }
+    return -1;
+}
+
+__global__ void k_zero_rows(op2g_bcsr m, const int *__restrict__ rows, long long n, double diag) {
+    const int lane = threadIdx.x & 31;
+    const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int bs = m.rdim * m.cdim;
+    for (long long k = w0; k < n; k += nw) {
+        const long long row = rows[k];
+        if (row < 0 || row >= m.nrows * m.rdim) continue;
+        const long long br = row / m.rdim;
+        const int ri = (int)(row - br * m.rdim);
+        const long long cb = row / m.cdim;
+        const int cj0 = (int)(row - cb * m.cdim);
+        for (long long q = m.rowptr[br] + lane; q < m.rowptr[br + 1]; q += 32)
+            for (int cj = 0; cj < m.cdim; ++cj)
+                m.values[q * bs + ri * m.cdim + cj] =
+                    (m.colidx[q] == cb && cj == cj0) ? diag : 0.0;
+    }
+}
+
+__global__ void k_set_diag(op2g_bcsr m, const int *__restrict__ rows, long long n, double diag,
+                           int *err) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += stride) {
+        const long long row = rows[k];
+        if (row < 0 || row >= m.nrows * m.rdim || row >= m.ncols * m.cdim) continue;
+        const long long br = row / m.rdim, cb = row / m.cdim;
+        const long long q = find_col(m.rowptr, m.colidx, br, (int)cb);
+        if (q < 0) {
+            if (err) atomicOr(err, OP2G_DEVERR_NEW_NONZERO);
+            continue;
+        }
+        m.values[q * m.rdim * m.cdim + (row - br * m.rdim) * m.cdim + (row - cb * m.cdim)] = diag;
+    }
+}
+
+__global__ void k_spmv(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
+    const long long nr = m.nrows * m.rdim;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const int bs = m.rdim * m.cdim;
+    for (long long row = blockIdx.x * (long long)blockDim.x + threadIdx.x; row < nr; row += stride) {
+        const long long br = row / m.rdim;
+        const int ri = (int)(row - br * m.rdim);
+        double acc = 0.0;
+        for (long long q = m.rowptr[br]; q < m.rowptr[br + 1]; ++q) {
+            const long long c0 = (long long)m.colidx[q] * m.cdim;
+            const double *v = m.values + q * bs + ri * m.cdim;
+            for (int cj = 0; cj < m.cdim; ++cj) acc += v[cj] * x[c0 + cj];
+        }
+        y[row] = acc;
+    }
+}
+
+__global__ void k_spmv_t(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
+    const long long nr = m.nrows * m.rdim;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const int bs = m.rdim * m.cdim;
+    for (long long row = blockIdx.x * (long long)blockDim.x + threadIdx.x; row < nr; row += stride) {
+        const long long br = row / m.rdim;
+        const int ri = (int)(row - br * m.rdim);
+        const double xv = x[row];
+        if (xv == 0.0) continue;
+        for (long long q = m.rowptr[br]; q < m.rowptr[br + 1]; ++q) {
+            const long long c0 = (long long)m.colidx[q] * m.cdim;
+            const double *v = m.values + q * bs + ri * m.cdim;
+            for (int cj = 0; cj < m.cdim; ++cj) atomicAdd(&y[c0 + cj], v[cj] * xv);
+        }
+    }
+}
+
+unsigned grid_for(long long n, int bs) {
+    long long g = (n + bs - 1) / bs;
+    const long long cap = (long long)sms_of_current() * 16;
+    if (g > cap) g = cap;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+op2g_status check_bcsr(const op2g_bcsr *m) {
+    if (!m || !m->rowptr || !m->values || m->rdim <= 0 || m->cdim <= 0 || m->nrows < 0)
+        return op2g::fail(OP2G_ERR_INVALID, "bad block-CSR descriptor");
+    return OP2G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+op2g_status op2g_mat_zero_rows(const op2g_bcsr *m, const int32_t *rows, int64_t n, double diag,
+                               void *stream) {
+    op2g_status s = check_bcsr(m);
+    if (s != OP2G_OK) return s;
+    if (n <= 0) return OP2G_OK;
+    k_zero_rows<<<grid_for(n * 32, 256), 256, 0, (cudaStream_t)stream>>>(*m, rows, n, diag);
+    CK(cudaGetLastError());
+    return OP2G_OK;
+}
+
+op2g_status op2g_mat_set_diagonal(const op2g_bcsr *m, const int32_t *rows, int64_t n, double diag,
+                                  int32_t *err, void *stream) {
+    op2g_status s = check_bcsr(m);
+    if (s != OP2G_OK) return s;
+    if (n <= 0) return OP2G_OK;
+    k_set_diag<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(*m, rows, n, diag, err);
+    CK(cudaGetLastError());
+    return OP2G_OK;
+}
+
+op2g_status op2g_mat_spmv(const op2g_bcsr *m, const double *x, double *y, int32_t transpose,
+                          void *stream) {
+    op2g_status s = check_bcsr(m);
+    if (s != OP2G_OK) return s;
+    const long long nr = m->nrows * m->rdim;
+    if (nr <= 0) return OP2G_OK;
+    if (transpose)
+        k_spmv_t<<<grid_for(nr, 256), 256, 0, (cudaStream_t)stream>>>(*m, x, y);
+    else
+        k_spmv<<<grid_for(nr, 256), 256, 0, (cudaStream_t)stream>>>(*m, x, y);
+    CK(cudaGetLastError());
+    return OP2G_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- colouring
+// Jones-Plassmann colouring on the implicit conflict graph "two entities
+// conflict if they share a target through one of the maps".  Each round every
+// uncoloured entity writes its priority (hash, id) into its targets with
+// atomicMax; an entity that holds the maximum at all of its targets is a local
+// maximum, so no two such entities share a target, and each takes the
+// smallest colour absent from its targets' colour masks (first fit), then
+// marks its colour there.  Rounds repeat until every entity is coloured.
+namespace {
+
+constexpr int CW = 4;  // 64-bit mask words per target -> at most 256 colours
+
+struct ColDev {
+    int nmaps;
+    const int *maps[8];
+    int arity[8];
+    long long tsz[8];
+    unsigned long long *tmax[8];
+    unsigned long long *tmask[8];
+};
+
+__device__ __forceinline__ unsigned long long prio_of(long long c) {
+    unsigned long long h = (unsigned long long)c * 0x9E3779B97F4A7C15ull;
+    h ^= h >> 29;
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 32;
+    return (h << 32) | (unsigned long long)(c & 0xffffffffll);
+}
+
+__global__ void k_jp_prio(ColDev C, long long n, const int *__restrict__ colour) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += stride) {
+        if (colour[c] >= 0) continue;
+        const unsigned long long pr = prio_of(c);
+        for (int k = 0; k < C.nmaps; ++k)
+            for (int j = 0; j < C.arity[k]; ++j) {
+                const int t = C.maps[k][c * C.arity[k] + j];
+                if (t >= 0 && t < C.tsz[k]) atomicMax(&C.tmax[k][t], pr);
+            }
+    }
+}
+
+__global__ void k_jp_select(ColDev C, long long n, int *__restrict__ colour, int max_colours,
+                            unsigned long long *__restrict__ remaining, int *__restrict__ err) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += stride) {
+        if (colour[c] >= 0) continue;
+        const unsigned long long pr = prio_of(c);
+        bool top = true;
+        unsigned long long used[CW] = {0, 0, 0, 0};
+        for (int k = 0; k < C.nmaps && top; ++k)
+            for (int j = 0; j < C.arity[k]; ++j) {
+                const int t = C.maps[k][c * C.arity[k] + j];
+                if (t < 0 || t >= C.tsz[k]) continue;
+                if (C.tmax[k][t] != pr) {
+                    top = false;
+                    break;
+                }
+#pragma unroll
+                for (int w = 0; w < CW; ++w) used[w] |= C.tmask[k][(long long)t * CW + w];
+            }
+        if (!top) {
+            atomicAdd(remaining, 1ull);
+            continue;
+        }
+        int col = -1;
+        for (int w = 0; w < CW && col < 0; ++w)
+            if (~used[w]) col = w * 64 + __ffsll((long long)~used[w]) - 1;
+        if (col < 0 || col >= max_colours) {
+            atomicOr(err, OP2G_DEVERR_CAPACITY);
+            continue;
+        }
+        colour[c] = col;
+        for (int k = 0; k < C.nmaps; ++k)
+            for (int j = 0; j < C.arity[k]; ++j) {
+                const int t = C.maps[k][c * C.arity[k] + j];
+                if (t >= 0 && t < C.tsz[k])
+                    atomicOr(&C.tmask[k][(long long)t * CW + col / 64], 1ull << (col % 64));
+            }
+    }
+}
+
+__global__ void k_col_hist(const int *__restrict__ colour, long long n, long long *__restrict__ cnt) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += stride)
+        atomicAdd((unsigned long long *)&cnt[colour[c]], 1ull);
+}
+
+// Stable placement: entity c goes to ptr[colour] + (number of entities of the
+// same colour before c).  Each block handles a contiguous chunk; ranks within
+// the chunk come from a per-colour running counter over the chunk in order.
+__global__ void k_col_scatter(const int *__restrict__ colour, long long n, long long chunk,
+                              const long long *__restrict__ chunk_base, int ncol,
+                              int *__restrict__ order) {
+    // chunk_base[b * ncol + k]: first slot of colour k for chunk b (exclusive scan)
+    const long long b = blockIdx.x;
+    const long long c0 = b * chunk, c1 = min(n, c0 + chunk);
+    if (threadIdx.x != 0) return;
+    extern __shared__ long long run[];
+    for (int k = 0; k < ncol; ++k) run[k] = chunk_base[b * ncol + k];
+    for (long long c = c0; c < c1; ++c) order[run[colour[c]]++] = (int)c;
+}
+
+__global__ void k_col_chunk_hist(const int *__restrict__ colour, long long n, long long chunk,
+                                 int ncol, long long *__restrict__ h) {
+    // h laid out colour-major: h[k * nchunks + b], so one exclusive scan gives
+    // each (colour, chunk) its first slot in colour-then-entity order.
+    const long long b = blockIdx.x;
+    const long long nch = gridDim.x;
+    const long long c0 = b * chunk, c1 = min(n, c0 + chunk);
+    for (long long c = c0 + threadIdx.x; c < c1; c += blockDim.x)
+        atomicAdd((unsigned long long *)&h[(long long)colour[c] * nch + b], 1ull);
+}
+
+__global__ void k_transpose_base(const long long *__restrict__ h, long long nch, int ncol,
+                                 long long *__restrict__ base) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nch * ncol) return;
+    const long long b = i / ncol, k = i - b * ncol;
+    base[i] = h[k * nch + b];
+}
+
+constexpr long long COL_CHUNK = 4096;
+
+}  // namespace
+
+extern "C" {
+
+op2g_status op2g_colour_workspace(int64_t ncells, int32_t nmaps, const int64_t *target_size,
+                                  size_t *bytes) {
+    if (nmaps <= 0 || nmaps > 8 || !target_size || ncells < 0)
+        return op2g::fail(OP2G_ERR_INVALID, "colouring takes 1..8 maps");
+    size_t off = 0;
+    for (int k = 0; k < nmaps; ++k) {
+        off = align256(off + sizeof(unsigned long long) * (size_t)target_size[k]);       // tmax
+        off = align256(off + sizeof(unsigned long long) * CW * (size_t)target_size[k]);  // tmask
+    }
+    const long long nch = (ncells + COL_CHUNK - 1) / COL_CHUNK;
+    const long long nh = nch * 256 + 1;
+    off = align256(off + sizeof(long long) * nh);                 // histogram
+    off = align256(off + sizeof(long long) * nh);                 // transposed bases
+    off = align256(off + sizeof(long long) * scan_tmp_elems(nh));  // scan temp
+    off = align256(off + 64);                                      // counters
+    if (bytes) *bytes = off;
+    return OP2G_OK;
+}
+
+op2g_status op2g_colour(int64_t ncells, int32_t nmaps, const int32_t *const *maps,
+                        const int32_t *arity, const int64_t *target_size, int32_t max_colours,
+                        void *ws, size_t ws_bytes, int32_t *colour, int32_t *order,
+                        int64_t *colour_ptr, int32_t *ncolours, void *stream) {
+    size_t need = 0;
+    op2g_status s = op2g_colour_workspace(ncells, nmaps, target_size, &need);
+    if (s != OP2G_OK) return s;
+    if (!ws || ws_bytes < need) return op2g::fail(OP2G_ERR_INVALID, "workspace too small");
+    if (max_colours <= 0 || max_colours > 64 * CW)
+        return op2g::fail(OP2G_ERR_INVALID, "max_colours must be in 1..256");
+    if (!maps || !arity || !colour || !order || !colour_ptr)
+        return op2g::fail(OP2G_ERR_INVALID, "NULL argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    ColDev C;
+    memset(&C, 0, sizeof C);
+    C.nmaps = nmaps;
+    char *w = (char *)ws;
+    size_t off = 0;
+    for (int k = 0; k < nmaps; ++k) {
+        if (!maps[k] || arity[k] <= 0) return op2g::fail(OP2G_ERR_INVALID, "bad colouring map");
+        C.maps[k] = maps[k];
+        C.arity[k] = arity[k];
+        C.tsz[k] = target_size[k];
+        C.tmax[k] = (unsigned long long *)(w + off);
+        off = align256(off + sizeof(unsigned long long) * (size_t)target_size[k]);
+        C.tmask[k] = (unsigned long long *)(w + off);
+        off = align256(off + sizeof(unsigned long long) * CW * (size_t)target_size[k]);
+        CK(cudaMemsetAsync(C.tmask[k], 0, sizeof(unsigned long long) * CW * target_size[k], st));
+    }
+    const long long nch = (ncells + COL_CHUNK - 1) / COL_CHUNK;
+    const long long nh = nch * 256 + 1;
+    long long *hist = (long long *)(w + off);
+    off = align256(off + sizeof(long long) * nh);
+    long long *base = (long long *)(w + off);
+    off = align256(off + sizeof(long long) * nh);
+    long long *scan = (long long *)(w + off);
+    off = align256(off + sizeof(long long) * scan_tmp_elems(nh));
+    unsigned long long *remaining = (unsigned long long *)(w + off);
+    int *err = (int *)(remaining + 1);
+    CK(cudaMemsetAsync(colour, 0xff, sizeof(int) * ncells, st));
+    CK(cudaMemsetAsync(err, 0, sizeof(int), st));
+    const unsigned grid = grid_for(ncells, 256);
+    unsigned long long left = (unsigned long long)ncells;
+    int rounds = 0;
+    while (left > 0) {
+        if (++rounds > 100000) return op2g::fail(OP2G_ERR_TIMEOUT, "colouring did not converge");
+        for (int k = 0; k < nmaps; ++k)
+            CK(cudaMemsetAsync(C.tmax[k], 0, sizeof(unsigned long long) * target_size[k], st));
+        CK(cudaMemsetAsync(remaining, 0, sizeof(unsigned long long), st));
+        k_jp_prio<<<grid, 256, 0, st>>>(C, ncells, colour);
+        k_jp_select<<<grid, 256, 0, st>>>(C, ncells, colour, max_colours, remaining, err);
+        CK(cudaGetLastError());
+        int herr = 0;
+        CK(cudaMemcpyAsync(&left, remaining, sizeof left, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (herr & OP2G_DEVERR_CAPACITY)
+            return op2g::fail(OP2G_ERR_CAPACITY, "colouring needs more than max_colours colours");
+    }
+    // Number of colours = 1 + max colour; per-colour counts; stable order.
+    std::vector<long long> hc;
+    int ncol = 0;
+    {
+        CK(cudaMemsetAsync(hist, 0, sizeof(long long) * 257, st));
+        if (ncells > 0) k_col_hist<<<grid, 256, 0, st>>>(colour, ncells, hist);
+        CK(cudaGetLastError());
+        hc.resize(256);
+        CK(cudaMemcpyAsync(hc.data(), hist, sizeof(long long) * 256, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int k = 0; k < 256; ++k)
+            if (hc[k]) ncol = k + 1;
+    }
+    if (ncolours) *ncolours = ncol;
+    std::vector<long long> cp(max_colours + 1, 0);
+    for (int k = 0; k < ncol; ++k) cp[k + 1] = cp[k] + hc[k];
+    for (int k = ncol; k < max_colours; ++k) cp[k + 1] = cp[k];
+    CK(cudaMemcpyAsync(colour_ptr, cp.data(), sizeof(long long) * (max_colours + 1),
+                       cudaMemcpyHostToDevice, st));
+    if (ncells > 0 && ncol > 0) {
+        const long long nhist = nch * ncol;
+        CK(cudaMemsetAsync(hist, 0, sizeof(long long) * (nhist + 1), st));
+        k_col_chunk_hist<<<(unsigned)nch, 256, 0, st>>>(colour, ncells, COL_CHUNK, ncol, hist);
+        CK(cudaGetLastError());
+        s = scan_exclusive(hist, nhist + 1, scan, st);
+        if (s != OP2G_OK) return s;
+        k_transpose_base<<<(unsigned)((nhist + 255) / 256), 256, 0, st>>>(hist, nch, ncol, base);
+        k_col_scatter<<<(unsigned)nch, 32, sizeof(long long) * ncol, st>>>(colour, ncells, COL_CHUNK,
+                                                                          base, ncol, order);
+        CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(st));
+    return OP2G_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- probe
+namespace {
+__device__ double g_dfma_sink;
+__global__ void __launch_bounds__(256) k_dfma(int iters, double a, double b) {
+    double x0 = threadIdx.x * 1e-9, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    const double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == 1234.5678) g_dfma_sink = s;  // keeps the chains alive
+}
+}  // namespace
+
+extern "C" op2g_status op2g_probe_fp64_peak(double *flops, void *stream) {
+    if (!flops) return op2g::fail(OP2G_ERR_INVALID, "NULL output");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int sms = sms_of_current();
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    k_dfma<<<blocks, threads, 0, st>>>(iters, 0.999999, 1e-7);  // warm-up
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; ++rep) {
+        CK(cudaEventRecord(e0, st));
+        k_dfma<<<blocks, threads, 0, st>>>(iters, 0.999999, 1e-7);
+        CK(cudaEventRecord(e1, st));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *flops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3);
+    return OP2G_OK;
+}

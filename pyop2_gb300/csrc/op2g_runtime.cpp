@@ -1,0 +1,469 @@
+// op2g_runtime.cpp -- C ABI of the par_loop engine: NVRTC compilation of the
+// generated wrappers, an on-disk cubin cache, module loading and launches.
+//
+// Replaces the reference's JIT pipeline (pyop2/compilation.py:427-626: write
+// C, run gcc, cache the .so, ctypes.CDLL) and the ctypes call of the wrapper
+// (pyop2/global_kernel.py:322-331).  Driver-API entry points are fetched
+// through the CUDA runtime (cudaGetDriverEntryPointByVersion), so the library
+// loads on machines without a GPU driver and only needs one when a kernel is
+// launched.
+#include <cuda.h>
+#include <cuda_runtime_api.h>
+#include <nvrtc.h>
+
+#include <cerrno>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include "op2g_internal.h"
+
+namespace op2g {
+
+static thread_local std::string g_last_error = "no error";
+
+op2g_status fail(op2g_status code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+op2g_status cuda_fail(int err, const char *what) {
+    std::ostringstream s;
+    s << what << ": " << cudaGetErrorName((cudaError_t)err) << " ("
+      << cudaGetErrorString((cudaError_t)err) << ")";
+    return fail(OP2G_ERR_CUDA, s.str());
+}
+
+// ------------------------------------------------------------ driver API
+struct Driver {
+    CUresult (*ModuleLoadData)(CUmodule *, const void *) = nullptr;
+    CUresult (*ModuleUnload)(CUmodule) = nullptr;
+    CUresult (*ModuleGetFunction)(CUfunction *, CUmodule, const char *) = nullptr;
+    CUresult (*LaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned,
+                             unsigned, unsigned, CUstream, void **, void **) = nullptr;
+    CUresult (*FuncGetAttribute)(int *, CUfunction_attribute, CUfunction) = nullptr;
+    CUresult (*OccupancyMaxActiveBlocksPerMultiprocessor)(int *, CUfunction, int,
+                                                          size_t) = nullptr;
+    CUresult (*GetErrorString)(CUresult, const char **) = nullptr;
+    bool ok = false;
+    std::string why;
+};
+
+static Driver &driver() {
+    static Driver d;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        struct Sym {
+            const char *name;
+            void **slot;
+        } syms[] = {
+            {"cuModuleLoadData", (void **)&d.ModuleLoadData},
+            {"cuModuleUnload", (void **)&d.ModuleUnload},
+            {"cuModuleGetFunction", (void **)&d.ModuleGetFunction},
+            {"cuLaunchKernel", (void **)&d.LaunchKernel},
+            {"cuFuncGetAttribute", (void **)&d.FuncGetAttribute},
+            {"cuOccupancyMaxActiveBlocksPerMultiprocessor",
+             (void **)&d.OccupancyMaxActiveBlocksPerMultiprocessor},
+            {"cuGetErrorString", (void **)&d.GetErrorString},
+        };
+        for (auto &s : syms) {
+            cudaDriverEntryPointQueryResult q;
+            cudaError_t e = cudaGetDriverEntryPointByVersion(s.name, s.slot, 12000,
+                                                             cudaEnableDefault, &q);
+            if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !*s.slot) {
+                d.why = std::string("driver entry point ") + s.name + " unavailable (" +
+                        cudaGetErrorString(e) + ")";
+                return;
+            }
+        }
+        d.ok = true;
+    });
+    return d;
+}
+
+static op2g_status cu_fail(CUresult r, const char *what) {
+    const char *s = "unknown";
+    if (driver().GetErrorString) driver().GetErrorString(r, &s);
+    return fail(OP2G_ERR_CUDA, std::string(what) + ": CUDA driver error " + std::to_string((int)r) +
+                                   " (" + (s ? s : "") + ")");
+}
+
+// -------------------------------------------------------------- hashing
+static void fnv1a(const std::string &s, uint64_t &h) {
+    for (unsigned char c : s) {
+        h ^= c;
+        h *= 1099511628211ull;
+    }
+}
+static std::string hash_hex(const std::string &s) {
+    uint64_t a = 1469598103934665603ull, b = 0x9e3779b97f4a7c15ull;
+    fnv1a(s, a);
+    fnv1a(std::to_string(s.size()) + s, b);
+    char buf[40];
+    snprintf(buf, sizeof buf, "%016llx%016llx", (unsigned long long)a, (unsigned long long)b);
+    return buf;
+}
+
+static bool read_file(const std::string &path, std::string &out) {
+    FILE *f = fopen(path.c_str(), "rb");
+    if (!f) return false;
+    std::string buf;
+    char tmp[1 << 16];
+    size_t n;
+    while ((n = fread(tmp, 1, sizeof tmp, f)) > 0) buf.append(tmp, n);
+    fclose(f);
+    out.swap(buf);
+    return true;
+}
+
+static void mkdirs(const std::string &dir) {
+    std::string cur;
+    for (size_t i = 0; i < dir.size(); ++i) {
+        cur.push_back(dir[i]);
+        if (dir[i] == '/' || i + 1 == dir.size()) mkdir(cur.c_str(), 0755);
+    }
+}
+
+static void write_file_atomic(const std::string &path, const std::string &data) {
+    std::string tmp = path + ".tmp." + std::to_string((long long)getpid());
+    FILE *f = fopen(tmp.c_str(), "wb");
+    if (!f) return;
+    bool ok = fwrite(data.data(), 1, data.size(), f) == data.size();
+    ok = (fclose(f) == 0) && ok;
+    if (ok) rename(tmp.c_str(), path.c_str());
+    else unlink(tmp.c_str());
+}
+
+std::string current_arch(op2g_status *st) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    int maj = 0, min = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&maj, cudaDevAttrComputeCapabilityMajor, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&min, cudaDevAttrComputeCapabilityMinor, dev);
+    if (e != cudaSuccess) {
+        *st = cuda_fail(e, "querying the current device");
+        return "";
+    }
+    *st = OP2G_OK;
+    return "sm_" + std::to_string(maj) + std::to_string(min) + (maj >= 9 ? "a" : "");
+}
+
+static op2g_status nvrtc_compile(const std::string &src, const std::string &arch,
+                                 std::string &cubin) {
+    nvrtcProgram prog;
+    const char *hdrs[] = {device_header_src};
+    const char *names[] = {"op2g_device.cuh"};
+    nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), "op2g_wrapper.cu", 1, hdrs, names);
+    if (r != NVRTC_SUCCESS)
+        return fail(OP2G_ERR_COMPILE, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
+    std::string archopt = "--gpu-architecture=" + arch;
+    const char *opts[] = {archopt.c_str(), "--device-as-default-execution-space", "-std=c++17",
+                          "-lineinfo", "-w"};
+    r = nvrtcCompileProgram(prog, sizeof opts / sizeof opts[0], opts);
+    size_t logsz = 0;
+    nvrtcGetProgramLogSize(prog, &logsz);
+    std::string log(logsz, '\0');
+    if (logsz) nvrtcGetProgramLog(prog, &log[0]);
+    while (!log.empty() && log.back() == '\0') log.pop_back();
+    if (r != NVRTC_SUCCESS) {
+        nvrtcDestroyProgram(&prog);
+        return fail(OP2G_ERR_COMPILE, std::string("NVRTC compilation failed (") +
+                                          nvrtcGetErrorString(r) + "):\n" + log +
+                                          "\n---- generated source ----\n" + src);
+    }
+    size_t n = 0;
+    r = nvrtcGetCUBINSize(prog, &n);
+    if (r == NVRTC_SUCCESS) {
+        cubin.resize(n);
+        r = nvrtcGetCUBIN(prog, &cubin[0]);
+    }
+    nvrtcDestroyProgram(&prog);
+    if (r != NVRTC_SUCCESS)
+        return fail(OP2G_ERR_COMPILE, std::string("nvrtcGetCUBIN: ") + nvrtcGetErrorString(r));
+    return OP2G_OK;
+}
+
+// Compile (or fetch from the cache dir) the cubin for `src`.
+op2g_status build_cubin(const std::string &src, const std::string &arch, const char *cache_dir,
+                        std::string &cubin) {
+    std::string key = hash_hex(src + "\n//arch=" + arch + "\n//abi=" +
+                               std::to_string(OP2G_ABI_VERSION) + "\n" + device_header_src);
+    std::string path;
+    if (cache_dir && *cache_dir) {
+        path = std::string(cache_dir) + "/op2g-" + key + "-" + arch + ".cubin";
+        if (read_file(path, cubin) && !cubin.empty()) return OP2G_OK;
+    }
+    op2g_status st = nvrtc_compile(src, arch, cubin);
+    if (st != OP2G_OK) return st;
+    if (!path.empty()) {
+        mkdirs(cache_dir);
+        write_file_atomic(path, cubin);
+    }
+    return OP2G_OK;
+}
+
+struct Loaded {
+    CUmodule mod = nullptr;
+    CUfunction f = nullptr, fb = nullptr;
+    int regs = -1;
+    int occ = 0;  // resident CTAs per SM
+    int sms = 0;
+};
+
+// Load `cubin` on the current device (cached per device in `per_dev`).
+op2g_status load_module(const std::string &cubin, const char *fname, const char *fname_b, int bs,
+                        std::map<int, Loaded> &per_dev, std::mutex &mu, Loaded **out) {
+    Driver &D = driver();
+    if (!D.ok) return fail(OP2G_ERR_CUDA, "CUDA driver not available: " + D.why);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    std::lock_guard<std::mutex> g(mu);
+    auto it = per_dev.find(dev);
+    if (it != per_dev.end()) {
+        *out = &it->second;
+        return OP2G_OK;
+    }
+    e = cudaFree(nullptr);  // make sure the primary context is current
+    if (e != cudaSuccess) return cuda_fail(e, "initialising the CUDA context");
+    Loaded L;
+    CUresult r = D.ModuleLoadData(&L.mod, cubin.data());
+    if (r != CUDA_SUCCESS) return cu_fail(r, "cuModuleLoadData");
+    r = D.ModuleGetFunction(&L.f, L.mod, fname);
+    if (r != CUDA_SUCCESS) return cu_fail(r, "cuModuleGetFunction");
+    if (fname_b) {
+        r = D.ModuleGetFunction(&L.fb, L.mod, fname_b);
+        if (r != CUDA_SUCCESS) return cu_fail(r, "cuModuleGetFunction (batched)");
+    }
+    D.FuncGetAttribute(&L.regs, CU_FUNC_ATTRIBUTE_NUM_REGS, L.f);
+    if (D.OccupancyMaxActiveBlocksPerMultiprocessor(&L.occ, L.f, bs, 0) != CUDA_SUCCESS) L.occ = 1;
+    if (L.occ < 1) L.occ = 1;
+    cudaDeviceGetAttribute(&L.sms, cudaDevAttrMultiProcessorCount, dev);
+    if (L.sms < 1) L.sms = 1;
+    auto res = per_dev.emplace(dev, L);
+    *out = &res.first->second;
+    return OP2G_OK;
+}
+
+op2g_status launch(CUfunction f, unsigned grid, unsigned block, void **params, void *stream) {
+    CUresult r = driver().LaunchKernel(f, grid, 1, 1, block, 1, 1, 0, (CUstream)stream, params,
+                                       nullptr);
+    if (r != CUDA_SUCCESS) return cu_fail(r, "cuLaunchKernel");
+    return OP2G_OK;
+}
+
+}  // namespace op2g
+
+using namespace op2g;
+
+struct op2g_kernel {
+    Signature sig;
+    std::string source, arch, cubin;
+    std::mutex mu;
+    std::map<int, Loaded> per_dev;
+    int param_bytes = 0;
+};
+
+extern "C" {
+
+const char *op2g_last_error(void) { return g_last_error.c_str(); }
+
+int32_t op2g_abi_version(void) { return OP2G_ABI_VERSION; }
+
+op2g_status op2g_device_init(int32_t device, int32_t *sm_count, int32_t *cc_major,
+                             int32_t *cc_minor) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    e = cudaFree(nullptr);
+    if (e != cudaSuccess) return cuda_fail(e, "initialising the CUDA context");
+    int v = 0;
+    if (sm_count) {
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device);
+        *sm_count = v;
+    }
+    if (cc_major) {
+        cudaDeviceGetAttribute(&v, cudaDevAttrComputeCapabilityMajor, device);
+        *cc_major = v;
+    }
+    if (cc_minor) {
+        cudaDeviceGetAttribute(&v, cudaDevAttrComputeCapabilityMinor, device);
+        *cc_minor = v;
+    }
+    if (!driver().ok) return fail(OP2G_ERR_CUDA, "CUDA driver not available: " + driver().why);
+    return OP2G_OK;
+}
+
+op2g_status op2g_kernel_create(const char *user_src, const char *kernel_name,
+                               const op2g_loop_desc *loop, const op2g_arg_desc *args,
+                               int32_t nargs, const op2g_map_desc *maps, int32_t nmaps,
+                               const char *arch, const char *cache_dir, op2g_kernel **out) {
+    if (!out) return fail(OP2G_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!user_src || !kernel_name || !loop) return fail(OP2G_ERR_INVALID, "NULL argument");
+    if (nargs < 0 || nargs > OP2G_MAX_ARGS) return fail(OP2G_ERR_INVALID, "too many arguments");
+    if (nmaps < 0 || nmaps > OP2G_MAX_MAPS) return fail(OP2G_ERR_INVALID, "too many maps");
+    if ((nargs && !args) || (nmaps && !maps)) return fail(OP2G_ERR_INVALID, "NULL descriptors");
+    Signature S;
+    S.user_src = user_src;
+    S.kernel_name = kernel_name;
+    S.loop = *loop;
+    S.block_size = loop->block_size > 0 ? loop->block_size : 256;
+    if (S.block_size % 32 || S.block_size > 1024)
+        return fail(OP2G_ERR_INVALID, "block_size must be a multiple of 32 and <= 1024");
+    if (loop->iteration_region < OP2G_ON_BOTTOM || loop->iteration_region > OP2G_ALL)
+        S.loop.iteration_region = OP2G_ALL;
+    int slot = 0;
+    for (int a = 0; a < nargs; ++a) {
+        ArgInfo A;
+        A.d = args[a];
+        A.slot = slot;
+        slot += (A.d.kind == OP2G_ARG_MAT) ? 3 : 1;
+        S.args.push_back(A);
+    }
+    S.map_slot0 = slot;
+    for (int m = 0; m < nmaps; ++m) {
+        MapInfo M;
+        M.kind = maps[m].kind;
+        M.arity = maps[m].arity;
+        M.base = maps[m].base;
+        M.ncomposed = maps[m].ncomposed;
+        for (int k = 0; k < OP2G_MAX_COMPOSED; ++k) M.composed[k] = maps[m].composed[k];
+        if (M.arity > 0 && M.arity < (1 << 20)) {
+            if (maps[m].offset) M.offset.assign(maps[m].offset, maps[m].offset + M.arity);
+            if (maps[m].offset_quotient)
+                M.offset_quotient.assign(maps[m].offset_quotient, maps[m].offset_quotient + M.arity);
+            if (maps[m].permutation)
+                M.permutation.assign(maps[m].permutation, maps[m].permutation + M.arity);
+        }
+        S.maps.push_back(M);
+    }
+    S.nptrs = slot + nmaps;
+    std::string why = validate_signature(S);
+    if (!why.empty()) return fail(OP2G_ERR_INVALID, why);
+
+    op2g_kernel *k = new op2g_kernel();
+    k->sig = S;
+    k->source = generate_source(S);
+    k->param_bytes = 8 * (5 + (S.nptrs > 0 ? S.nptrs : 1) + (nmaps > 0 ? nmaps : 1));
+    op2g_status st = OP2G_OK;
+    k->arch = (arch && *arch) ? std::string(arch) : current_arch(&st);
+    if (st != OP2G_OK) {
+        delete k;
+        return st;
+    }
+    st = build_cubin(k->source, k->arch, cache_dir, k->cubin);
+    if (st != OP2G_OK) {
+        delete k;
+        return st;
+    }
+    *out = k;
+    return OP2G_OK;
+}
+
+void op2g_kernel_destroy(op2g_kernel *k) {
+    if (!k) return;
+    if (driver().ok) {
+        for (auto &kv : k->per_dev)
+            if (kv.second.mod) driver().ModuleUnload(kv.second.mod);
+    }
+    delete k;
+}
+
+op2g_status op2g_kernel_source(const op2g_kernel *k, char *buf, size_t len, size_t *needed) {
+    if (!k) return fail(OP2G_ERR_INVALID, "NULL kernel");
+    if (needed) *needed = k->source.size() + 1;
+    if (buf && len) {
+        size_t n = k->source.size() < len - 1 ? k->source.size() : len - 1;
+        memcpy(buf, k->source.data(), n);
+        buf[n] = '\0';
+    }
+    return OP2G_OK;
+}
+
+int32_t op2g_kernel_num_ptrs(const op2g_kernel *k) { return k ? k->sig.nptrs : -1; }
+
+int32_t op2g_kernel_num_regs(const op2g_kernel *k) {
+    if (!k) return -1;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    auto it = k->per_dev.find(dev);
+    return it == k->per_dev.end() ? -1 : it->second.regs;
+}
+
+int32_t op2g_kernel_param_bytes(const op2g_kernel *k) { return k ? k->param_bytes : -1; }
+
+op2g_status op2g_kernel_pack_params(const op2g_kernel *k, const op2g_launch_desc *d, void *out) {
+    if (!k || !d || !out) return fail(OP2G_ERR_INVALID, "NULL argument");
+    if (!d->ptrs && k->sig.nptrs > 0) return fail(OP2G_ERR_INVALID, "ptrs is NULL");
+    const Signature &S = k->sig;
+    if (S.loop.extruded && !d->layers) return fail(OP2G_ERR_INVALID, "extruded loop needs layers");
+    if (S.loop.indexed && !d->indices) return fail(OP2G_ERR_INVALID, "indexed loop needs indices");
+    int64_t *w = (int64_t *)out;
+    memset(out, 0, k->param_bytes);
+    w[0] = d->start;
+    w[1] = d->end;
+    w[2] = (int64_t)(intptr_t)d->layers;
+    w[3] = (int64_t)(intptr_t)d->indices;
+    w[4] = (int64_t)(intptr_t)d->err;
+    for (int i = 0; i < S.nptrs; ++i) w[5 + i] = (int64_t)(intptr_t)d->ptrs[i];
+    const int np = S.nptrs > 0 ? S.nptrs : 1;
+    for (size_t m = 0; m < S.maps.size(); ++m)
+        w[5 + np + m] = d->map_toset ? d->map_toset[m] : INT64_MAX;
+    // Every slot the generated code dereferences must be non-NULL.
+    for (const ArgInfo &A : S.args) {
+        int nslots = A.d.kind == OP2G_ARG_MAT ? 3 : 1;
+        for (int s = 0; s < nslots; ++s)
+            if (!d->ptrs[A.slot + s] && A.d.kind != OP2G_ARG_PASSTHROUGH)
+                return fail(OP2G_ERR_INVALID, "NULL device pointer for an argument");
+    }
+    for (size_t m = 0; m < S.maps.size(); ++m)
+        if (S.maps[m].kind == OP2G_MAP_PLAIN && !d->ptrs[S.map_slot((int)m)] )
+            return fail(OP2G_ERR_INVALID, "NULL device pointer for map " + std::to_string(m));
+    return OP2G_OK;
+}
+
+op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *stream) {
+    if (!k || !d) return fail(OP2G_ERR_INVALID, "NULL argument");
+    if (d->end < d->start || d->start < 0) return fail(OP2G_ERR_INVALID, "bad iteration range");
+    std::vector<int64_t> buf(k->param_bytes / 8);
+    op2g_status st = op2g_kernel_pack_params(k, d, buf.data());
+    if (st != OP2G_OK) return st;
+    Loaded *L = nullptr;
+    st = load_module(k->cubin, "op2g_wrap", "op2g_wrap_batched", k->sig.block_size, k->per_dev,
+                     k->mu, &L);
+    if (st != OP2G_OK) return st;
+    const int64_t per = d->layers_per_entity > 0 ? d->layers_per_entity : 1;
+    const int64_t items = (d->end - d->start) * (k->sig.loop.extruded && k->sig.loop.constant_layers ? per : 1);
+    if (items <= 0) return OP2G_OK;
+    const int bs = k->sig.block_size;
+    int64_t grid = d->grid > 0 ? d->grid : (items + bs - 1) / bs;
+    const int64_t cap = (int64_t)L->occ * L->sms;
+    if (d->grid <= 0 && grid > cap) grid = cap;
+    if (grid < 1) grid = 1;
+    void *params[] = {buf.data()};
+    return launch(L->f, (unsigned)grid, (unsigned)bs, params, stream);
+}
+
+op2g_status op2g_kernel_launch_batched(op2g_kernel *k, const void *params_dev,
+                                       const int64_t *work_dev, int64_t nwork, int32_t grid,
+                                       void *stream) {
+    if (!k || !params_dev || !work_dev) return fail(OP2G_ERR_INVALID, "NULL argument");
+    if (nwork <= 0) return OP2G_OK;
+    Loaded *L = nullptr;
+    op2g_status st = load_module(k->cubin, "op2g_wrap", "op2g_wrap_batched", k->sig.block_size,
+                                 k->per_dev, k->mu, &L);
+    if (st != OP2G_OK) return st;
+    int64_t g = grid > 0 ? grid : (int64_t)L->occ * L->sms;
+    if (g > nwork) g = nwork;
+    const void *p0 = params_dev;
+    const int64_t *w0 = work_dev;
+    long long nw = nwork;
+    void *params[] = {(void *)&p0, (void *)&w0, (void *)&nw};
+    return launch(L->fb, (unsigned)g, (unsigned)k->sig.block_size, params, stream);
+}
+
+}  // extern "C"

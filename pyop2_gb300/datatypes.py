@@ -1,0 +1,41 @@
+"""Element types (pyop2/datatypes.py).  IntType is PETSc's default int32 and
+ScalarType float64, fixed here because there is no PETSc."""
+import numpy
+
+from pyop2_gb300 import _lib
+
+IntType = numpy.dtype(numpy.int32)
+RealType = numpy.dtype(numpy.float64)
+ScalarType = numpy.dtype(numpy.float64)
+
+_CODES = {
+    "float64": _lib.F64, "float32": _lib.F32, "int32": _lib.I32, "uint32": _lib.U32,
+    "int64": _lib.I64, "uint64": _lib.U64, "int16": _lib.I16, "uint16": _lib.U16,
+    "int8": _lib.I8, "uint8": _lib.U8,
+}
+
+
+def as_code(dtype):
+    """libop2g element-type code of a numpy dtype."""
+    name = numpy.dtype(dtype).name
+    try:
+        return _CODES[name]
+    except KeyError:
+        raise TypeError("pyop2_gb300 has no device element type for %s" % name)
+
+
+def as_cstr(dtype):
+    """C type name of a numpy dtype (pyop2/datatypes.py:13-29)."""
+    return {"bool": "unsigned char", "int8": "int8_t", "int16": "int16_t",
+            "int32": "int32_t", "int64": "int64_t", "uint8": "uint8_t",
+            "uint16": "uint16_t", "uint32": "uint32_t", "uint64": "uint64_t",
+            "float32": "float", "float64": "double"}[numpy.dtype(dtype).name]
+
+
+def dtype_limits(dtype):
+    """(min, max) of a numpy dtype."""
+    try:
+        info = numpy.iinfo(dtype)
+    except ValueError:
+        info = numpy.finfo(dtype)
+    return info.min, info.max

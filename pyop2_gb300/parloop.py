@@ -1,0 +1,535 @@
+"""par_loop orchestration (pyop2/parloop.py:167-760) on the GPU.
+
+``op2.par_loop(kernel, iterset, *args)`` validates its arguments exactly as
+the reference does, builds a descriptor of the loop signature, obtains the
+compiled wrapper for that signature from libop2g (generated CUDA around the
+user kernel, NVRTC-compiled, cached by signature) and launches it on torch's
+current stream.  The loop executes [0, iterset.size) in one launch: on one
+GPU there is no halo exchange to overlap, so the reference's core/owned split
+(pyop2/parloop.py:243-260) collapses to a single range.
+
+INC/MIN/MAX conflicts through maps are resolved by hardware atomics (default),
+warp-aggregated atomics, or a greedy colouring with one launch per colour
+(``configuration['scatter']``; ``'auto'`` lets the autotuner choose).
+"""
+import ctypes
+from dataclasses import dataclass
+from typing import Any, Optional, Tuple
+
+import numpy as np
+import torch
+
+from pyop2_gb300 import _lib, device
+from pyop2_gb300.configuration import configuration
+from pyop2_gb300.datatypes import IntType, as_code
+from pyop2_gb300.exceptions import KernelTypeError, MapValueError, SetTypeError
+from pyop2_gb300.local_kernel import CStringLocalKernel, LocalKernel
+from pyop2_gb300.types.access import ALL, Access, IterationRegion
+from pyop2_gb300.types.dat import Dat
+from pyop2_gb300.types.glob import Constant, Global
+from pyop2_gb300.types.map import ComposedMap, Map, PermutedMap
+from pyop2_gb300.types.mat import Mat
+from pyop2_gb300.types.set import ExtrudedSet, MixedSet, Set, Subset
+
+
+# --------------------------------------------------------------- legacy args
+class LegacyArg:
+    """Old-style par_loop argument: data + access (+ maps)."""
+
+
+@dataclass
+class GlobalLegacyArg(LegacyArg):
+    data: Global
+    access: Access
+
+    @property
+    def dtype(self):
+        return self.data.dtype
+
+    @property
+    def maps(self):
+        return ()
+
+
+@dataclass
+class DatLegacyArg(LegacyArg):
+    data: Dat
+    map_: Optional[Map]
+    access: Access
+
+    @property
+    def dtype(self):
+        return self.data.dtype
+
+    @property
+    def maps(self):
+        return (self.map_,) if self.map_ is not None else ()
+
+
+@dataclass
+class MatLegacyArg(LegacyArg):
+    data: Mat
+    maps: Tuple[Map, Map]
+    access: Access
+    lgmaps: Optional[Tuple[Any, Any]] = None
+    needs_unrolling: Optional[bool] = False
+
+    @property
+    def dtype(self):
+        return self.data.dtype
+
+
+@dataclass
+class PassthroughArg(LegacyArg):
+    """A raw device pointer handed to the kernel untouched (dtype for codegen)."""
+    dtype: Any
+    data: int
+    access = Access.RW
+
+    @property
+    def maps(self):
+        return ()
+
+
+# ------------------------------------------------------------- validation
+def _check_map(m):
+    if configuration["type_check"]:
+        if isinstance(m, ComposedMap):
+            for m_ in m.maps_:
+                _check_map(m_)
+        elif isinstance(m, PermutedMap):
+            _check_map(m.map_)
+        elif m.iterset.total_size > 0 and len(m.values_with_halo) == 0:
+            raise MapValueError("%s is not initialized" % m)
+
+
+def _check_iterset(iterset, args):
+    """pyop2/parloop.py:470-499."""
+    if not configuration["type_check"]:
+        return
+    if not isinstance(iterset, Set):
+        raise SetTypeError("Iteration set is of the wrong type")
+    if isinstance(iterset, MixedSet):
+        raise SetTypeError("Cannot iterate over mixed sets")
+    if isinstance(iterset, Subset):
+        iterset = iterset.superset
+    for i, a in enumerate(args):
+        if isinstance(a, DatLegacyArg) and a.map_ is None:
+            _iterset = iterset.parent if isinstance(iterset, ExtrudedSet) else iterset
+            if a.data.dataset.set != _iterset:
+                raise MapValueError("Iterset of direct arg %d does not match parloop iterset" % i)
+        for j, m in enumerate(a.maps):
+            if m.iterset != iterset and m.iterset not in iterset:
+                raise MapValueError("Iterset of arg %d map %d does not match parloop iterset" % (i, j))
+
+
+# ------------------------------------------------------------ signature
+class _MapTable:
+    """Unique maps of a loop, in first-seen order (pyop2/parloop.py:204-212),
+    flattened into plain / permuted / composed entries for libop2g."""
+
+    def __init__(self):
+        self.entries = []     # (kind, arity, base, composed tuple, offset, oq, perm)
+        self.objs = []        # plain Map object per entry (None otherwise)
+        self._index = {}
+
+    def add(self, m):
+        key = id(m)
+        if key in self._index:
+            return self._index[key]
+        if isinstance(m, ComposedMap):
+            comps = [self.add(c) for c in m.flattened_maps]
+            entry = (_lib.MAP_COMPOSED, m.arity, -1, tuple(comps), None, None, None)
+            obj = None
+        elif isinstance(m, PermutedMap):
+            base = self.add(m.map_)
+            entry = (_lib.MAP_PERMUTED, m.arity, base, (), None, None,
+                     tuple(int(x) for x in m.permutation))
+            obj = None
+        else:
+            off = None if m.offset is None else tuple(int(x) for x in m.offset)
+            oq = None if m.offset_quotient is None else tuple(int(x) for x in m.offset_quotient)
+            entry = (_lib.MAP_PLAIN, m.arity, -1, (), off, oq, None)
+            obj = m
+        idx = len(self.entries)
+        self.entries.append(entry)
+        self.objs.append(obj)
+        self._index[key] = idx
+        return idx
+
+    def key(self):
+        return tuple(self.entries)
+
+
+_KERNELS = {}   # signature key -> _Compiled
+
+
+class _Compiled:
+    """A libop2g kernel handle with its ctypes descriptors."""
+
+    def __init__(self, handle, nptrs):
+        self.handle = handle
+        self.nptrs = nptrs
+
+    def __del__(self):
+        try:
+            if self.handle:
+                _lib.lib().op2g_kernel_destroy(self.handle)
+        except Exception:
+            pass
+
+    def source(self):
+        n = ctypes.c_size_t()
+        _lib.call("op2g_kernel_source", self.handle, None, 0, ctypes.byref(n))
+        buf = ctypes.create_string_buffer(n.value)
+        _lib.call("op2g_kernel_source", self.handle, buf, n.value, ctypes.byref(n))
+        return buf.value.decode()
+
+
+def compile_signature(code, name, loop, args, maps, arch=None):
+    """Compile (or fetch) the wrapper for a signature given as plain tuples:
+    loop = dict of LoopDesc fields, args = list of ArgDesc field tuples,
+    maps = list of _MapTable entries."""
+    key = (code, name, tuple(sorted(loop.items())), tuple(args), tuple(maps), arch)
+    c = _KERNELS.get(key)
+    if c is not None:
+        return c
+    L = _lib.LoopDesc(**loop)
+    A = (_lib.ArgDesc * max(1, len(args)))()
+    for i, a in enumerate(args):
+        A[i] = _lib.ArgDesc(*a)
+    M = (_lib.MapDesc * max(1, len(maps)))()
+    keep = []
+    for i, (kind, arity, base, comps, off, oq, perm) in enumerate(maps):
+        d = M[i]
+        d.kind, d.arity, d.base, d.ncomposed = kind, arity, base, len(comps)
+        for k, c in enumerate(comps):
+            d.composed[k] = c
+        for fld, vals in (("offset", off), ("offset_quotient", oq), ("permutation", perm)):
+            if vals is not None:
+                arr = (ctypes.c_int32 * len(vals))(*vals)
+                keep.append(arr)
+                setattr(d, fld, ctypes.cast(arr, ctypes.POINTER(ctypes.c_int32)))
+    h = ctypes.c_void_p()
+    cache_dir = configuration["cache_dir"]
+    _lib.call("op2g_kernel_create", code.encode(), name.encode(), ctypes.byref(L), A, len(args),
+              M, len(maps), arch.encode() if arch else None,
+              cache_dir.encode() if cache_dir else None, ctypes.byref(h))
+    c = _Compiled(h.value, _lib.lib().op2g_kernel_num_ptrs(h.value))
+    _KERNELS[key] = c
+    return c
+
+
+# ---------------------------------------------------------------- Parloop
+class Parloop:
+    """A parallel loop invocation (pyop2/parloop.py:167-537).
+
+    ``Parloop(kernel, iterset, args, iteration_region=None,
+    pass_layer_arg=False)``; ``compute()`` (or calling it) executes it.
+    """
+
+    def __init__(self, local_knl, iterset, args, iteration_region=None, pass_layer_arg=False):
+        if not isinstance(local_knl, LocalKernel):
+            raise KernelTypeError
+        if pass_layer_arg and not iterset._extruded:
+            raise ValueError("Cannot request layer argument for non-extruded iteration")
+        for a in args:
+            for m in (a.maps if not isinstance(a, MatLegacyArg) else a.maps):
+                _check_map(m)
+            if isinstance(a, GlobalLegacyArg) and isinstance(a.data, Constant) \
+                    and a.access is not Access.READ:
+                raise ValueError("Constants can only ever be read in a parloop, not modified")
+        _check_iterset(iterset, args)
+        self.local_kernel = local_knl
+        self.iterset = iterset
+        self.args = tuple(args)
+        self.iteration_region = IterationRegion(iteration_region or ALL)
+        self.pass_layer_arg = bool(pass_layer_arg)
+        self._built = None
+
+    @property
+    def accesses(self):
+        return tuple(a.access for a in self.args)
+
+    @property
+    def arguments(self):
+        return self.args
+
+    # ---- signature
+    def _signature(self):
+        table = _MapTable()
+        argdescs = []
+        for a in self.args:
+            if isinstance(a, GlobalLegacyArg):
+                argdescs.append((_lib.ARG_GLOBAL, int(a.access), as_code(a.data.dtype),
+                                 a.data.cdim, -1, -1, 0, 0))
+            elif isinstance(a, DatLegacyArg):
+                mi = table.add(a.map_) if a.map_ is not None else -1
+                argdescs.append((_lib.ARG_DAT, int(a.access), as_code(a.data.dtype),
+                                 a.data.cdim, mi, -1, 0, 0))
+            elif isinstance(a, MatLegacyArg):
+                rm = table.add(a.maps[0])
+                cm = table.add(a.maps[1])
+                rdim, cdim = a.data.dims[0][0]
+                argdescs.append((_lib.ARG_MAT, int(a.access), as_code(a.data.dtype), 1, rm, cm,
+                                 rdim, cdim))
+            elif isinstance(a, PassthroughArg):
+                argdescs.append((_lib.ARG_PASSTHROUGH, int(Access.RW), as_code(a.dtype), 1,
+                                 -1, -1, 0, 0))
+            else:
+                raise ValueError("Unhandled argument type %r" % type(a))
+        return table, argdescs
+
+    def _loop_desc(self, scatter, block_size):
+        it = self.iterset
+        return dict(extruded=int(it._extruded),
+                    constant_layers=int(bool(it._extruded and it.constant_layers)),
+                    extruded_periodic=int(bool(it._extruded_periodic)),
+                    indexed=int(isinstance(it, Subset) or scatter == _lib.SCATTER_PLAIN),
+                    iteration_region=int(self.iteration_region),
+                    pass_layer_arg=int(self.pass_layer_arg),
+                    scatter=scatter, block_size=block_size,
+                    debug_checks=int(bool(configuration["debug"])), batched=0)
+
+    def _needs_conflict_handling(self):
+        return any(isinstance(a, (DatLegacyArg, MatLegacyArg)) and
+                   (isinstance(a, MatLegacyArg) or a.map_ is not None) and
+                   a.access in (Access.INC, Access.MIN, Access.MAX) for a in self.args)
+
+    def _choose_strategy(self):
+        mode = configuration["scatter"]
+        bs = int(configuration["block_size"])
+        if mode == "auto" or configuration["autotune"]:
+            from pyop2_gb300 import autotune
+            return autotune.choose(self)
+        if not self._needs_conflict_handling():
+            return _lib.SCATTER_ATOMIC, bs
+        if mode == "warp":
+            it = self.iterset
+            if it._extruded and not it.constant_layers:
+                return _lib.SCATTER_ATOMIC, bs
+            return _lib.SCATTER_WARP, bs
+        if mode == "colour" and self._colourable():
+            return _lib.SCATTER_PLAIN, bs
+        return _lib.SCATTER_ATOMIC, bs
+
+    def _colourable(self):
+        if self.iterset._extruded:
+            return False
+        for a in self.args:
+            if isinstance(a, DatLegacyArg) and a.map_ is not None and \
+                    a.access in (Access.INC, Access.MIN, Access.MAX, Access.WRITE, Access.RW):
+                if isinstance(a.map_, ComposedMap):
+                    return False
+            if isinstance(a, MatLegacyArg):
+                if any(isinstance(m, ComposedMap) for m in a.maps):
+                    return False
+        return True
+
+    def build(self, scatter=None, block_size=None):
+        """Compile the wrapper for this loop (idempotent per strategy)."""
+        if scatter is None:
+            scatter, block_size = self._choose_strategy()
+        table, argdescs = self._signature()
+        loop = self._loop_desc(scatter, block_size)
+        k = compile_signature(self.local_kernel.source, self.local_kernel.name, loop, argdescs,
+                              table.key())
+        self._built = (scatter, block_size, k, table, argdescs)
+        return k
+
+    # ---- execution
+    def _pointers(self, table, k):
+        """Device pointer slots (order documented in include/op2g.h) and the
+        error-word pointer."""
+        ptrs = []
+        err = None
+        for a in self.args:
+            if isinstance(a, (GlobalLegacyArg, DatLegacyArg)):
+                ptrs.append(a.data._device_ptr())
+            elif isinstance(a, MatLegacyArg):
+                m = a.data
+                ptrs += [m._values.data_ptr(), m.sparsity.rowptr.data_ptr(),
+                         m.sparsity._colidx.data_ptr()]
+                if err is None:
+                    err = m._err
+            elif isinstance(a, PassthroughArg):
+                ptrs.append(int(a.data))
+        for obj in table.objs:
+            ptrs.append(obj._device_values().data_ptr() if obj is not None else 0)
+        assert len(ptrs) == k.nptrs
+        return ptrs, err
+
+    def _layers_per_entity(self):
+        it = self.iterset
+        if not (it._extruded and it.constant_layers):
+            return 1
+        L = int(it.layers_array[0, 1]) - int(it.layers_array[0, 0])   # layers
+        ncell = L - 1
+        r = self.iteration_region
+        if r in (IterationRegion.BOTTOM, IterationRegion.TOP):
+            return 1
+        if r == IterationRegion.INTERIOR_FACETS and not it._extruded_periodic:
+            return max(ncell - 1, 0)
+        return ncell
+
+    def __call__(self):
+        self.compute()
+
+    def compute(self):
+        device.require()
+        if self._built is None:
+            self.build()
+        scatter, bs, k, table, argdescs = self._built
+        it = self.iterset
+        # Mat assembly state (pyop2/parloop.py:279-301, 454-468)
+        for a in self.args:
+            if isinstance(a, MatLegacyArg):
+                a.data.change_assembly_state(Mat.ADD_VALUES if a.access is Access.INC
+                                             else Mat.INSERT_VALUES)
+        ptrs, err = self._pointers(table, k)
+        dbg_err = None
+        if configuration["debug"] and err is None:
+            dbg_err = torch.zeros(1, dtype=torch.int32, device=device.device())
+            err = dbg_err
+        P = (ctypes.c_void_p * max(1, len(ptrs)))(*ptrs)
+        toset = (ctypes.c_int64 * max(1, len(table.objs)))()
+        for i, e in enumerate(table.entries):
+            toset[i] = 2**62
+        for i, a in enumerate(self.args):
+            if isinstance(a, DatLegacyArg) and a.map_ is not None:
+                toset[table.add(a.map_)] = a.data.dataset.total_size
+        D = _lib.LaunchDesc()
+        D.layers = it._layers_device().data_ptr() if it._extruded else None
+        D.err = err.data_ptr() if err is not None else None
+        D.ptrs = P
+        D.map_toset = toset
+        D.layers_per_entity = self._layers_per_entity()
+        D.grid = 0
+        st = device.stream_handle()
+        if scatter == _lib.SCATTER_PLAIN:
+            plan = colour_plan(self)
+            base_idx = it._indices_mirror.dev() if isinstance(it, Subset) else None
+            order = plan.order if base_idx is None else plan.order_for_subset(base_idx)
+            D.indices = order.data_ptr()
+            for c in range(plan.ncolours):
+                D.start, D.end = plan.ptr[c], plan.ptr[c + 1]
+                if D.end > D.start:
+                    _lib.call("op2g_kernel_launch", k.handle, ctypes.byref(D), st)
+        else:
+            D.indices = it._indices_mirror.dev().data_ptr() if isinstance(it, Subset) else None
+            D.start, D.end = 0, it.size
+            _lib.call("op2g_kernel_launch", k.handle, ctypes.byref(D), st)
+        # state updates
+        for a in self.args:
+            if a.access is Access.READ or isinstance(a, PassthroughArg):
+                continue
+            if isinstance(a, MatLegacyArg):
+                a.data.assembly_state = (Mat.ADD_VALUES if a.access is Access.INC
+                                         else Mat.INSERT_VALUES)
+                a.data.increment_dat_version()
+            else:
+                a.data._m.dev_modified()
+                a.data.increment_dat_version()
+                if isinstance(a, DatLegacyArg):
+                    a.data.halo_valid = False
+        if dbg_err is not None:
+            e = int(dbg_err.item())
+            if e & _lib.DEVERR_MAP_BOUNDS:
+                raise MapValueError("par_loop %s: a map value is outside its target set"
+                                    % self.local_kernel.name)
+
+    def generated_source(self):
+        """CUDA source of the wrapper this loop runs."""
+        if self._built is None:
+            self.build()
+        return self._built[2].source()
+
+
+# ------------------------------------------------------------- colouring
+class ColourPlan:
+    """Greedy colouring of an iteration set w.r.t. the targets of its
+    conflicting maps: ``order`` lists entities colour by colour,
+    ``ptr[c]:ptr[c+1]`` is colour c's segment."""
+
+    def __init__(self, order, ptr, ncolours, colour):
+        self.order = order
+        self.ptr = ptr
+        self.ncolours = ncolours
+        self.colour = colour
+
+    def order_for_subset(self, subset_indices):
+        raise NotImplementedError
+
+
+def colour_plan(loop, max_colours=256):
+    """Colouring of ``loop.iterset`` (cached on the set per map tuple)."""
+    it = loop.iterset
+    if isinstance(it, Subset):
+        raise NotImplementedError("coloured execution of subsets")
+    maps = []
+    for a in loop.args:
+        if a.access is Access.READ:
+            continue
+        if isinstance(a, DatLegacyArg) and a.map_ is not None:
+            maps.append(a.map_)
+        elif isinstance(a, MatLegacyArg):
+            maps.extend(a.maps)
+    base = []
+    seen = set()
+    for m in maps:
+        b = m.map_ if isinstance(m, PermutedMap) else m
+        if id(b) not in seen:
+            seen.add(id(b))
+            base.append(b)
+    key = ("colour", tuple(id(b) for b in base))
+    plan = it._cache.get(key)
+    if plan is not None:
+        return plan
+    n = it.size
+    dev = device.device()
+    arrs = (ctypes.c_void_p * len(base))(*[b._device_values().data_ptr() for b in base])
+    ar = (ctypes.c_int32 * len(base))(*[b.arity for b in base])
+    tsz = (ctypes.c_int64 * len(base))(*[b.toset.total_size for b in base])
+    ws = ctypes.c_size_t()
+    _lib.call("op2g_colour_workspace", n, len(base), tsz, ctypes.byref(ws))
+    work = device.empty_bytes(ws.value)
+    colour = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+    order = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+    cptr = torch.empty(max_colours + 1, dtype=torch.int64, device=dev)
+    nc = ctypes.c_int32()
+    _lib.call("op2g_colour", n, len(base), arrs, ar, tsz, max_colours, work.data_ptr(), ws.value,
+              colour.data_ptr(), order.data_ptr(), cptr.data_ptr(), ctypes.byref(nc),
+              device.stream_handle())
+    ptr = cptr[:nc.value + 1].cpu().numpy().tolist()
+    plan = ColourPlan(order, ptr, nc.value, colour)
+    it._cache[key] = plan
+    return plan
+
+
+# ------------------------------------------------------------ entry points
+def LegacyParloop(local_knl, iterset, *args, **kwargs):
+    """Build a Parloop from legacy arguments (pyop2/parloop.py:707-741)."""
+    if not all(isinstance(a, LegacyArg) for a in args):
+        raise ValueError("LegacyParloop only expects LegacyArg arguments")
+    if not isinstance(iterset, Set):
+        raise SetTypeError("Iteration set is of the wrong type")
+    local_knl.accesses = tuple(a.access for a in args)
+    if isinstance(local_knl, CStringLocalKernel):
+        local_knl.dtypes = tuple(a.dtype for a in args)
+    return Parloop(local_knl, iterset, args, **kwargs)
+
+
+def ParLoop(*args, **kwargs):
+    return LegacyParloop(*args, **kwargs)
+
+
+def parloop(knl, *args, **kwargs):
+    """Construct and execute a par_loop (pyop2/parloop.py:748-760)."""
+    if isinstance(knl, LocalKernel):
+        LegacyParloop(knl, *args, **kwargs)()
+    else:
+        raise KernelTypeError
+
+
+def par_loop(*args, **kwargs):
+    parloop(*args, **kwargs)

@@ -1,0 +1,256 @@
+"""Dats (pyop2/types/dat.py:25-784): per-entity data held in HBM.
+
+Storage is ``(dataset.total_size,) + dim`` C-contiguous (pyop2/types/dat.py:81)
+in a device buffer with a lazily synchronised host mirror.  ``data`` /
+``data_ro`` / ``data_wo`` (and the ``_with_halos`` variants) have the
+reference's meaning; reading them after a par_loop copies the device data
+back once.
+"""
+import numpy as np
+
+from pyop2_gb300 import exceptions as ex
+from pyop2_gb300 import utils
+from pyop2_gb300.configuration import configuration
+from pyop2_gb300.datatypes import ScalarType
+from pyop2_gb300.device import Mirror
+from pyop2_gb300.types.access import Access
+from pyop2_gb300.types.dataset import DataSet
+from pyop2_gb300.types.set import ExtrudedSet, Set
+
+
+class DataCarrier:
+    """Common base of Dat, Global and Mat (pyop2/types/data_carrier.py:13-48)."""
+
+    _version = 0
+
+    def increment_dat_version(self):
+        self._version += 1
+
+    @property
+    def dat_version(self):
+        return self._version
+
+    @property
+    def ctype(self):
+        from pyop2_gb300.datatypes import as_cstr
+        return as_cstr(self.dtype)
+
+
+class AbstractDat(DataCarrier):
+    _modes = [Access.READ, Access.WRITE, Access.RW, Access.INC, Access.MIN, Access.MAX]
+
+
+class Dat(AbstractDat):
+    """OP2 vector data: values on every entity of a DataSet.
+
+    ``Dat(set_or_dataset, data=None, dtype=None, name=None)``; a Set means a
+    dim-1 DataSet, a Dat means a copy; missing data is zero.
+    """
+
+    @utils.validate_type(('dataset', (DataCarrier, DataSet, Set), ex.DataSetTypeError),
+                         ('name', str, ex.NameTypeError))
+    @utils.validate_dtype(('dtype', None, ex.DataTypeError))
+    def __init__(self, dataset, data=None, dtype=None, name=None):
+        if isinstance(dataset, Dat):
+            src = dataset
+            self.__init__(src.dataset, None, dtype=src.dtype, name="copy_of_%s" % src.name)
+            src.copy(self)
+            return
+        if type(dataset) is Set or type(dataset) is ExtrudedSet:
+            dataset = dataset ** 1
+        self._dataset = dataset
+        self.comm = dataset.comm
+        self._shape = (dataset.total_size,) + (() if dataset.cdim == 1 else dataset.dim)
+        if data is None:
+            self._dtype = np.dtype(dtype if dtype is not None else ScalarType)
+            self._m = Mirror(self._dtype, self._shape)
+        else:
+            arr = utils.verify_reshape(data, dtype, self._shape, allow_none=True)
+            if arr.size == 0 and int(np.prod(self._shape)) != 0:
+                raise ex.DataValueError("Invalid data: expected %d values" % int(np.prod(self._shape)))
+            self._dtype = arr.dtype
+            self._m = Mirror(self._dtype, self._shape, np.array(arr, copy=True))
+        self._name = name or "dat_#x%x" % id(self)
+        self.halo_valid = True
+        self._version = 0
+
+    # ---- kernel-argument construction
+    @utils.validate_in(('access', AbstractDat._modes, ex.ModeValueError))
+    def __call__(self, access, path=None):
+        from pyop2_gb300.parloop import DatLegacyArg
+        if configuration["type_check"] and path is not None and path.toset != self.dataset.set:
+            raise ex.MapValueError("To Set of Map does not match Set of Dat.")
+        return DatLegacyArg(self, path, access)
+
+    def __getitem__(self, idx):
+        if idx != 0:
+            raise ex.IndexValueError("Can only extract component 0 from %r" % self)
+        return self
+
+    @property
+    def split(self):
+        return (self,)
+
+    @property
+    def dataset(self):
+        return self._dataset
+
+    @property
+    def dim(self):
+        return self.dataset.dim
+
+    @property
+    def cdim(self):
+        return self.dataset.cdim
+
+    @property
+    def shape(self):
+        return self._shape
+
+    @property
+    def dtype(self):
+        return self._dtype
+
+    @property
+    def name(self):
+        return self._name
+
+    @property
+    def nbytes(self):
+        return self.dtype.itemsize * self.dataset.total_size * self.dataset.cdim
+
+    # ---- host accessors
+    @property
+    def data(self):
+        """Writable host view of the owned values (marks the host newer)."""
+        self.increment_dat_version()
+        self.halo_valid = False
+        v = self._m.host(write=True)[:self.dataset.size].view()
+        v.setflags(write=True)
+        return v
+
+    @property
+    def data_with_halos(self):
+        self.increment_dat_version()
+        self.halo_valid = False
+        v = self._m.host(write=True).view()
+        v.setflags(write=True)
+        return v
+
+    @property
+    def data_ro(self):
+        v = self._m.host(write=False)[:self.dataset.size].view()
+        v.setflags(write=False)
+        return v
+
+    @property
+    def data_ro_with_halos(self):
+        v = self._m.host(write=False).view()
+        v.setflags(write=False)
+        return v
+
+    @property
+    def data_wo(self):
+        return self.data
+
+    @property
+    def data_wo_with_halos(self):
+        return self.data_with_halos
+
+    # ---- device access
+    @property
+    def tensor(self):
+        """The device values as a torch tensor of shape ``shape`` (no copy).
+        Writes through this view must be followed by ``mark_device_modified``."""
+        return self._m.tensor().view(self._shape)
+
+    def mark_device_modified(self):
+        self._m.dev_modified()
+        self.increment_dat_version()
+
+    def _device_ptr(self):
+        return self._m.dev().data_ptr()
+
+    @classmethod
+    def from_tensor(cls, dataset, tensor, name=None):
+        """A Dat whose device storage is ``tensor`` (CUDA, contiguous, matching
+        shape and dtype), without copying.  The Dat writes into the tensor."""
+        import torch
+        from pyop2_gb300 import device
+        if type(dataset) is Set:
+            dataset = dataset ** 1
+        d = cls.__new__(cls)
+        d._dataset = dataset
+        d.comm = dataset.comm
+        d._shape = (dataset.total_size,) + (() if dataset.cdim == 1 else dataset.dim)
+        if not tensor.is_cuda or not tensor.is_contiguous():
+            raise ValueError("from_tensor needs a contiguous CUDA tensor")
+        if tuple(tensor.shape) != d._shape and tensor.numel() != int(np.prod(d._shape)):
+            raise ValueError("tensor shape %s does not match %s" % (tuple(tensor.shape), d._shape))
+        npdt = {torch.float64: np.float64, torch.float32: np.float32,
+                torch.int32: np.int32, torch.int64: np.int64}[tensor.dtype]
+        d._dtype = np.dtype(npdt)
+        d._m = Mirror(d._dtype, d._shape)
+        d._m._dev = tensor.view(-1).view(torch.uint8)
+        d._m.state = "device"
+        d._name = name or "dat_#x%x" % id(d)
+        d.halo_valid = True
+        d._version = 0
+        device.require()
+        return d
+
+    # ---- operations
+    def zero(self, subset=None):
+        self.increment_dat_version()
+        if subset is None:
+            self._m.zero()
+            self.halo_valid = True
+        elif subset.superset != self.dataset.set:
+            raise ex.MapValueError("The subset and dataset are incompatible")
+        else:
+            self.data[subset.owned_indices] = 0
+
+    def copy(self, other, subset=None):
+        if other is self:
+            return
+        if subset is None:
+            other.data_with_halos[:] = self.data_ro_with_halos
+            other.halo_valid = True
+        elif subset.superset != self.dataset.set:
+            raise ex.MapValueError("The subset and dataset are incompatible")
+        else:
+            other.data[subset.owned_indices] = self.data_ro[subset.owned_indices]
+
+    def save(self, filename):
+        """Write the owned values to ``filename`` in NumPy format."""
+        np.save(filename, self.data_ro)
+
+    def load(self, filename):
+        if filename[-4:] != ".npy":
+            filename = filename + ".npy"
+        self.data[:] = np.load(filename)
+
+    def __iter__(self):
+        yield self
+
+    def __len__(self):
+        return 1
+
+    def __str__(self):
+        return "OP2 Dat: %s on (%s) with datatype %s" % (self._name, self._dataset, self.dtype.name)
+
+    def __repr__(self):
+        return "Dat(%r, None, %r, %r)" % (self._dataset, self.dtype, self._name)
+
+    # halo operations are no-ops on one device (no MPI halos)
+    def global_to_local_begin(self, access_mode):
+        pass
+
+    def global_to_local_end(self, access_mode):
+        pass
+
+    def local_to_global_begin(self, insert_mode):
+        pass
+
+    def local_to_global_end(self, insert_mode):
+        pass

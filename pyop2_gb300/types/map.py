@@ -1,0 +1,268 @@
+"""Maps (pyop2/types/map.py): Map :17-168, PermutedMap :171-215,
+ComposedMap :218-294, MixedMap :297-434 (container only).
+
+Map values live on the device as int32 ``[iterset.total_size, arity]``; the
+host copy is kept read-only so the two can never diverge.
+"""
+import itertools
+import numbers
+
+import numpy as np
+
+from pyop2_gb300 import exceptions as ex
+from pyop2_gb300 import utils
+from pyop2_gb300.datatypes import IntType
+from pyop2_gb300.device import Mirror
+from pyop2_gb300.types.set import Set
+
+
+class Map:
+    """Each entity of ``iterset`` maps to ``arity`` entities of ``toset``.
+
+    ``offset`` (length arity) is the per-layer increment of the values for
+    extruded iteration; ``offset_quotient`` is used by periodic extrusion.
+    """
+
+    dtype = IntType
+
+    @utils.validate_type(('iterset', Set, ex.SetTypeError), ('toset', Set, ex.SetTypeError),
+                         ('arity', numbers.Integral, ex.ArityTypeError),
+                         ('name', str, ex.NameTypeError))
+    def __init__(self, iterset, toset, arity, values=None, name=None, offset=None,
+                 offset_quotient=None):
+        self._iterset = iterset
+        self._toset = toset
+        self.comm = toset.comm
+        self._arity = int(arity)
+        self._values = utils.verify_reshape(values, IntType, (iterset.total_size, arity),
+                                            allow_none=True)
+        self._values.setflags(write=False)
+        self.shape = (iterset.total_size, arity)
+        self._name = name or "map_#x%x" % id(self)
+        if offset is None or len(offset) == 0:
+            self._offset = None
+        else:
+            self._offset = utils.verify_reshape(offset, IntType, (arity,))
+        if offset_quotient is None or len(offset_quotient) == 0:
+            self._offset_quotient = None
+        else:
+            self._offset_quotient = utils.verify_reshape(offset_quotient, IntType, (arity,))
+        self._cache = {}
+        self._mirror = None
+
+    # ---- device
+    def _device_values(self):
+        """Device int32 buffer of the values (uploaded once)."""
+        if self._mirror is None:
+            self._mirror = Mirror(IntType, self._values.shape, self._values)
+        return self._mirror.dev()
+
+    @property
+    def _cache_key(self):
+        """What of this map determines generated code (pyop2/types/map.py:60-62)."""
+        return (type(self).__name__, self.arity, utils.tuplify(self.offset),
+                utils.tuplify(self.offset_quotient))
+
+    def __iter__(self):
+        yield self
+
+    def __len__(self):
+        return 1
+
+    @property
+    def split(self):
+        return (self,)
+
+    @property
+    def iterset(self):
+        return self._iterset
+
+    @property
+    def toset(self):
+        return self._toset
+
+    @property
+    def arity(self):
+        return self._arity
+
+    @property
+    def arities(self):
+        return (self._arity,)
+
+    @property
+    def arange(self):
+        return (0, self._arity)
+
+    @property
+    def values(self):
+        return self._values[:self.iterset.size]
+
+    @property
+    def values_with_halo(self):
+        return self._values
+
+    @property
+    def name(self):
+        return self._name
+
+    @property
+    def offset(self):
+        return self._offset
+
+    @property
+    def offset_quotient(self):
+        return self._offset_quotient
+
+    @property
+    def flattened_maps(self):
+        return (self,)
+
+    def __str__(self):
+        return "OP2 Map: %s from (%s) to (%s) with arity %s" % (self._name, self._iterset,
+                                                               self._toset, self._arity)
+
+    def __repr__(self):
+        return "Map(%r, %r, %r, None, %r, %r, %r)" % (self._iterset, self._toset, self._arity,
+                                                    self._name, self._offset,
+                                                    self._offset_quotient)
+
+    def __le__(self, o):
+        return self == o
+
+
+class PermutedMap(Map):
+    """``local[i] = global[map[permutation[i]]]`` (pyop2/types/map.py:171-215)."""
+
+    def __init__(self, map_, permutation):
+        if not isinstance(map_, Map):
+            raise TypeError("map_ must be a Map instance")
+        if isinstance(map_, ComposedMap):
+            raise NotImplementedError("PermutedMap of ComposedMap not implemented: simply "
+                                      "permute before composing")
+        self.map_ = map_
+        self.comm = map_.comm
+        self.permutation = np.asarray(permutation, dtype=IntType)
+        assert (np.unique(self.permutation) == np.arange(map_.arity, dtype=IntType)).all()
+
+    @property
+    def _cache_key(self):
+        return self.map_._cache_key + (tuple(self.permutation),)
+
+    def __getattr__(self, name):
+        if name.startswith("__") or name == "map_":
+            raise AttributeError(name)
+        return getattr(self.map_, name)
+
+    @property
+    def iterset(self):
+        return self.map_.iterset
+
+    @property
+    def toset(self):
+        return self.map_.toset
+
+    @property
+    def arity(self):
+        return self.map_.arity
+
+    @property
+    def offset(self):
+        return self.map_.offset
+
+    @property
+    def offset_quotient(self):
+        return self.map_.offset_quotient
+
+    @property
+    def values_with_halo(self):
+        return self.map_.values_with_halo
+
+    @property
+    def values(self):
+        return self.map_.values
+
+    @property
+    def flattened_maps(self):
+        return (self,)
+
+
+class ComposedMap(Map):
+    """``local[i] = global[maps_[0][maps_[1][...[n]]][i]]``; inner maps have
+    arity 1 (pyop2/types/map.py:218-294)."""
+
+    def __init__(self, *maps_, name=None):
+        if not all(isinstance(m, Map) for m in maps_):
+            raise TypeError("All maps must be Map instances")
+        for tomap, frommap in zip(maps_[:-1], maps_[1:]):
+            if tomap.iterset is not frommap.toset:
+                raise ex.MapTypeError("tomap.iterset must match frommap.toset")
+            if frommap.arity != 1:
+                raise ex.MapTypeError("frommap.arity must be 1")
+        self._iterset = maps_[-1].iterset
+        self._toset = maps_[0].toset
+        self.comm = self._toset.comm
+        self._arity = maps_[0].arity
+        self._values = None
+        self.shape = (self._iterset.total_size, self._arity)
+        self._name = name or "cmap_#x%x" % id(self)
+        self._offset = maps_[0].offset
+        self._offset_quotient = maps_[0].offset_quotient
+        self._cache = {}
+        self.maps_ = tuple(maps_)
+
+    @property
+    def _cache_key(self):
+        return tuple(m._cache_key for m in self.maps_)
+
+    @property
+    def values(self):
+        raise RuntimeError("ComposedMap does not store values directly")
+
+    @property
+    def values_with_halo(self):
+        raise RuntimeError("ComposedMap does not store values directly")
+
+    def __str__(self):
+        return "OP2 ComposedMap of Maps: [%s]" % ",".join(str(m) for m in self.maps_)
+
+    def __repr__(self):
+        return "ComposedMap(%s)" % ",".join(repr(m) for m in self.maps_)
+
+    def __le__(self, o):
+        raise NotImplementedError("__le__ not implemented for ComposedMap")
+
+    @property
+    def flattened_maps(self):
+        return tuple(itertools.chain(*(m.flattened_maps for m in self.maps_)))
+
+
+class MixedMap(Map):
+    """A tuple of Maps (container only)."""
+
+    def __init__(self, maps):
+        self._maps = tuple(maps)
+        self.comm = None
+        self._name = "mmap_#x%x" % id(self)
+        self._cache = {}
+
+    @property
+    def split(self):
+        return self._maps
+
+    def __iter__(self):
+        yield from self._maps
+
+    def __len__(self):
+        return len(self._maps)
+
+    @property
+    def iterset(self):
+        return self._maps[0].iterset
+
+    @property
+    def arity(self):
+        return sum(m.arity for m in self._maps)
+
+    @property
+    def arities(self):
+        return tuple(m.arity for m in self._maps)

@@ -1,0 +1,106 @@
+"""Wrapper generation and NVRTC compilation for sm_103a, on CPU (NVRTC needs
+no GPU when the architecture is given).  Covers every access mode, element
+type, Global reductions, Mats, extruded regions, permuted and composed maps
+and the three INC strategies."""
+import numpy as np
+import pytest
+
+from pyop2_gb300 import _lib
+from pyop2_gb300.parloop import LegacyParloop, compile_signature
+
+
+@pytest.fixture(scope="module")
+def op2():
+    from pyop2_gb300.csrc import build
+    build.build()
+    from pyop2_gb300 import op2
+    return op2
+
+
+def compile_loop(pl, scatter=_lib.SCATTER_ATOMIC, bs=256):
+    table, argdescs = pl._signature()
+    loop = pl._loop_desc(scatter, bs)
+    return compile_signature(pl.local_kernel.source, pl.local_kernel.name, loop, argdescs,
+                             table.key(), arch="sm_103a")
+
+
+@pytest.mark.parametrize("scatter", [_lib.SCATTER_ATOMIC, _lib.SCATTER_WARP, _lib.SCATTER_PLAIN])
+@pytest.mark.parametrize("dtype,ctype", [(np.float64, "double"), (np.float32, "float"),
+                                         (np.int32, "int"), (np.uint32, "unsigned int"),
+                                         (np.int64, "long long")])
+def test_all_access_modes(op2, scatter, dtype, ctype):
+    cells, verts = op2.Set(8), op2.Set(10)
+    m = op2.Map(cells, verts, 3, np.arange(24) % 10)
+    dats = [op2.Dat(verts ** 2, dtype=dtype) for _ in range(6)]
+    direct = op2.Dat(cells, dtype=dtype)
+    g = [op2.Global(2, dtype=dtype) for _ in range(4)]
+    src = "static void k(%s) {}" % ", ".join(["%s *a%d" % (ctype, i) for i in range(11)])
+    k = op2.Kernel(src, "k")
+    pl = LegacyParloop(k, cells, dats[0](op2.READ, m), dats[1](op2.WRITE, m), dats[2](op2.RW, m),
+                       dats[3](op2.INC, m), dats[4](op2.MIN, m), dats[5](op2.MAX, m),
+                       direct(op2.RW), g[0](op2.READ), g[1](op2.INC), g[2](op2.MIN), g[3](op2.MAX))
+    c = compile_loop(pl, scatter)
+    assert c.nptrs == 12
+    s = c.source()
+    assert "op2g_wrap" in s and "op2g_wrap_batched" in s
+    if scatter == _lib.SCATTER_WARP:
+        assert "warp_agg_inc" in s
+
+
+@pytest.mark.parametrize("region", [1, 2, 3, 4])
+@pytest.mark.parametrize("constant", [True, False])
+@pytest.mark.parametrize("periodic", [False, True])
+def test_extruded_regions(op2, region, constant, periodic):
+    base = op2.Set(4)
+    layers = 5 if constant else np.array([[0, 5], [1, 4], [0, 3], [2, 5]])
+    ext = op2.ExtrudedSet(base, layers, extruded_periodic=periodic)
+    nodes = op2.Set(5 * 6)
+    m = op2.Map(ext, nodes, 2, np.arange(8) % 6 * 5, offset=[1, 1],
+                offset_quotient=[0, 1] if periodic else None)
+    d = op2.Dat(nodes, dtype=np.float64)
+    k = op2.Kernel("static void k(double *y, int layer) { y[0] += layer; }", "k")
+    pl = LegacyParloop(k, ext, d(op2.INC, m), iteration_region=region, pass_layer_arg=True)
+    c = compile_loop(pl)
+    assert "layer" in c.source()
+
+
+def test_mat_argument(op2):
+    cells, verts = op2.Set(2), op2.Set(4)
+    m = op2.Map(cells, verts, 3, [0, 1, 3, 2, 3, 1])
+    from pyop2_gb300.parloop import MatLegacyArg
+
+    class FakeMat:  # signature only: no device needed to generate code
+        dtype = np.dtype(np.float64)
+        dims = (((2, 2),),)
+    k = op2.Kernel("static void k(double A[6][6]) {}", "k")
+    for acc in (op2.INC, op2.WRITE):
+        pl = LegacyParloop(k, cells, MatLegacyArg(FakeMat(), (m, m), acc))
+        src = compile_loop(pl).source()
+        assert "bcsr_find" in src
+
+
+def test_permuted_and_composed_maps(op2):
+    setB, nodesetB = op2.Set(3), op2.Set(6)
+    setA, nodesetA = op2.Set(5), op2.Set(8)
+    mapB = op2.Map(setB, nodesetB, 2, [[0, 1], [2, 3], [4, 5]])
+    mapA0 = op2.Map(setA, nodesetA, 2, [[0, 1], [2, 3], [4, 5], [6, 7], [0, 1]])
+    mapA1 = op2.Map(setB, setA, 1, [3, 1, 2])
+    cm = op2.ComposedMap(op2.PermutedMap(mapA0, [1, 0]), mapA1)
+    dB = op2.Dat(nodesetB)
+    dA = op2.Dat(nodesetA)
+    k = op2.Kernel("void copy(double *to, const double * restrict from) { to[0] = from[0]; }",
+                   "copy")
+    pl = LegacyParloop(k, setB, dB(op2.WRITE, op2.PermutedMap(mapB, [1, 0])), dA(op2.READ, cm))
+    src = compile_loop(pl).source()
+    assert "op2g_perm" in src
+
+
+def test_compile_error_is_a_compilation_error(op2):
+    from pyop2_gb300.exceptions import CompilationError
+    s = op2.Set(4)
+    d = op2.Dat(s)
+    pl = LegacyParloop(op2.Kernel("static void k(double *x) { this is not C; }", "k"), s,
+                       d(op2.WRITE))
+    with pytest.raises(CompilationError) as e:
+        compile_loop(pl)
+    assert "generated source" in str(e.value)

@@ -1,0 +1,65 @@
+"""Benchmark configurations on the GPU against the oracle (small sizes) and
+through size-independent properties (full sizes)."""
+import numpy as np
+import pytest
+
+from pyop2_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+STRATEGIES = ["atomic", "warp", "colour"]
+
+
+@pytest.fixture(params=STRATEGIES)
+def strategy(request, gpu_op2):
+    from pyop2_gb300.configuration import configuration
+    old = configuration["scatter"]
+    configuration["scatter"] = request.param
+    yield request.param
+    configuration["scatter"] = old
+
+
+def relerr(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def test_config1_p1_2d(gpu_op2, oracle_op2, strategy):
+    g = workloads.build_p1_2d(gpu_op2, n=64, seed=0)
+    o = workloads.build_p1_2d(oracle_op2, n=64, seed=0)
+    g["run"]()
+    o["run"]()
+    assert abs(g["area"].data[0] - 1.0) < 1e-12
+    assert abs(g["area"].data[0] - o["area"].data[0]) < 1e-14
+    assert relerr(g["y"].data_ro, o["y"].data) <= 1e-12
+
+
+@pytest.mark.parametrize("permute", [False, True])
+def test_config2a_small_vs_oracle(gpu_op2, oracle_op2, strategy, permute):
+    g = workloads.build_p1_3d(gpu_op2, n=24, permute=permute, seed=3)
+    o = workloads.build_p1_3d(oracle_op2, n=24, permute=permute, seed=3)
+    g["run"]()
+    o["run"]()
+    assert relerr(g["y"].data_ro, o["y"].data) <= 1e-12
+
+
+@pytest.mark.parametrize("permute", [False, True])
+def test_config2a_full_size_properties(gpu_op2, permute):
+    """128^3 x 6 tets: the Laplacian annihilates constants (sum y = 0 up to
+    rounding) and the action is linear."""
+    op2 = gpu_op2
+    p = workloads.build_p1_3d(op2, n=128, permute=permute, seed=0)
+    x0 = p["x"].data_ro.copy()
+    p["run"]()
+    y1 = p["y"].data_ro.copy()
+    scale = np.abs(y1).max()
+    assert abs(y1.sum()) <= 1e-9 * scale * np.sqrt(len(y1))
+    # linearity: A(2x) = 2 A(x)
+    p["x"].data[:] = 2 * x0
+    p["y"].zero()
+    p["run"]()
+    assert relerr(p["y"].data_ro, 2 * y1) <= 1e-12
+    # constant field -> zero action
+    p["x"].data[:] = 1.0
+    p["y"].zero()
+    p["run"]()
+    assert np.abs(p["y"].data_ro).max() <= 1e-12 * scale
