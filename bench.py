@@ -273,10 +273,12 @@ def run_ours(args):
     flops = workloads.P1_3D_FLOPS * C
     fp64_achieved = flops / (per_launch_ms * 1e-3) / 1e12
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic_p1_laplace_3d_128cube.json")
-    if os.path.exists(tf):
+    tf = os.path.join(ROOT, "profiles", "op2g_wrap_p1_laplace_3d_128cube.md")
+    if os.path.exists(tf) and not args.permute:
+        import re
         with open(tf) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+            m = re.search(r"dram_bytes_per_launch:\s*(\d+)", f.read())
+        traffic = int(m.group(1)) if m else None
     cpu = None
     if not args.no_cpu_baseline:
         coords = p["coords"]

@@ -19,7 +19,9 @@ def candidates(loop):
             if not (it._extruded and not it.constant_layers):
                 out.append((_lib.SCATTER_WARP, bs))
             if loop._colourable():
-                out.append((_lib.SCATTER_PLAIN, bs))
+                from pyop2_gb300.parloop import colour_plan
+                if colour_plan(loop) is not None:
+                    out.append((_lib.SCATTER_PLAIN, bs))
     return out
 
 

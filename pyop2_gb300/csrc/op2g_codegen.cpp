@@ -231,10 +231,20 @@ struct Gen {
           << "};\n";
 
         const int BS = S.block_size;
-        const bool warp = S.loop.scatter == OP2G_SCATTER_WARP;
+        bool warp = S.loop.scatter == OP2G_SCATTER_WARP;
         const bool plain = S.loop.scatter == OP2G_SCATTER_PLAIN;
         const bool extr = S.loop.extruded != 0;
-        const bool varlay = extr && !S.loop.constant_layers;
+        // One thread per column (layers in sequence) when layers differ per
+        // column, when a colour's launch must not touch a column twice in
+        // parallel, or when a direct argument is written: direct arguments are
+        // indexed by the column only (pyop2/codegen/builder.py:367-377), so the
+        // layers of one column update the same entry and must run in order.
+        bool direct_written = false;
+        for (const ArgInfo &A : S.args)
+            if (A.d.kind == OP2G_ARG_DAT && A.d.map < 0 && A.d.access != OP2G_READ)
+                direct_written = true;
+        const bool varlay = extr && (!S.loop.constant_layers || plain || direct_written);
+        if (varlay) warp = false;  // lanes of a warp run different layer counts
 
         // ----- the run function: a strided sweep of [start, end) plus reductions
         O << "__device__ __forceinline__ void op2g_run(const op2g_params_t &p, long long start, "
@@ -298,7 +308,10 @@ struct Gen {
             emit_body(J, warp, plain);
         } else if (varlay) {
             O << J << "const long long n = " << (S.loop.indexed ? "p.indices[it]" : "it") << ";\n";
-            O << J << "const int cs_ = lay_[2 * n], ce_ = lay_[2 * n + 1] - 1;\n";
+            if (S.loop.constant_layers)
+                O << J << "const int cs_ = lay_[0], ce_ = lay_[1] - 1;\n";
+            else
+                O << J << "const int cs_ = lay_[2 * n], ce_ = lay_[2 * n + 1] - 1;\n";
             emit_layer_extents("cs_", "ce_", "ls_", "le_", J);
             O << J << "const int bottom = " << (S.loop.iteration_region == OP2G_ON_TOP ? "cs_" : "ls_")
               << ";\n";
@@ -629,8 +642,6 @@ std::string validate_signature(const Signature &S) {
                 return an + "unknown kind";
         }
     }
-    if (S.loop.extruded && !S.loop.constant_layers && S.loop.scatter == OP2G_SCATTER_WARP)
-        return "warp-aggregated scatter needs constant layers";
     if (S.loop.pass_layer_arg && !S.loop.extruded) return "layer argument needs an extruded loop";
     return "";
 }

@@ -260,6 +260,16 @@ op2g_status launch(CUfunction f, unsigned grid, unsigned block, void **params, v
 
 using namespace op2g;
 
+// True when the wrapper spreads the layers of a column over threads (the
+// codegen's choice for constant layers without written direct arguments).
+static bool column_parallel(const Signature &S) {
+    if (!S.loop.extruded || !S.loop.constant_layers || S.loop.scatter == OP2G_SCATTER_PLAIN)
+        return false;
+    for (const ArgInfo &A : S.args)
+        if (A.d.kind == OP2G_ARG_DAT && A.d.map < 0 && A.d.access != OP2G_READ) return false;
+    return true;
+}
+
 struct op2g_kernel {
     Signature sig;
     std::string source, arch, cubin;
@@ -437,7 +447,8 @@ op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *
                      k->mu, &L);
     if (st != OP2G_OK) return st;
     const int64_t per = d->layers_per_entity > 0 ? d->layers_per_entity : 1;
-    const int64_t items = (d->end - d->start) * (k->sig.loop.extruded && k->sig.loop.constant_layers ? per : 1);
+    const int64_t items = (d->end - d->start) * (k->sig.loop.extruded && k->sig.loop.constant_layers &&
+                                                 column_parallel(k->sig) ? per : 1);
     if (items <= 0) return OP2G_OK;
     const int bs = k->sig.block_size;
     int64_t grid = d->grid > 0 ? d->grid : (items + bs - 1) / bs;

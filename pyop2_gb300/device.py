@@ -7,6 +7,8 @@ historical OP2 CUDA backend (doc/sphinx/source/backends.rst:222-236): the host
 copy is refreshed only when the host reads data that the device modified, and
 uploaded only when a launch needs data that the host modified.
 """
+import warnings
+
 import numpy as np
 import torch
 
@@ -85,7 +87,12 @@ def zeros_bytes(nbytes):
 def upload(arr, out=None):
     """Copy a host array into a (new or given) device byte buffer."""
     a = np.ascontiguousarray(arr)
-    src = torch.from_numpy(a.reshape(-1).view(np.uint8)) if a.size else None
+    src = None
+    if a.size:
+        with warnings.catch_warnings():
+            # read-only host arrays (Map values) are only read by the copy
+            warnings.simplefilter("ignore", UserWarning)
+            src = torch.from_numpy(a.reshape(-1).view(np.uint8))
     if out is None:
         out = empty_bytes(a.nbytes)
     if src is not None:

@@ -309,12 +309,12 @@ class Parloop:
             if it._extruded and not it.constant_layers:
                 return _lib.SCATTER_ATOMIC, bs
             return _lib.SCATTER_WARP, bs
-        if mode == "colour" and self._colourable():
+        if mode == "colour" and self._colourable() and colour_plan(self) is not None:
             return _lib.SCATTER_PLAIN, bs
         return _lib.SCATTER_ATOMIC, bs
 
     def _colourable(self):
-        if self.iterset._extruded:
+        if self.iterset._extruded or isinstance(self.iterset, Subset):
             return False
         for a in self.args:
             if isinstance(a, DatLegacyArg) and a.map_ is not None and \
@@ -482,9 +482,8 @@ def colour_plan(loop, max_colours=256):
             seen.add(id(b))
             base.append(b)
     key = ("colour", tuple(id(b) for b in base))
-    plan = it._cache.get(key)
-    if plan is not None:
-        return plan
+    if key in it._cache:
+        return it._cache[key]
     n = it.size
     dev = device.device()
     arrs = (ctypes.c_void_p * len(base))(*[b._device_values().data_ptr() for b in base])
@@ -497,9 +496,14 @@ def colour_plan(loop, max_colours=256):
     order = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
     cptr = torch.empty(max_colours + 1, dtype=torch.int64, device=dev)
     nc = ctypes.c_int32()
-    _lib.call("op2g_colour", n, len(base), arrs, ar, tsz, max_colours, work.data_ptr(), ws.value,
-              colour.data_ptr(), order.data_ptr(), cptr.data_ptr(), ctypes.byref(nc),
-              device.stream_handle())
+    st = _lib.lib().op2g_colour(n, len(base), arrs, ar, tsz, max_colours, work.data_ptr(),
+                                ws.value, colour.data_ptr(), order.data_ptr(), cptr.data_ptr(),
+                                ctypes.byref(nc), device.stream_handle())
+    if st == _lib.ERR_CAPACITY:
+        # more than max_colours colours: the loop falls back to atomics
+        it._cache[key] = None
+        return None
+    _lib.check(st)
     ptr = cptr[:nc.value + 1].cpu().numpy().tolist()
     plan = ColourPlan(order, ptr, nc.value, colour)
     it._cache[key] = plan
