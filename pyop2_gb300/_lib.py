@@ -103,6 +103,8 @@ SIGNATURES = {
                                      ctypes.POINTER(ctypes.c_size_t)]),
     "op2g_colour": (_i32, [_i64, _i32, ctypes.POINTER(_p), _pi32, ctypes.POINTER(_i64), _i32,
                            _p, ctypes.c_size_t, _p, _p, _p, _pi32, _p]),
+    "op2g_colour_noalloc": (_i32, [_i64, _i32, ctypes.POINTER(_p), _pi32, ctypes.POINTER(_i64),
+                                   _i32, _p, _p, _p, _pi32, _p]),
     "op2g_probe_fp64_peak": (_i32, [ctypes.POINTER(ctypes.c_double), _p]),
 }
 

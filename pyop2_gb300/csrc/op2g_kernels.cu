@@ -16,6 +16,8 @@
 
 #include <climits>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "op2g_internal.h"
@@ -904,6 +906,146 @@ op2g_status op2g_colour(int64_t ncells, int32_t nmaps, const int32_t *const *map
 }
 
 }  // extern "C"
+
+// ------------------------------------------------- colouring without allocation
+// For callers that cannot allocate device memory: a host embedding the
+// library in a process whose allocator belongs to someone else (a
+// framework's caching allocator, a memory pool sized up front), code running
+// while a CUDA graph is being captured, or a runtime that forbids
+// cudaMalloc after start-up.  op2g_colour_noalloc is op2g_colour with its
+// scratch taken from a fixed device array of this file instead of a
+// caller-provided workspace; the caller still passes every input and output.
+namespace {
+
+// Every GPU that loads the library holds this array until the process exits.
+__device__ __align__(256) unsigned char g_colour_scratch[OP2G_COLOUR_NOALLOC_SCRATCH_BYTES];
+
+std::mutex g_colour_scratch_mu;
+void *g_colour_scratch_addr[OP2G_NOALLOC_MAX_DEVICES];  // device address, per device
+
+// Device address of g_colour_scratch on the current device.  The host-side
+// name of a __device__ array is only a stand-in: the address has to come from
+// cudaGetSymbolAddress, done once per device with that device current.
+op2g_status colour_scratch(void **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return op2g::cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= OP2G_NOALLOC_MAX_DEVICES)
+        return op2g::fail(OP2G_ERR_UNSUPPORTED, "device index above OP2G_NOALLOC_MAX_DEVICES");
+    std::lock_guard<std::mutex> g(g_colour_scratch_mu);
+    if (!g_colour_scratch_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_colour_scratch);
+        if (e != cudaSuccess) return op2g::cuda_fail(e, "cudaGetSymbolAddress(g_colour_scratch)");
+        g_colour_scratch_addr[dev] = p;
+    }
+    *out = g_colour_scratch_addr[dev];
+    return OP2G_OK;
+}
+
+}  // namespace
+
+extern "C" op2g_status op2g_colour_noalloc(int64_t ncells, int32_t nmaps,
+                                           const int32_t *const *maps, const int32_t *arity,
+                                           const int64_t *target_size, int32_t max_colours,
+                                           int32_t *colour, int32_t *order, int64_t *colour_ptr,
+                                           int32_t *ncolours, void *stream) {
+    size_t need = 0;
+    op2g_status s = op2g_colour_workspace(ncells, nmaps, target_size, &need);
+    if (s != OP2G_OK) return s;
+    if (need > (size_t)OP2G_COLOUR_NOALLOC_SCRATCH_BYTES)
+        return op2g::fail(OP2G_ERR_CAPACITY,
+                          "op2g_colour_noalloc: problem needs " + std::to_string(need) +
+                              " bytes of scratch, above the fixed " +
+                              std::to_string((long long)OP2G_COLOUR_NOALLOC_SCRATCH_BYTES) +
+                              " (use op2g_colour with a workspace)");
+    if (max_colours <= 0 || max_colours > 64 * CW)
+        return op2g::fail(OP2G_ERR_INVALID, "max_colours must be in 1..256");
+    if (!maps || !arity || !colour || !order || !colour_ptr)
+        return op2g::fail(OP2G_ERR_INVALID, "NULL argument");
+    void *ws = nullptr;
+    s = colour_scratch(&ws);
+    if (s != OP2G_OK) return s;
+    cudaStream_t st = (cudaStream_t)stream;
+    // Same layout and steps as op2g_colour; everything that must start at
+    // zero is cleared here because the array keeps the previous call's data.
+    ColDev C;
+    memset(&C, 0, sizeof C);
+    C.nmaps = nmaps;
+    char *w = (char *)ws;
+    size_t off = 0;
+    for (int k = 0; k < nmaps; ++k) {
+        if (!maps[k] || arity[k] <= 0) return op2g::fail(OP2G_ERR_INVALID, "bad colouring map");
+        C.maps[k] = maps[k];
+        C.arity[k] = arity[k];
+        C.tsz[k] = target_size[k];
+        C.tmax[k] = (unsigned long long *)(w + off);
+        off = align256(off + sizeof(unsigned long long) * (size_t)target_size[k]);
+        C.tmask[k] = (unsigned long long *)(w + off);
+        off = align256(off + sizeof(unsigned long long) * CW * (size_t)target_size[k]);
+        CK(cudaMemsetAsync(C.tmask[k], 0, sizeof(unsigned long long) * CW * target_size[k], st));
+    }
+    const long long nch = (ncells + COL_CHUNK - 1) / COL_CHUNK;
+    const long long nh = nch * 256 + 1;
+    long long *hist = (long long *)(w + off);
+    off = align256(off + sizeof(long long) * nh);
+    long long *base = (long long *)(w + off);
+    off = align256(off + sizeof(long long) * nh);
+    long long *scan = (long long *)(w + off);
+    off = align256(off + sizeof(long long) * scan_tmp_elems(nh));
+    unsigned long long *remaining = (unsigned long long *)(w + off);
+    int *err = (int *)(remaining + 1);
+    CK(cudaMemsetAsync(colour, 0xff, sizeof(int) * ncells, st));
+    CK(cudaMemsetAsync(err, 0, sizeof(int), st));
+    const unsigned grid = grid_for(ncells, 256);
+    unsigned long long left = (unsigned long long)ncells;
+    int rounds = 0;
+    while (left > 0) {
+        if (++rounds > 100000) return op2g::fail(OP2G_ERR_TIMEOUT, "colouring did not converge");
+        for (int k = 0; k < nmaps; ++k)
+            CK(cudaMemsetAsync(C.tmax[k], 0, sizeof(unsigned long long) * target_size[k], st));
+        CK(cudaMemsetAsync(remaining, 0, sizeof(unsigned long long), st));
+        k_jp_prio<<<grid, 256, 0, st>>>(C, ncells, colour);
+        k_jp_select<<<grid, 256, 0, st>>>(C, ncells, colour, max_colours, remaining, err);
+        CK(cudaGetLastError());
+        int herr = 0;
+        CK(cudaMemcpyAsync(&left, remaining, sizeof left, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (herr & OP2G_DEVERR_CAPACITY)
+            return op2g::fail(OP2G_ERR_CAPACITY, "colouring needs more than max_colours colours");
+    }
+    long long hc[256];
+    long long cp[257];
+    CK(cudaMemsetAsync(hist, 0, sizeof(long long) * 257, st));
+    if (ncells > 0) k_col_hist<<<grid, 256, 0, st>>>(colour, ncells, hist);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(hc, hist, sizeof hc, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    int ncol = 0;
+    for (int k = 0; k < 256; ++k)
+        if (hc[k]) ncol = k + 1;
+    if (ncolours) *ncolours = ncol;
+    cp[0] = 0;
+    for (int k = 0; k < max_colours; ++k) cp[k + 1] = cp[k] + (k < ncol ? hc[k] : 0);
+    CK(cudaMemcpyAsync(colour_ptr, cp, sizeof(long long) * (max_colours + 1),
+                       cudaMemcpyHostToDevice, st));
+    if (ncells > 0 && ncol > 0) {
+        const long long nhist = nch * ncol;
+        CK(cudaMemsetAsync(hist, 0, sizeof(long long) * (nhist + 1), st));
+        k_col_chunk_hist<<<(unsigned)nch, 256, 0, st>>>(colour, ncells, COL_CHUNK, ncol, hist);
+        CK(cudaGetLastError());
+        s = scan_exclusive(hist, nhist + 1, scan, st);
+        if (s != OP2G_OK) return s;
+        k_transpose_base<<<(unsigned)((nhist + 255) / 256), 256, 0, st>>>(hist, nch, ncol, base);
+        k_col_scatter<<<(unsigned)nch, 32, sizeof(long long) * ncol, st>>>(colour, ncells, COL_CHUNK,
+                                                                          base, ncol, order);
+        CK(cudaGetLastError());
+    }
+    // the host arrays hc/cp are read by the copies above: wait for them
+    CK(cudaStreamSynchronize(st));
+    return OP2G_OK;
+}
 
 // ---------------------------------------------------------------- probe
 namespace {
