@@ -175,6 +175,93 @@ def run_reference(args):
     return 0
 
 
+def _time_loop(loop, steps, warmup):
+    """Mean device ms per compute() of a prebuilt ParLoop (CUDA events)."""
+    import torch
+    for _ in range(warmup):
+        loop.compute()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        loop.compute()
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def measure_adjoint(op2, steps, warmup, n=64):
+    """Forward residual, its adjoint (VJP) and the fused forward+adjoint on
+    64^3 x 6 = 1,572,864 P1 tets (the differentiation configuration)."""
+    from pyop2_gb300 import workloads as W
+    p = W.build_nonlinear(op2, n=n, seed=0)
+    V, C = p["verts"].size, p["cells"].size
+    c2v, X = p["c2v"], p["X"]
+    F = op2.Dat(p["verts"], np.zeros(V))
+    lam = op2.Dat(p["verts"], p["lam"])
+    u = op2.Dat(p["verts"], p["u"])
+    k = op2.Dat(p["cells"], p["kappa"])
+    du = op2.Dat(p["verts"], np.zeros(V))
+    dk = op2.Dat(p["cells"], np.zeros(C))
+    fwd = op2.ParLoop(op2.Kernel(W.NL_RESIDUAL, "nl_residual"), p["cells"], F(op2.INC, c2v),
+                      X(op2.READ, c2v), u(op2.READ, c2v), k(op2.READ))
+    bwd = op2.ParLoop(op2.Kernel(W.NL_RESIDUAL_VJP, "nl_residual_vjp"), p["cells"],
+                      lam(op2.READ, c2v), X(op2.READ, c2v), u(op2.READ, c2v), k(op2.READ),
+                      du(op2.INC, c2v), dk(op2.WRITE))
+    fus = op2.ParLoop(op2.Kernel(W.NL_RESIDUAL_FUSED, "nl_residual_fused"), p["cells"],
+                      F(op2.INC, c2v), lam(op2.READ, c2v), X(op2.READ, c2v), u(op2.READ, c2v),
+                      k(op2.READ), du(op2.INC, c2v), dk(op2.WRITE))
+    tf = _time_loop(fwd, steps, warmup)
+    tb = _time_loop(bwd, steps, warmup)
+    tu = _time_loop(fus, steps, warmup)
+    return {"workload": "nonlinear_residual_p1_tet_64cube", "cells": C, "vertices": V,
+            "forward_ms": tf, "adjoint_ms": tb, "fused_forward_adjoint_ms": tu,
+            "ratio_forward_plus_adjoint_over_forward": (tf + tb) / tf,
+            "ratio_fused_over_forward": tu / tf, "launches": 3 * (steps + warmup)}
+
+
+def measure_batch(op2, steps, warmup, nmeshes=256):
+    """256 P2 meshes with log-uniform cell counts in [1e3, 1e6]: per-mesh
+    par_loop launches against one persistent launch replayed from a CUDA graph
+    (chunk and CTA size picked by the batch autotuner)."""
+    import torch
+    from pyop2_gb300 import meshes
+    from pyop2_gb300 import workloads as W
+    from pyop2_gb300.batch import autotune_batch
+    sizes = meshes.batch_sizes(nmeshes, seed=0)
+    probs = W.build_p2_batch(op2, sizes, seed=0)
+    loops = [op2.ParLoop(p["kernel"], p["cells"], *p["args"]) for p in probs]
+    ncells = sum(lp.iterset.size for lp in loops)
+
+    def plain():
+        for lp in loops:
+            lp.compute()
+    for _ in range(warmup):
+        plain()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        plain()
+    e1.record()
+    e1.synchronize()
+    t_plain = e0.elapsed_time(e1) / steps
+    batch, tuned = autotune_batch(loops)
+    for _ in range(warmup):
+        batch.replay()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(steps):
+        batch.replay()
+    e1.record()
+    e1.synchronize()
+    t_batch = e0.elapsed_time(e1) / steps
+    return {"workload": "p2_mass_laplace_256_meshes", "meshes": nmeshes, "cells": ncells,
+            "plain_ms": t_plain, "batched_graph_ms": t_batch, "speedup": t_plain / t_batch,
+            "batched_cells_per_s": ncells / (t_batch * 1e-3), "tuned": tuned,
+            "flops_per_cell": W.P2_FLOPS}
+
+
 def run_ours(args):
     import torch
     world, rank, local = _dist()
@@ -279,6 +366,8 @@ def run_ours(args):
         with open(tf) as f:
             m = re.search(r"dram_bytes_per_launch:\s*(\d+)", f.read())
         traffic = int(m.group(1)) if m else None
+    adjoint = measure_adjoint(op2, max(args.steps, 5), 3) if not args.skip_extras else None
+    batch = measure_batch(op2, 5, 3) if not args.skip_extras else None
     cpu = None
     if not args.no_cpu_baseline:
         coords = p["coords"]
@@ -307,6 +396,8 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "cells/s", "h2d_bytes_per_step": 8 * V,
                 "d2h_bytes_per_step": 8 * V},
+        "adjoint": adjoint,
+        "batch": batch,
         "gpu_launches": args.steps,
         "clocks": clk.summary(),
         "wall_s_timed": wall,
@@ -324,6 +415,8 @@ def main():
     ap.add_argument("--permute", action="store_true", help="random vertex numbering")
     ap.add_argument("--scatter", default=None, choices=["atomic", "warp", "colour"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-extras", action="store_true",
+                    help="only the headline action (no adjoint / batch measurements)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

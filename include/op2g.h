@@ -154,6 +154,10 @@ void op2g_kernel_destroy(op2g_kernel *k);
 /* Copy the generated CUDA source into buf (NUL-terminated, truncated to len);
  * *needed receives strlen+1. */
 op2g_status op2g_kernel_source(const op2g_kernel *k, char *buf, size_t len, size_t *needed);
+/* Load the compiled wrapper on the current device without launching it.
+ * Launches load it on first use; call this first when the first launch will
+ * happen inside a CUDA stream capture (module loading is not capturable). */
+op2g_status op2g_kernel_prepare(op2g_kernel *k);
 /* Number of device-pointer slots op2g_kernel_launch expects in `ptrs`:
  *   per argument, in order: DAT 1 (data), GLOBAL 1 (data, or the zeroed
  *   reduction temporary for INC), MAT 3 (values, rowptr int64, colidx int32),

@@ -85,6 +85,7 @@ SIGNATURES = {
     "op2g_kernel_destroy": (None, [_p]),
     "op2g_kernel_source": (_i32, [_p, ctypes.c_char_p, ctypes.c_size_t,
                                   ctypes.POINTER(ctypes.c_size_t)]),
+    "op2g_kernel_prepare": (_i32, [_p]),
     "op2g_kernel_num_ptrs": (_i32, [_p]),
     "op2g_kernel_num_regs": (_i32, [_p]),
     "op2g_kernel_launch": (_i32, [_p, ctypes.POINTER(LaunchDesc), _p]),

@@ -394,6 +394,13 @@ op2g_status op2g_kernel_source(const op2g_kernel *k, char *buf, size_t len, size
     return OP2G_OK;
 }
 
+op2g_status op2g_kernel_prepare(op2g_kernel *k) {
+    if (!k) return fail(OP2G_ERR_INVALID, "NULL kernel");
+    Loaded *L = nullptr;
+    return load_module(k->cubin, "op2g_wrap", "op2g_wrap_batched", k->sig.block_size, k->per_dev,
+                       k->mu, &L);
+}
+
 int32_t op2g_kernel_num_ptrs(const op2g_kernel *k) { return k ? k->sig.nptrs : -1; }
 
 int32_t op2g_kernel_num_regs(const op2g_kernel *k) {

@@ -70,23 +70,40 @@ def unit_cube_tets(n, permute=False, seed=0, jitter=0.0):
 
 
 def p2_square(n, jitter=0.2, seed=0):
-    """P2 Lagrange discretisation of an n x n split-square mesh.
+    """P2 Lagrange numbering of the n x n split-square mesh of unit_square_tris.
 
     Returns (coords float64[V, 2], cell2vert int32[C, 3], cell2dof int32[C, 6],
-    ndofs).  Dofs 0..V-1 are the vertices, then one dof per edge; local dof
-    order is (v0, v1, v2, e12, e02, e01) with e_ab the edge opposite... no:
-    e_ab joins local vertices a and b.
+    ndofs).  Dofs 0..V-1 are the vertices, then one per edge: horizontal
+    edges, vertical edges, quad diagonals, numbered analytically.  Local dof
+    order is (v0, v1, v2, e12, e02, e01), e_ab the edge joining local
+    vertices a and b.
     """
     coords, cells = unit_square_tris(n, jitter=jitter, seed=seed)
-    V = coords.shape[0]
-    e = np.concatenate([cells[:, [1, 2]], cells[:, [0, 2]], cells[:, [0, 1]]])
-    e.sort(axis=1)
-    key = e[:, 0].astype(np.int64) * V + e[:, 1]
-    uniq, inv = np.unique(key, return_inverse=True)
-    C = cells.shape[0]
-    edge_ids = inv.reshape(3, C).T + V
-    c2d = np.concatenate([cells, edge_ids], axis=1).astype(np.int32)
-    return coords, cells, c2d, V + len(uniq)
+    V = (n + 1) * (n + 1)
+    qi, qj = np.meshgrid(np.arange(n), np.arange(n), indexing="xy")
+    qi, qj = qi.ravel(), qj.ravel()
+    H = lambda i, j: V + j * n + i                                   # (i,j)-(i+1,j)
+    Vt = lambda i, j: V + n * (n + 1) + j * (n + 1) + i              # (i,j)-(i,j+1)
+    D = lambda i, j: V + 2 * n * (n + 1) + j * n + i                 # (i,j)-(i+1,j+1)
+    c2d = np.empty((2 * n * n, 6), dtype=np.int64)
+    c2d[:, :3] = cells
+    # lower [v00, v10, v11]: e12 = v10-v11, e02 = v00-v11, e01 = v00-v10
+    c2d[0::2, 3] = Vt(qi + 1, qj)
+    c2d[0::2, 4] = D(qi, qj)
+    c2d[0::2, 5] = H(qi, qj)
+    # upper [v00, v11, v01]: e12 = v11-v01, e02 = v00-v01, e01 = v00-v11
+    c2d[1::2, 3] = H(qi, qj + 1)
+    c2d[1::2, 4] = Vt(qi, qj)
+    c2d[1::2, 5] = D(qi, qj)
+    return coords, cells, c2d.astype(np.int32), V + 2 * n * (n + 1) + n * n
+
+
+def batch_sizes(nmeshes=256, lo=1e3, hi=1e6, seed=0):
+    """Cell counts drawn log-uniformly in [lo, hi] and the grid size n of each
+    mesh (2 n^2 cells, n = round(sqrt(C / 2)))."""
+    rng = np.random.default_rng(seed)
+    cells = np.exp(rng.uniform(np.log(lo), np.log(hi), nmeshes))
+    return [max(1, int(round(np.sqrt(c / 2)))) for c in cells]
 
 
 def extruded_prisms(n, layers, seed=0, jitter=0.2):

@@ -334,7 +334,10 @@ class Parloop:
         loop = self._loop_desc(scatter, block_size)
         k = compile_signature(self.local_kernel.source, self.local_kernel.name, loop, argdescs,
                               table.key())
+        device.require()
+        _lib.call("op2g_kernel_prepare", k.handle)   # module loaded outside any capture
         self._built = (scatter, block_size, k, table, argdescs)
+        self._launch_cache = None
         return k
 
     # ---- execution
@@ -375,27 +378,35 @@ class Parloop:
     def __call__(self):
         self.compute()
 
-    def compute(self):
+    def launch_desc(self):
+        """Synchronise the arguments to the device and return the launch
+        descriptor of this loop (cached; pointer arrays kept alive on self).
+        Also updates Mat assembly states as the reference does before a loop
+        (pyop2/parloop.py:279-301)."""
         device.require()
         if self._built is None:
             self.build()
         scatter, bs, k, table, argdescs = self._built
         it = self.iterset
-        # Mat assembly state (pyop2/parloop.py:279-301, 454-468)
         for a in self.args:
             if isinstance(a, MatLegacyArg):
                 a.data.change_assembly_state(Mat.ADD_VALUES if a.access is Access.INC
                                              else Mat.INSERT_VALUES)
         ptrs, err = self._pointers(table, k)
-        dbg_err = None
-        if configuration["debug"] and err is None:
-            dbg_err = torch.zeros(1, dtype=torch.int32, device=device.device())
-            err = dbg_err
+        dbg = configuration["debug"] and err is None
+        cache = getattr(self, "_launch_cache", None)
+        if cache is not None and cache[0] == ptrs and cache[1] == dbg:
+            return cache[2]
+        if dbg:
+            self._dbg_err = torch.zeros(1, dtype=torch.int32, device=device.device())
+            err = self._dbg_err
+        else:
+            self._dbg_err = None
         P = (ctypes.c_void_p * max(1, len(ptrs)))(*ptrs)
         toset = (ctypes.c_int64 * max(1, len(table.objs)))()
-        for i, e in enumerate(table.entries):
+        for i in range(len(table.entries)):
             toset[i] = 2**62
-        for i, a in enumerate(self.args):
+        for a in self.args:
             if isinstance(a, DatLegacyArg) and a.map_ is not None:
                 toset[table.add(a.map_)] = a.data.dataset.total_size
         D = _lib.LaunchDesc()
@@ -405,21 +416,14 @@ class Parloop:
         D.map_toset = toset
         D.layers_per_entity = self._layers_per_entity()
         D.grid = 0
-        st = device.stream_handle()
-        if scatter == _lib.SCATTER_PLAIN:
-            plan = colour_plan(self)
-            base_idx = it._indices_mirror.dev() if isinstance(it, Subset) else None
-            order = plan.order if base_idx is None else plan.order_for_subset(base_idx)
-            D.indices = order.data_ptr()
-            for c in range(plan.ncolours):
-                D.start, D.end = plan.ptr[c], plan.ptr[c + 1]
-                if D.end > D.start:
-                    _lib.call("op2g_kernel_launch", k.handle, ctypes.byref(D), st)
-        else:
-            D.indices = it._indices_mirror.dev().data_ptr() if isinstance(it, Subset) else None
-            D.start, D.end = 0, it.size
-            _lib.call("op2g_kernel_launch", k.handle, ctypes.byref(D), st)
-        # state updates
+        D.indices = it._indices_mirror.dev().data_ptr() if isinstance(it, Subset) else None
+        D.start, D.end = 0, it.size
+        self._keep = (P, toset)
+        self._launch_cache = (ptrs, dbg, D)
+        return D
+
+    def mark_written(self):
+        """State updates after a launch (pyop2/parloop.py:454-468)."""
         for a in self.args:
             if a.access is Access.READ or isinstance(a, PassthroughArg):
                 continue
@@ -432,9 +436,29 @@ class Parloop:
                 a.data.increment_dat_version()
                 if isinstance(a, DatLegacyArg):
                     a.data.halo_valid = False
-        if dbg_err is not None:
-            e = int(dbg_err.item())
+
+    def compute(self):
+        D = self.launch_desc()
+        scatter, bs, k, table, argdescs = self._built
+        st = device.stream_handle()
+        if scatter == _lib.SCATTER_PLAIN:
+            plan = colour_plan(self)
+            start, end, idx = D.start, D.end, D.indices
+            D.indices = plan.order.data_ptr()
+            try:
+                for c in range(plan.ncolours):
+                    D.start, D.end = plan.ptr[c], plan.ptr[c + 1]
+                    if D.end > D.start:
+                        _lib.call("op2g_kernel_launch", k.handle, ctypes.byref(D), st)
+            finally:
+                D.start, D.end, D.indices = start, end, idx
+        else:
+            _lib.call("op2g_kernel_launch", k.handle, ctypes.byref(D), st)
+        self.mark_written()
+        if self._dbg_err is not None:
+            e = int(self._dbg_err.item())
             if e & _lib.DEVERR_MAP_BOUNDS:
+                self._dbg_err.zero_()
                 raise MapValueError("par_loop %s: a map value is outside its target set"
                                     % self.local_kernel.name)
 

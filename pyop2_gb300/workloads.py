@@ -144,3 +144,251 @@ def build_p1_3d(op2, n=128, permute=False, seed=0):
         op2.par_loop(k, cset, y(op2.INC, c2v), X(op2.READ, c2v), x(op2.READ, c2v))
     return dict(run=run, y=y, cells=cset, verts=verts, c2v=c2v, X=X, x=x, kernel=k,
                 coords=coords, cellmap=cells)
+
+
+# ------------------------------------------------------- nonlinear residual
+# F(u)_i = sum_e int kappa_e (1 + u^2) grad u . grad v_i - f v_i, P1 tets, f = 1.
+# With C the cofactor matrix (rows b x c, c x a, a x b) and d = u_k - u_0:
+#   v = C^T d = det grad u,  G_0 = -(C_0 + C_1 + C_2), G_k = C_{k-1},
+#   q = (sum u_i^2 + (sum u_i)^2) / 20 = (1/vol) int u^2,
+#   F_i = kappa (1 + q) (G_i . v) / (6 |det|) - |det| / 24.
+_TET_GEOM = r"""
+  const double a0 = X[3] - X[0], a1 = X[4] - X[1], a2 = X[5]  - X[2];
+  const double b0 = X[6] - X[0], b1 = X[7] - X[1], b2 = X[8]  - X[2];
+  const double c0 = X[9] - X[0], c1 = X[10] - X[1], c2 = X[11] - X[2];
+  const double C00 = b1 * c2 - b2 * c1, C01 = b2 * c0 - b0 * c2, C02 = b0 * c1 - b1 * c0;
+  const double C10 = a2 * c1 - a1 * c2, C11 = a0 * c2 - a2 * c0, C12 = a1 * c0 - a0 * c1;
+  const double C20 = a1 * b2 - a2 * b1, C21 = a2 * b0 - a0 * b2, C22 = a0 * b1 - a1 * b0;
+  const double det = a0 * C00 + a1 * C01 + a2 * C02;
+  const double adet = fabs(det);
+  const double s = 1.0 / (6.0 * adet);
+  const double d0 = u[1] - u[0], d1 = u[2] - u[0], d2 = u[3] - u[0];
+  const double v0 = C00 * d0 + C10 * d1 + C20 * d2;
+  const double v1 = C01 * d0 + C11 * d1 + C21 * d2;
+  const double v2 = C02 * d0 + C12 * d1 + C22 * d2;
+  const double S = u[0] + u[1] + u[2] + u[3];
+  const double q = (u[0] * u[0] + u[1] * u[1] + u[2] * u[2] + u[3] * u[3] + S * S) * 0.05;
+"""
+
+NL_RESIDUAL = r"""
+static void nl_residual(double *restrict F, const double *restrict X,
+                        const double *restrict u, const double *restrict kappa)
+{""" + _TET_GEOM + r"""
+  const double c = kappa[0] * (1.0 + q) * s;
+  const double f4 = adet * (1.0 / 24.0);
+  const double w1 = c * (C00 * v0 + C01 * v1 + C02 * v2);
+  const double w2 = c * (C10 * v0 + C11 * v1 + C12 * v2);
+  const double w3 = c * (C20 * v0 + C21 * v1 + C22 * v2);
+  F[0] += -(w1 + w2 + w3) - f4;
+  F[1] += w1 - f4;
+  F[2] += w2 - f4;
+  F[3] += w3 - f4;
+}
+"""
+NL_RESIDUAL_FLOPS = 120
+
+# Vector-Jacobian product: given lambda on the vertices, L = lambda . F;
+#   vl = C^T (lambda_k - lambda_0),  gg = vl . v,
+#   dL/dkappa_e = (1 + q) gg / (6 |det|),
+#   dL/du_j += kappa / (6|det|) [ (u_j + S)/10 gg + (1 + q) (G_j . vl) ].
+NL_RESIDUAL_VJP = r"""
+static void nl_residual_vjp(const double *restrict lam, const double *restrict X,
+                            const double *restrict u, const double *restrict kappa,
+                            double *restrict du, double *restrict dkappa)
+{""" + _TET_GEOM + r"""
+  const double l0 = lam[1] - lam[0], l1 = lam[2] - lam[0], l2 = lam[3] - lam[0];
+  const double vl0 = C00 * l0 + C10 * l1 + C20 * l2;
+  const double vl1 = C01 * l0 + C11 * l1 + C21 * l2;
+  const double vl2 = C02 * l0 + C12 * l1 + C22 * l2;
+  const double gg = vl0 * v0 + vl1 * v1 + vl2 * v2;
+  const double b = 1.0 + q;
+  dkappa[0] = b * gg * s;
+  const double a = kappa[0] * s;
+  const double t1 = C00 * vl0 + C01 * vl1 + C02 * vl2;
+  const double t2 = C10 * vl0 + C11 * vl1 + C12 * vl2;
+  const double t3 = C20 * vl0 + C21 * vl1 + C22 * vl2;
+  const double h = 0.1 * gg;
+  du[0] += a * ((u[0] + S) * h - b * (t1 + t2 + t3));
+  du[1] += a * ((u[1] + S) * h + b * t1);
+  du[2] += a * ((u[2] + S) * h + b * t2);
+  du[3] += a * ((u[3] + S) * h + b * t3);
+}
+"""
+NL_RESIDUAL_VJP_FLOPS = 170
+
+# Forward and VJP in one pass (lambda known when the residual is evaluated):
+# the geometry and grad u are computed once.
+NL_RESIDUAL_FUSED = r"""
+static void nl_residual_fused(double *restrict F, const double *restrict lam,
+                              const double *restrict X, const double *restrict u,
+                              const double *restrict kappa, double *restrict du,
+                              double *restrict dkappa)
+{""" + _TET_GEOM + r"""
+  const double b = 1.0 + q;
+  const double a = kappa[0] * s;
+  const double c = a * b;
+  const double f4 = adet * (1.0 / 24.0);
+  const double w1 = C00 * v0 + C01 * v1 + C02 * v2;
+  const double w2 = C10 * v0 + C11 * v1 + C12 * v2;
+  const double w3 = C20 * v0 + C21 * v1 + C22 * v2;
+  F[0] += -c * (w1 + w2 + w3) - f4;
+  F[1] += c * w1 - f4;
+  F[2] += c * w2 - f4;
+  F[3] += c * w3 - f4;
+  const double l0 = lam[1] - lam[0], l1 = lam[2] - lam[0], l2 = lam[3] - lam[0];
+  /* gg = vl . v = (lam - lam_0) . (w1, w2, w3) since w_k = C_k . v */
+  const double gg = l0 * w1 + l1 * w2 + l2 * w3;
+  const double vl0 = C00 * l0 + C10 * l1 + C20 * l2;
+  const double vl1 = C01 * l0 + C11 * l1 + C21 * l2;
+  const double vl2 = C02 * l0 + C12 * l1 + C22 * l2;
+  dkappa[0] = b * gg * s;
+  const double t1 = C00 * vl0 + C01 * vl1 + C02 * vl2;
+  const double t2 = C10 * vl0 + C11 * vl1 + C12 * vl2;
+  const double t3 = C20 * vl0 + C21 * vl1 + C22 * vl2;
+  const double h = 0.1 * gg;
+  du[0] += a * ((u[0] + S) * h - b * (t1 + t2 + t3));
+  du[1] += a * ((u[1] + S) * h + b * t1);
+  du[2] += a * ((u[2] + S) * h + b * t2);
+  du[3] += a * ((u[3] + S) * h + b * t3);
+}
+"""
+
+# Jacobian dF/du as 4x4 element blocks (for J^T lambda checks):
+#   J_ij = kappa / (6|det|) [ (u_j + S)/10 (G_i . v) + (1 + q) (G_i . G_j) ].
+NL_RESIDUAL_JACOBIAN = r"""
+static void nl_residual_jac(double A[4][4], const double *restrict X,
+                            const double *restrict u, const double *restrict kappa)
+{""" + _TET_GEOM + r"""
+  double G[4][3] = {{0, 0, 0}, {C00, C01, C02}, {C10, C11, C12}, {C20, C21, C22}};
+  for (int k = 0; k < 3; ++k) G[0][k] = -(G[1][k] + G[2][k] + G[3][k]);
+  const double a = kappa[0] * s, b = 1.0 + q;
+  for (int i = 0; i < 4; ++i) {
+    const double gv = G[i][0] * v0 + G[i][1] * v1 + G[i][2] * v2;
+    for (int j = 0; j < 4; ++j)
+      A[i][j] += a * ((u[j] + S) * 0.1 * gv +
+                      b * (G[i][0] * G[j][0] + G[i][1] * G[j][1] + G[i][2] * G[j][2]));
+  }
+}
+"""
+
+
+def build_nonlinear(op2, n=64, seed=0):
+    """Config 4 data: P1 tets of an n^3 cube, u ~ U[-1,1], kappa ~ lognormal(0, 0.5)
+    per cell, lambda ~ U[-1,1] (seeded)."""
+    coords, cells = meshes.unit_cube_tets(n, permute=False, seed=seed)
+    rng = np.random.default_rng(seed + 7)
+    V, C = coords.shape[0], cells.shape[0]
+    verts = op2.Set(V, "vertices")
+    cset = op2.Set(C, "cells")
+    c2v = op2.Map(cset, verts, 4, cells, "cell2vert")
+    X = op2.Dat(verts ** 3, coords, np.float64, "coords")
+    u = rng.uniform(-1, 1, V)
+    kappa = rng.lognormal(0.0, 0.5, C)
+    lam = rng.uniform(-1, 1, V)
+    return dict(verts=verts, cells=cset, c2v=c2v, X=X, u=u, kappa=kappa, lam=lam,
+                coords=coords, cellmap=cells)
+
+
+# ------------------------------------------------------------ P2 triangles
+def _p2_reference_matrices():
+    """Exact reference-triangle integrals of the P2 basis (v0, v1, v2, e12,
+    e02, e01): mass M and stiffness blocks K_ab = int d_a phi_i d_b phi_j.
+    Monomials integrate exactly: int_T xi^a eta^b = a! b! / (a + b + 2)!."""
+    from math import factorial
+    # polynomials as {(a, b): coeff} in xi, eta
+    L = [{(0, 0): 1.0, (1, 0): -1.0, (0, 1): -1.0}, {(1, 0): 1.0}, {(0, 1): 1.0}]
+
+    def mul(p, q):
+        r = {}
+        for (a, b), c in p.items():
+            for (d, e), f in q.items():
+                r[(a + d, b + e)] = r.get((a + d, b + e), 0.0) + c * f
+        return r
+
+    def add(p, q, s=1.0):
+        r = dict(p)
+        for k, v in q.items():
+            r[k] = r.get(k, 0.0) + s * v
+        return r
+
+    def scale(p, s):
+        return {k: s * v for k, v in p.items()}
+
+    def deriv(p, axis):
+        r = {}
+        for (a, b), c in p.items():
+            if axis == 0 and a > 0:
+                r[(a - 1, b)] = r.get((a - 1, b), 0.0) + a * c
+            if axis == 1 and b > 0:
+                r[(a, b - 1)] = r.get((a, b - 1), 0.0) + b * c
+        return r
+
+    def integ(p):
+        return sum(c * factorial(a) * factorial(b) / factorial(a + b + 2) for (a, b), c in p.items())
+
+    phi = [add(scale(mul(L[i], L[i]), 2.0), L[i], -1.0) for i in range(3)]
+    phi += [scale(mul(L[1], L[2]), 4.0), scale(mul(L[0], L[2]), 4.0), scale(mul(L[0], L[1]), 4.0)]
+    M = np.array([[integ(mul(a, b)) for b in phi] for a in phi])
+    K = {}
+    for ax in range(2):
+        for bx in range(2):
+            K[(ax, bx)] = np.array([[integ(mul(deriv(a, ax), deriv(b, bx))) for b in phi]
+                                    for a in phi])
+    return M, K
+
+
+def _p2_kernel():
+    M, K = _p2_reference_matrices()
+    mats = [M, K[(0, 0)], K[(0, 1)] + K[(1, 0)], K[(1, 1)]]
+    lines = [r"""static void p2_mass_laplace(double *restrict y, const double *restrict X,
+                            const double *restrict x, double *restrict norm)
+{
+  const double j00 = X[2] - X[0], j01 = X[4] - X[0];
+  const double j10 = X[3] - X[1], j11 = X[5] - X[1];
+  const double det = j00 * j11 - j01 * j10;
+  const double adet = fabs(det), ia = 1.0 / adet;
+  /* G = |det| J^{-1} J^{-T} */
+  const double G00 = (j11 * j11 + j01 * j01) * ia;
+  const double G01 = -(j10 * j11 + j00 * j01) * ia;
+  const double G11 = (j10 * j10 + j00 * j00) * ia;
+  const double w[4] = {adet, G00, G01, G11};"""]
+    flops = 20
+    for i in range(6):
+        terms = []
+        for m, R in enumerate(mats):
+            row = " + ".join("%.17g * x[%d]" % (R[i, j], j) for j in range(6) if R[i, j] != 0.0)
+            if row:
+                terms.append("w[%d] * (%s)" % (m, row))
+                flops += 2 * sum(1 for j in range(6) if R[i, j] != 0.0) + 2
+        lines.append("  const double c%d = %s;" % (i, " + ".join(terms)))
+    for i in range(6):
+        lines.append("  y[%d] += c%d;" % (i, i))
+    lines.append("  norm[0] += c0 * c0 + c1 * c1 + c2 * c2 + c3 * c3 + c4 * c4 + c5 * c5;")
+    lines.append("}")
+    flops += 12
+    return "\n".join(lines) + "\n", flops
+
+
+P2_MASS_LAPLACE, P2_FLOPS = _p2_kernel()
+
+
+def build_p2_batch(op2, sizes, seed=0):
+    """Config 3: one P2 mass+Laplace action problem per grid size n in sizes."""
+    out = []
+    k = op2.Kernel(P2_MASS_LAPLACE, "p2_mass_laplace")
+    for i, n in enumerate(sizes):
+        coords, cells, c2d, ndofs = meshes.p2_square(n, jitter=0.2, seed=seed + i)
+        rng = np.random.default_rng(seed + 1000 + i)
+        verts = op2.Set(coords.shape[0])
+        dofs = op2.Set(ndofs)
+        cset = op2.Set(cells.shape[0])
+        c2v = op2.Map(cset, verts, 3, cells)
+        cmap = op2.Map(cset, dofs, 6, c2d)
+        X = op2.Dat(verts ** 2, coords, np.float64)
+        x = op2.Dat(dofs, rng.uniform(-1, 1, ndofs), np.float64)
+        y = op2.Dat(dofs, np.zeros(ndofs), np.float64)
+        g = op2.Global(1, 0.0, np.float64)
+        out.append(dict(cells=cset, c2v=c2v, c2d=cmap, X=X, x=x, y=y, g=g, kernel=k,
+                        args=(y(op2.INC, cmap), X(op2.READ, c2v), x(op2.READ, cmap),
+                              g(op2.INC))))
+    return out
