@@ -262,6 +262,120 @@ def measure_batch(op2, steps, warmup, nmeshes=256):
             "flops_per_cell": W.P2_FLOPS}
 
 
+def measure_sparsity_assembly(op2, p, steps, warmup):
+    """Configuration 2b on the benchmark mesh: GPU sparsity build (block CSR,
+    bit-exact pattern), CSR assembly of the 4x4 element matrices and SpMV."""
+    import torch
+    from pyop2_gb300 import workloads as W
+    from pyop2_gb300.types.mat import Sparsity
+    t = []
+    sp = None
+    for i in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sp = Sparsity.__new__(Sparsity, (p["verts"] ** 1, p["verts"] ** 1),
+                              [(p["c2v"], p["c2v"], None)])
+        sp._initialized = False           # force a rebuild (bypass the object cache)
+        sp.__init__((p["verts"] ** 1, p["verts"] ** 1), [(p["c2v"], p["c2v"], None)])
+        torch.cuda.synchronize()
+        t.append(time.perf_counter() - t0)
+    A = op2.Mat(sp)
+    asm = op2.ParLoop(op2.Kernel(W.P1_3D_LAPLACE_MATRIX, "p1_laplace_3d_mat"), p["cells"],
+                      A(op2.INC, (p["c2v"], p["c2v"])), p["X"](op2.READ, p["c2v"]))
+    t_asm = _time_loop(asm, steps, warmup)
+    y = op2.Dat(p["verts"])
+    for _ in range(warmup):
+        A.mult(p["x"], y)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        A.mult(p["x"], y)
+    e1.record()
+    e1.synchronize()
+    t_spmv = e0.elapsed_time(e1) / steps
+    C = p["cells"].size
+    nnz = sp.nblocks
+    out = {"workload": "p1_tet_laplace_128cube_csr", "nnz": nnz, "rows": p["verts"].size,
+           "sparsity_build_ms": 1e3 * min(t), "assembly_ms": t_asm,
+           "assembly_cells_per_s": C / (t_asm * 1e-3), "spmv_ms": t_spmv,
+           "spmv_gbs": (nnz * 12 + p["verts"].size * 8 * 3) / (t_spmv * 1e-3) / 1e9}
+    del A, sp
+    return out
+
+
+def measure_prisms(op2, steps, warmup):
+    """Configuration 5: 256^2 x 64 extruded prisms, P1 elasticity with 8 RHS:
+    matrix-free action, its adjoint (displacement and Lame fields), both in
+    one CUDA graph; BAIJ 3x3 sparsity and assembly."""
+    import torch
+    from pyop2_gb300 import workloads as W
+    p = W.build_prisms(op2, n=256, layers=65, seed=0)
+    NR = p["nrhs"]
+    nodes, cells, c2n, c2c = p["nodes"], p["cells"], p["c2n"], p["c2c"]
+    ds = op2.DataSet(nodes, (NR, 3))
+    u = op2.Dat(ds, p["u"])
+    w = op2.Dat(ds, p["w"])
+    y = op2.Dat(ds)
+    du = op2.Dat(ds)
+    dL = op2.Dat(p["prisms"] ** 2)
+    act = op2.ParLoop(op2.Kernel(W.PRISM_ELASTICITY_ACTION, "prism_elasticity"), cells,
+                      y(op2.INC, c2n), p["X"](op2.READ, c2n), u(op2.READ, c2n),
+                      p["L"](op2.READ, c2c))
+    adj = op2.ParLoop(op2.Kernel(W.PRISM_ELASTICITY_VJP, "prism_elasticity_vjp"), cells,
+                      w(op2.READ, c2n), p["X"](op2.READ, c2n), u(op2.READ, c2n),
+                      p["L"](op2.READ, c2c), du(op2.INC, c2n), dL(op2.WRITE, c2c))
+    t_act = _time_loop(act, steps, warmup)
+    t_adj = _time_loop(adj, steps, warmup)
+    # both in one graph
+    for lp in (act, adj):
+        lp.launch_desc()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    from pyop2_gb300 import _lib, device
+    import ctypes
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            for lp in (act, adj):
+                _lib.call("op2g_kernel_launch", lp._built[2].handle,
+                          ctypes.byref(lp.launch_desc()), device.stream_handle())
+    torch.cuda.current_stream().wait_stream(s)
+    for _ in range(warmup):
+        g.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        g.replay()
+    e1.record()
+    e1.synchronize()
+    t_graph = e0.elapsed_time(e1) / steps
+    for lp in (act, adj):
+        lp.mark_written()
+    # BAIJ sparsity + assembly
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sp = op2.Sparsity((nodes ** 3, nodes ** 3), [(c2n, c2n, None)])
+    torch.cuda.synchronize()
+    t_sp = time.perf_counter() - t0
+    A = op2.Mat(sp)
+    asm = op2.ParLoop(op2.Kernel(W.PRISM_ELASTICITY_MATRIX, "prism_elasticity_mat"), cells,
+                      A(op2.INC, (c2n, c2n)), p["X"](op2.READ, c2n), p["L"](op2.READ, c2c))
+    t_asm = _time_loop(asm, 2, 1)
+    C = p["ncell"]
+    out = {"workload": "prism_elasticity_256x256x64_8rhs", "cells": C, "nodes": p["nnodes"],
+           "rhs": NR, "action_ms": t_act, "adjoint_ms": t_adj,
+           "graph_action_adjoint_ms": t_graph,
+           "action_cell_rhs_per_s": C * NR / (t_act * 1e-3),
+           "adjoint_over_action": t_adj / t_act,
+           "baij_blocks": sp.nblocks, "sparsity_build_ms": 1e3 * t_sp,
+           "assembly_ms": t_asm, "values_gb": sp.nblocks * 9 * 8 / 1e9}
+    del A, sp
+    return out
+
+
 def run_ours(args):
     import torch
     world, rank, local = _dist()
@@ -366,8 +480,10 @@ def run_ours(args):
         with open(tf) as f:
             m = re.search(r"dram_bytes_per_launch:\s*(\d+)", f.read())
         traffic = int(m.group(1)) if m else None
+    sparsity = measure_sparsity_assembly(op2, p, 5, 3) if not args.skip_extras else None
     adjoint = measure_adjoint(op2, max(args.steps, 5), 3) if not args.skip_extras else None
     batch = measure_batch(op2, 5, 3) if not args.skip_extras else None
+    prisms = measure_prisms(op2, 5, 2) if not args.skip_extras else None
     cpu = None
     if not args.no_cpu_baseline:
         coords = p["coords"]
@@ -396,8 +512,10 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "cells/s", "h2d_bytes_per_step": 8 * V,
                 "d2h_bytes_per_step": 8 * V},
+        "sparsity_assembly": sparsity,
         "adjoint": adjoint,
         "batch": batch,
+        "prisms": prisms,
         "gpu_launches": args.steps,
         "clocks": clk.summary(),
         "wall_s_timed": wall,

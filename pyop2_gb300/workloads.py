@@ -392,3 +392,208 @@ def build_p2_batch(op2, sizes, seed=0):
                         args=(y(op2.INC, cmap), X(op2.READ, c2v), x(op2.READ, cmap),
                               g(op2.INC))))
     return out
+
+
+# ---------------------------------------------------- extruded P1 prisms
+# Linear elasticity sigma = lambda tr(grad u) I + mu (grad u + grad u^T) on
+# straight vertical prisms: node (a, k) = base vertex a (0..2), level k (0
+# bottom, 1 top); N_ak = lambda_a(xi, eta) phi_k(zeta).  The in-plane
+# gradients of lambda_a are constant, d/dz N_ak = lambda_a phi_k' / h.
+# Quadrature: 3-point degree-2 triangle rule x 2-point Gauss in zeta, exact
+# for the integrands (degree 2 in (xi, eta) and in zeta).  Dats of the
+# displacement have shape (NRHS, 3) per node, packed [node][rhs][component].
+PRISM_NRHS = 8
+
+_PRISM_GEOM = r"""
+  const double j00 = X[3] - X[0], j01 = X[6] - X[0];
+  const double j10 = X[4] - X[1], j11 = X[7] - X[1];
+  const double det2 = j00 * j11 - j01 * j10;
+  const double h = X[11] - X[2];
+  const double id = 1.0 / det2;
+  double g[3][2];
+  g[1][0] = j11 * id;  g[1][1] = -j01 * id;
+  g[2][0] = -j10 * id; g[2][1] = j00 * id;
+  g[0][0] = -g[1][0] - g[2][0]; g[0][1] = -g[1][1] - g[2][1];
+  const double ih = 1.0 / h;
+  const double vol = fabs(det2 * h);
+  const double wq = vol * (1.0 / 12.0);   /* 6 points: 1/6 (triangle) x 1/2 (Gauss) */
+  const double TL[3][3] = {{2.0 / 3.0, 1.0 / 6.0, 1.0 / 6.0},
+                           {1.0 / 6.0, 2.0 / 3.0, 1.0 / 6.0},
+                           {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0}};
+  const double ZQ[2] = {0.5 - 0.28867513459481287, 0.5 + 0.28867513459481287};
+"""
+
+# grad of field F (indexed F[(node * NRHS + r) * 3 + c]) at quadrature point
+# (tq, zq) into du[c][d]; Gx/Gy/D precomputed per rhs.
+_PRISM_PREP = r"""
+    double Gx[2][3], Gy[2][3], D[3][3];
+    for (int c = 0; c < 3; ++c) {
+      for (int k = 0; k < 2; ++k) {
+        double sx = 0.0, sy = 0.0;
+        for (int a = 0; a < 3; ++a) {
+          const double v = FIELD[((a + 3 * k) * NRHS + r) * 3 + c];
+          sx += g[a][0] * v; sy += g[a][1] * v;
+        }
+        Gx[k][c] = sx; Gy[k][c] = sy;
+      }
+      for (int a = 0; a < 3; ++a)
+        D[a][c] = (FIELD[((a + 3) * NRHS + r) * 3 + c] - FIELD[(a * NRHS + r) * 3 + c]) * ih;
+    }
+"""
+
+
+def _prism_prep(field, prefix):
+    return (_PRISM_PREP.replace("FIELD", field).replace("Gx", prefix + "Gx")
+            .replace("Gy", prefix + "Gy").replace("D[", prefix + "D["))
+
+
+_PRISM_GRAD = r"""
+        double PRE_du[3][3];
+        for (int c = 0; c < 3; ++c) {
+          PRE_du[c][0] = z0 * PRE_Gx[0][c] + z1 * PRE_Gx[1][c];
+          PRE_du[c][1] = z0 * PRE_Gy[0][c] + z1 * PRE_Gy[1][c];
+          PRE_du[c][2] = TL[tq][0] * PRE_D[0][c] + TL[tq][1] * PRE_D[1][c] + TL[tq][2] * PRE_D[2][c];
+        }
+"""
+
+
+def _prism_grad(prefix):
+    return _PRISM_GRAD.replace("PRE_", prefix)
+
+
+PRISM_ELASTICITY_ACTION = (r"""
+#define NRHS %d
+static void prism_elasticity(double *restrict y, const double *restrict X,
+                             const double *restrict u, const double *restrict lame)
+{""" % PRISM_NRHS + _PRISM_GEOM + r"""
+  const double lam = lame[0], mu = lame[1];
+  for (int r = 0; r < NRHS; ++r) {""" + _prism_prep("u", "u") + r"""
+    double Sxy[2][3][2] = {{{0}}}, T[3][3] = {{0}};
+    for (int zq = 0; zq < 2; ++zq) {
+      const double z1 = ZQ[zq], z0 = 1.0 - z1;
+      for (int tq = 0; tq < 3; ++tq) {""" + _prism_grad("u") + r"""
+        const double tr = udu[0][0] + udu[1][1] + udu[2][2];
+        double s[3][3];
+        for (int c = 0; c < 3; ++c)
+          for (int d = 0; d < 3; ++d)
+            s[c][d] = mu * (udu[c][d] + udu[d][c]) + (c == d ? lam * tr : 0.0);
+        const double w0 = wq * z0, w1 = wq * z1;
+        for (int c = 0; c < 3; ++c) {
+          Sxy[0][c][0] += w0 * s[c][0]; Sxy[0][c][1] += w0 * s[c][1];
+          Sxy[1][c][0] += w1 * s[c][0]; Sxy[1][c][1] += w1 * s[c][1];
+          for (int a = 0; a < 3; ++a) T[a][c] += wq * TL[tq][a] * s[c][2];
+        }
+      }
+    }
+    for (int a = 0; a < 3; ++a)
+      for (int c = 0; c < 3; ++c) {
+        const double xy0 = g[a][0] * Sxy[0][c][0] + g[a][1] * Sxy[0][c][1];
+        const double xy1 = g[a][0] * Sxy[1][c][0] + g[a][1] * Sxy[1][c][1];
+        y[(a * NRHS + r) * 3 + c] += xy0 - T[a][c] * ih;
+        y[((a + 3) * NRHS + r) * 3 + c] += xy1 + T[a][c] * ih;
+      }
+  }
+}
+#undef NRHS
+""").replace("udu", "udu")
+PRISM_ACTION_FLOPS_PER_RHS = 800
+
+# Adjoint of L = sum_r w_r . y_r with y_r = K(lambda, mu) u_r:
+#   dL/du_r = K w_r (K symmetric), dL/dlambda = sum_r int tr(grad w_r) tr(grad u_r),
+#   dL/dmu = sum_r int 2 eps(w_r) : eps(u_r).
+PRISM_ELASTICITY_VJP = (r"""
+#define NRHS %d
+static void prism_elasticity_vjp(const double *restrict w, const double *restrict X,
+                                 const double *restrict u, const double *restrict lame,
+                                 double *restrict du, double *restrict dlame)
+{""" % PRISM_NRHS + _PRISM_GEOM + r"""
+  const double lam = lame[0], mu = lame[1];
+  double dl = 0.0, dm = 0.0;
+  for (int r = 0; r < NRHS; ++r) {""" + _prism_prep("w", "w") + _prism_prep("u", "u") + r"""
+    double Sxy[2][3][2] = {{{0}}}, T[3][3] = {{0}};
+    for (int zq = 0; zq < 2; ++zq) {
+      const double z1 = ZQ[zq], z0 = 1.0 - z1;
+      for (int tq = 0; tq < 3; ++tq) {""" + _prism_grad("w") + _prism_grad("u") + r"""
+        const double trw = wdu[0][0] + wdu[1][1] + wdu[2][2];
+        const double tru = udu[0][0] + udu[1][1] + udu[2][2];
+        double s[3][3], ee = 0.0;
+        for (int c = 0; c < 3; ++c)
+          for (int d = 0; d < 3; ++d) {
+            const double ew = wdu[c][d] + wdu[d][c];
+            s[c][d] = mu * ew + (c == d ? lam * trw : 0.0);
+            ee += ew * (udu[c][d] + udu[d][c]);
+          }
+        dl += wq * trw * tru;
+        dm += wq * 0.5 * ee;
+        const double w0 = wq * z0, w1 = wq * z1;
+        for (int c = 0; c < 3; ++c) {
+          Sxy[0][c][0] += w0 * s[c][0]; Sxy[0][c][1] += w0 * s[c][1];
+          Sxy[1][c][0] += w1 * s[c][0]; Sxy[1][c][1] += w1 * s[c][1];
+          for (int a = 0; a < 3; ++a) T[a][c] += wq * TL[tq][a] * s[c][2];
+        }
+      }
+    }
+    for (int a = 0; a < 3; ++a)
+      for (int c = 0; c < 3; ++c) {
+        const double xy0 = g[a][0] * Sxy[0][c][0] + g[a][1] * Sxy[0][c][1];
+        const double xy1 = g[a][0] * Sxy[1][c][0] + g[a][1] * Sxy[1][c][1];
+        du[(a * NRHS + r) * 3 + c] += xy0 - T[a][c] * ih;
+        du[((a + 3) * NRHS + r) * 3 + c] += xy1 + T[a][c] * ih;
+      }
+  }
+  dlame[0] = dl;
+  dlame[1] = dm;
+}
+#undef NRHS
+""")
+
+# 18 x 18 element stiffness matrix (3x3 blocks per node pair) into a BAIJ Mat.
+PRISM_ELASTICITY_MATRIX = (r"""
+static void prism_elasticity_mat(double A[18][18], const double *restrict X,
+                                 const double *restrict lame)
+{""" + _PRISM_GEOM + r"""
+  const double lam = lame[0], mu = lame[1];
+  for (int zq = 0; zq < 2; ++zq) {
+    const double z1 = ZQ[zq], z0 = 1.0 - z1;
+    for (int tq = 0; tq < 3; ++tq) {
+      double G[6][3];
+      for (int a = 0; a < 3; ++a) {
+        G[a][0] = g[a][0] * z0; G[a][1] = g[a][1] * z0; G[a][2] = -TL[tq][a] * ih;
+        G[a + 3][0] = g[a][0] * z1; G[a + 3][1] = g[a][1] * z1; G[a + 3][2] = TL[tq][a] * ih;
+      }
+      for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+          const double dot = G[i][0] * G[j][0] + G[i][1] * G[j][1] + G[i][2] * G[j][2];
+          for (int c = 0; c < 3; ++c)
+            for (int d = 0; d < 3; ++d)
+              A[3 * i + c][3 * j + d] += wq * (lam * G[i][c] * G[j][d] +
+                                               mu * ((c == d ? dot : 0.0) + G[i][d] * G[j][c]));
+        }
+    }
+  }
+}
+""")
+
+
+def build_prisms(op2, n=256, layers=65, seed=0, nrhs=PRISM_NRHS):
+    """Config 5: n x n split-square base extruded to `layers` levels
+    (layers - 1 prisms per column), P1 displacement (nrhs, 3) per node,
+    Lame (lambda, mu) per prism ~ lognormal(0, 0.3) (seeded)."""
+    bc, tri, base, offset, nnodes, ncoords = meshes.extruded_prisms(n, layers, seed=seed)
+    Cb = tri.shape[0]
+    ncell = Cb * (layers - 1)
+    rng = np.random.default_rng(seed + 5)
+    bset = op2.Set(Cb, "base_cells")
+    cells = op2.ExtrudedSet(bset, layers)
+    nodes = op2.Set(nnodes, "nodes")
+    prisms = op2.Set(ncell, "prisms")
+    c2n = op2.Map(cells, nodes, 6, base, "cell2node", offset)
+    c2c = op2.Map(cells, prisms, 1, (np.arange(Cb) * (layers - 1)).astype(np.int32), "cell2cell",
+                  np.ones(1, dtype=np.int32))
+    X = op2.Dat(nodes ** 3, ncoords, np.float64, "coords")
+    lame = np.stack([rng.lognormal(0.0, 0.3, ncell), rng.lognormal(0.0, 0.3, ncell)], axis=1)
+    L = op2.Dat(prisms ** 2, lame, np.float64, "lame")
+    u = rng.uniform(-1, 1, (nnodes, nrhs, 3))
+    w = rng.uniform(-1, 1, (nnodes, nrhs, 3))
+    return dict(cells=cells, nodes=nodes, prisms=prisms, c2n=c2n, c2c=c2c, X=X, L=L,
+                u=u, w=w, nrhs=nrhs, ncell=ncell, nnodes=nnodes)
