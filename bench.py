@@ -304,13 +304,13 @@ def measure_sparsity_assembly(op2, p, steps, warmup):
     return out
 
 
-def measure_prisms(op2, steps, warmup):
+def measure_prisms(op2, steps, warmup, n=256):
     """Configuration 5: 256^2 x 64 extruded prisms, P1 elasticity with 8 RHS:
     matrix-free action, its adjoint (displacement and Lame fields), both in
     one CUDA graph; BAIJ 3x3 sparsity and assembly."""
     import torch
     from pyop2_gb300 import workloads as W
-    p = W.build_prisms(op2, n=256, layers=65, seed=0)
+    p = W.build_prisms(op2, n=n, layers=65, seed=0)
     NR = p["nrhs"]
     nodes, cells, c2n, c2c = p["nodes"], p["cells"], p["c2n"], p["c2c"]
     ds = op2.DataSet(nodes, (NR, 3))
@@ -365,7 +365,7 @@ def measure_prisms(op2, steps, warmup):
                       A(op2.INC, (c2n, c2n)), p["X"](op2.READ, c2n), p["L"](op2.READ, c2c))
     t_asm = _time_loop(asm, 2, 1)
     C = p["ncell"]
-    out = {"workload": "prism_elasticity_256x256x64_8rhs", "cells": C, "nodes": p["nnodes"],
+    out = {"workload": "prism_elasticity_%dx%dx64_8rhs" % (n, n), "cells": C, "nodes": p["nnodes"],
            "rhs": NR, "action_ms": t_act, "adjoint_ms": t_adj,
            "graph_action_adjoint_ms": t_graph,
            "action_cell_rhs_per_s": C * NR / (t_act * 1e-3),
@@ -524,6 +524,26 @@ def run_ours(args):
     return 0
 
 
+def run_only(args):
+    """One secondary measurement on its own (used for ncu captures); prints
+    its JSON object."""
+    from pyop2_gb300.csrc import build as _b
+    _b.build()
+    from pyop2_gb300 import device, op2, workloads
+    device.require()
+    if args.only == "sparsity":
+        p = workloads.build_p1_3d(op2, n=args.size or N_CUBE, seed=0)
+        out = measure_sparsity_assembly(op2, p, args.steps, args.warmup)
+    elif args.only == "adjoint":
+        out = measure_adjoint(op2, args.steps, args.warmup, n=args.size or 64)
+    elif args.only == "batch":
+        out = measure_batch(op2, args.steps, args.warmup)
+    else:
+        out = measure_prisms(op2, args.steps, args.warmup, n=args.size or 256)
+    print(json.dumps({"only": args.only, "result": out}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -535,11 +555,18 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the headline action (no adjoint / batch measurements)")
+    ap.add_argument("--only", default=None,
+                    choices=["sparsity", "adjoint", "batch", "prisms"],
+                    help="run one secondary measurement alone (profiling runs)")
+    ap.add_argument("--size", type=int, default=None,
+                    help="with --only: mesh size (cube edge / prism base edge)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.only:
+        return run_only(args)
     return run_ours(args)
 
 
