@@ -190,6 +190,33 @@ def _time_loop(loop, steps, warmup):
     return e0.elapsed_time(e1) / steps
 
 
+def measure_strategies(op2, p, steps, warmup):
+    """The benchmark action under each INC conflict strategy (hardware
+    atomics, warp-aggregated atomics, greedy colouring), for the given
+    problem's numbering."""
+    from pyop2_gb300.configuration import configuration
+    out = {}
+    old = configuration["scatter"]
+    try:
+        for sc in ("atomic", "warp", "colour"):
+            configuration["scatter"] = sc
+            lp = op2.ParLoop(p["kernel"], p["cells"], p["y"](op2.INC, p["c2v"]),
+                             p["X"](op2.READ, p["c2v"]), p["x"](op2.READ, p["c2v"]))
+            t0 = time.perf_counter()
+            lp.compute()                    # builds the colouring plan when needed
+            import torch
+            torch.cuda.synchronize()
+            setup = time.perf_counter() - t0
+            out[sc] = {"ms": _time_loop(lp, steps, warmup), "first_call_s": setup}
+            if sc == "colour":
+                from pyop2_gb300.parloop import colour_plan
+                plan = colour_plan(lp)
+                out[sc]["colours"] = plan.ncolours if plan is not None else None
+    finally:
+        configuration["scatter"] = old
+    return out
+
+
 def measure_adjoint(op2, steps, warmup, n=64):
     """Forward residual, its adjoint (VJP) and the fused forward+adjoint on
     64^3 x 6 = 1,572,864 P1 tets (the differentiation configuration)."""
@@ -236,6 +263,20 @@ def measure_batch(op2, steps, warmup, nmeshes=256):
     def plain():
         for lp in loops:
             lp.compute()
+
+    def plain_api():
+        for pr in probs:
+            op2.par_loop(pr["kernel"], pr["cells"], *pr["args"])
+    for _ in range(warmup):
+        plain_api()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        plain_api()
+    e1.record()
+    e1.synchronize()
+    t_api = e0.elapsed_time(e1) / steps
     for _ in range(warmup):
         plain()
     torch.cuda.synchronize()
@@ -257,7 +298,9 @@ def measure_batch(op2, steps, warmup, nmeshes=256):
     e1.synchronize()
     t_batch = e0.elapsed_time(e1) / steps
     return {"workload": "p2_mass_laplace_256_meshes", "meshes": nmeshes, "cells": ncells,
-            "plain_ms": t_plain, "batched_graph_ms": t_batch, "speedup": t_plain / t_batch,
+            "plain_par_loop_ms": t_api, "plain_prebuilt_ms": t_plain,
+            "batched_graph_ms": t_batch, "speedup_vs_par_loop": t_api / t_batch,
+            "speedup_vs_prebuilt": t_plain / t_batch,
             "batched_cells_per_s": ncells / (t_batch * 1e-3), "tuned": tuned,
             "flops_per_cell": W.P2_FLOPS}
 
@@ -480,6 +523,12 @@ def run_ours(args):
         with open(tf) as f:
             m = re.search(r"dram_bytes_per_launch:\s*(\d+)", f.read())
         traffic = int(m.group(1)) if m else None
+    strategies = None
+    if not args.skip_extras:
+        strategies = {"lexicographic": measure_strategies(op2, p, 5, 2)}
+        pr = workloads.build_p1_3d(op2, n=N_CUBE, permute=True, seed=0)
+        strategies["random_permutation"] = measure_strategies(op2, pr, 5, 2)
+        del pr
     sparsity = measure_sparsity_assembly(op2, p, 5, 3) if not args.skip_extras else None
     adjoint = measure_adjoint(op2, max(args.steps, 5), 3) if not args.skip_extras else None
     batch = measure_batch(op2, 5, 3) if not args.skip_extras else None
@@ -512,6 +561,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "cells/s", "h2d_bytes_per_step": 8 * V,
                 "d2h_bytes_per_step": 8 * V},
+        "strategies": strategies,
         "sparsity_assembly": sparsity,
         "adjoint": adjoint,
         "batch": batch,

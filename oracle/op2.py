@@ -33,9 +33,9 @@ from oracle import build as _build
 READ, WRITE, RW, INC, MIN, MAX = 1, 2, 3, 4, 5, 6
 ON_BOTTOM, ON_TOP, ON_INTERIOR_FACETS, ALL = 1, 2, 3, 4
 
-_CTYPE = {"float64": "double", "float32": "float", "int32": "int32_t", "uint32": "uint32_t",
-          "int64": "int64_t", "uint64": "uint64_t", "int16": "int16_t", "uint16": "uint16_t",
-          "int8": "int8_t", "uint8": "uint8_t"}
+_CTYPE = {"float64": "double", "float32": "float", "int32": "int", "uint32": "unsigned int",
+          "int64": "long long", "uint64": "unsigned long long", "int16": "short",
+          "uint16": "unsigned short", "int8": "signed char", "uint8": "unsigned char"}
 
 # "parity": strict IEEE (no contraction) so results are reproducible;
 # "timing": the reference's JIT flags (pyop2/compilation.py:324-328).

@@ -1,0 +1,129 @@
+"""Edge cases on the GPU: empty iteration sets and subsets, Global-only
+loops, columns of one cell, tuple-shaped Dats, 64-bit integers, ragged
+extruded layers, Maps with ghost entries, and the autotuned strategy."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_empty_iteration_set(gpu_op2):
+    op2 = gpu_op2
+    s = op2.Set(0)
+    t = op2.Set(5)
+    m = op2.Map(s, t, 2, np.zeros((0, 2), dtype=np.int32))
+    d = op2.Dat(t, np.arange(5.0))
+    g = op2.Global(1, 3.0)
+    k = op2.Kernel("static void k(double *x, double *g) { x[0] += 1; x[1] += 1; g[0] += 1; }", "k")
+    op2.par_loop(k, s, d(op2.INC, m), g(op2.INC))
+    assert np.all(d.data_ro == np.arange(5.0)) and g.data_ro[0] == 3.0
+
+
+def test_empty_subset_and_global_only_loop(gpu_op2):
+    op2 = gpu_op2
+    s = op2.Set(100)
+    d = op2.Dat(s, np.ones(100))
+    op2.par_loop(op2.Kernel("static void k(double *x) { *x = 7; }", "k"), op2.Subset(s, []),
+                 d(op2.WRITE))
+    assert np.all(d.data_ro == 1.0)
+    g = op2.Global(1, 0, np.int64)
+    op2.par_loop(op2.Kernel("static void k(long long *g) { *g += 3; }", "k"), s, g(op2.INC))
+    assert g.data_ro[0] == 300
+
+
+def test_tuple_dim_and_int64(gpu_op2, oracle_op2):
+    res = []
+    for op2 in (gpu_op2, oracle_op2):
+        cells, verts = op2.Set(50), op2.Set(30)
+        vals = (np.arange(100) * 7 % 30).astype(np.int32)
+        m = op2.Map(cells, verts, 2, vals)
+        d = op2.Dat(op2.DataSet(verts, (2, 3)), np.zeros((30, 2, 3), dtype=np.int64), np.int64)
+        k = op2.Kernel("""static void k(long long d[2][2][3]) {
+            for (int i = 0; i < 2; ++i) for (int a = 0; a < 2; ++a) for (int b = 0; b < 3; ++b)
+              d[i][a][b] += (long long)(1 + i + 10 * a + 100 * b) << 33; }""", "k")
+        op2.par_loop(k, cells, d(op2.INC, m))
+        res.append(np.asarray(d.data_ro if hasattr(d, "data_ro") else d.data).copy())
+    assert np.array_equal(res[0], res[1])
+
+
+def test_one_cell_columns_and_ragged_layers(gpu_op2, oracle_op2):
+    out = []
+    for op2 in (gpu_op2, oracle_op2):
+        base = op2.Set(4)
+        layers = np.array([[0, 2], [1, 5], [2, 3], [0, 4]], dtype=np.int32)   # 1, 3, 0, 3 cells
+        ext = op2.ExtrudedSet(base, layers)
+        nodes = op2.Set(4 * 6)
+        m = op2.Map(ext, nodes, 2, np.array([[0, 6], [6, 12], [12, 18], [18, 0]], dtype=np.int32),
+                    offset=[1, 1])
+        d = op2.Dat(nodes, np.zeros(24))
+        k = op2.Kernel("static void k(double *x, int layer) { x[0] += 1 + layer; x[1] += 10; }",
+                       "k")
+        op2.par_loop(k, ext, d(op2.INC, m), pass_layer_arg=True)
+        out.append(np.asarray(d.data_ro if hasattr(d, "data_ro") else d.data).copy())
+    assert np.array_equal(out[0], out[1])
+    const = []
+    for op2 in (gpu_op2, oracle_op2):
+        ext = op2.ExtrudedSet(op2.Set(3), 2)     # one cell per column
+        nodes = op2.Set(3 * 2)
+        m = op2.Map(ext, nodes, 1, np.array([0, 2, 4], dtype=np.int32), offset=[1])
+        d = op2.Dat(nodes, np.zeros(6))
+        op2.par_loop(op2.Kernel("static void k(double *x) { x[0] += 1; }", "k"), ext,
+                     d(op2.INC, m))
+        const.append(np.asarray(d.data_ro if hasattr(d, "data_ro") else d.data).copy())
+    assert np.array_equal(const[0], const[1]) and const[0].sum() == 3
+
+
+def test_ghost_entities_are_not_iterated(gpu_op2):
+    """Sizes (core, owned, total): only [0, owned) is executed; maps may point
+    at ghost target entities."""
+    op2 = gpu_op2
+    cells = op2.Set((2, 4, 6))
+    verts = op2.Set((3, 5, 8))
+    m = op2.Map(cells, verts, 2, np.array([[0, 7], [1, 6], [2, 5], [3, 4], [0, 1], [1, 2]]))
+    d = op2.Dat(verts, np.zeros(8))
+    op2.par_loop(op2.Kernel("static void k(double *x) { x[0] += 1; x[1] += 1; }", "k"), cells,
+                 d(op2.INC, m))
+    full = d.data_ro_with_halos
+    assert np.array_equal(full, [1, 1, 1, 1, 1, 1, 1, 1])
+    assert d.data_ro.shape == (5,)
+
+
+def test_autotuned_strategy_is_correct(gpu_op2, oracle_op2):
+    from pyop2_gb300 import workloads as W
+    from pyop2_gb300.configuration import configuration
+    old = configuration["scatter"]
+    configuration["scatter"] = "auto"
+    try:
+        g = W.build_p1_3d(gpu_op2, n=20, seed=6)
+        g["run"]()
+        y = g["y"].data_ro.copy()
+    finally:
+        configuration["scatter"] = old
+    o = W.build_p1_3d(oracle_op2, n=20, seed=6)
+    o["run"]()
+    assert np.max(np.abs(y - o["y"].data)) <= 1e-12 * np.max(np.abs(o["y"].data))
+
+
+def test_debug_bounds_check_reports_bad_map(gpu_op2):
+    """With configuration['debug'] a map value outside the target set is
+    skipped on the device and reported as MapValueError (no device fault)."""
+    from pyop2_gb300.configuration import configuration
+    from pyop2_gb300.exceptions import MapValueError
+    op2 = gpu_op2
+    s, t = op2.Set(4), op2.Set(3)
+    m = op2.Map(s, t, 1, np.array([0, 1, 2, 2]))
+    d = op2.Dat(t, np.zeros(3))
+    # same map object, values checked against a smaller target size: use a
+    # Dat on a 2-entity set through a map onto a 3-entity set is rejected by
+    # type checking, so shrink the declared target size via a second map
+    t2 = op2.Set(2)
+    m2 = op2.Map(s, t2, 1, np.array([0, 1, 2, 1]))     # value 2 is out of range for t2
+    d2 = op2.Dat(t2, np.zeros(2))
+    configuration["debug"] = True
+    try:
+        with pytest.raises(MapValueError):
+            op2.par_loop(op2.Kernel("static void k(double *x) { x[0] += 1; }", "k"), s,
+                         d2(op2.INC, m2))
+    finally:
+        configuration["debug"] = False
+    assert d2.data_ro.sum() == 3.0       # the out-of-range contribution was skipped

@@ -31,7 +31,10 @@ def test_gpu_sized(gpu_op2, sc, sizes):
 
 @pytest.mark.parametrize("sc", UNSIZED, ids=lambda f: f.__name__)
 def test_gpu_unsized(gpu_op2, strategy, sc):
-    sc(gpu_op2)
+    if sc is S.sc_extrusion_write_coords:
+        sc(gpu_op2, sequential=False)
+    else:
+        sc(gpu_op2)
 
 
 @pytest.mark.parametrize("sc", [S.sc_indirect_inc, S.sc_global_inc, S.sc_indirect_min,
