@@ -141,89 +141,122 @@ __global__ void k_max_cand(const int *__restrict__ cand, long long n, int diag, 
     if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
-// One warp per row: gather candidate columns of every incident virtual cell
-// into shared memory, bitonic-sort them, count (pass 0) or write (pass 1) the
-// distinct ones.
+// One warp per row: insert the candidate columns of every incident virtual
+// cell into a per-warp open-addressing hash table in shared memory (empty
+// slot = -1, linear probing, table at least twice the largest candidate
+// count), collecting each first occurrence into a list; sort the distinct
+// columns (rank sort with shuffles when they fit a warp, bitonic otherwise)
+// and store them at the row's candidate offset.  A mesh row has ~100
+// candidates but ~15 distinct columns, so only the distinct ones are sorted.
+constexpr int ROW_HDR = 32;  // per-warp header ints (distinct counter)
+
+__device__ __forceinline__ unsigned col_hash(int c, unsigned mask) {
+    return ((unsigned)c * 2654435761u) & mask;
+}
+
+__device__ __forceinline__ void row_insert(int c, int *tab, unsigned mask, int tsize, int *uniq,
+                                           int *ucount, int *err) {
+    unsigned h = col_hash(c, mask);
+    for (int probe = 0; probe < tsize; ++probe) {
+        const int old = atomicCAS(&tab[h], -1, c);
+        if (old == -1) {
+            uniq[atomicAdd(ucount, 1)] = c;
+            return;
+        }
+        if (old == c) return;
+        h = (h + 1) & mask;
+    }
+    atomicOr(err, OP2G_DEVERR_CAPACITY);  // table full: cannot happen (tsize >= 2 x candidates)
+}
+
 __global__ void k_rows(SpDev S, const PairDev *__restrict__ pairs,
                        const long long *__restrict__ tptr, const long long *__restrict__ tlist,
-                       int cap, int pass, long long *__restrict__ rowcount,
-                       const long long *__restrict__ rowptr, int *__restrict__ colidx) {
+                       int tsize, int ucap, const long long *__restrict__ candptr,
+                       int *__restrict__ tmp, long long *__restrict__ rowcount) {
     extern __shared__ int smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
-    int *s = smem + warp * cap;
+    int *hdr = smem + warp * (ROW_HDR + tsize + ucap);
+    int *tab = hdr + ROW_HDR;
+    int *uniq = tab + tsize;
+    const unsigned mask = (unsigned)tsize - 1u;
     for (long long r = (long long)blockIdx.x * wpb + warp; r < S.nrows;
          r += (long long)gridDim.x * wpb) {
+        for (int i = lane; i < tsize; i += 32) tab[i] = -1;
+        if (lane == 0) hdr[0] = 0;
+        __syncwarp();
         const long long e0 = tptr[r], e1 = tptr[r + 1];
-        int n = 0;  // warp-uniform candidate count
-        for (long long eb = e0; eb < e1; eb += 32) {
-            const long long e = eb + lane;
-            int cnt = 0;
-            long long cent = 0;
-            int layer = 0, nl = 1;
-            const PairDev *P = nullptr;
-            if (e < e1) {
-                const long long code = tlist[e];
-                P = &pairs[(int)(code >> 56)];
-                long long rent;
-                if (vcell(S, *P, code & ((1ll << 56) - 1), rent, cent, layer, nl)) cnt = P->tc;
-            }
-            int off = cnt;  // inclusive warp scan
-            for (int o = 1; o < 32; o <<= 1) {
-                int t = __shfl_up_sync(0xffffffffu, off, o);
-                if (lane >= o) off += t;
-            }
-            const int tot = __shfl_sync(0xffffffffu, off, 31);
-            off -= cnt;
-            for (int j = 0; j < cnt; ++j) {
-                int c = col_of(S, *P, cent, j, layer, nl);
+        for (long long e = e0 + lane; e < e1; e += 32) {
+            const long long code = tlist[e];
+            const PairDev &P = pairs[(int)(code >> 56)];
+            long long rent, cent;
+            int layer, nl;
+            if (!vcell(S, P, code & ((1ll << 56) - 1), rent, cent, layer, nl)) continue;
+            for (int j = 0; j < P.tc; ++j) {
+                const int c = col_of(S, P, cent, j, layer, nl);
+                if (c < 0) continue;
                 if (c >= S.ncols) {
                     atomicOr(S.err, OP2G_DEVERR_MAP_BOUNDS);
-                    c = -1;
+                    continue;
                 }
-                if (n + off + j < cap) s[n + off + j] = c < 0 ? INT_MAX : c;
+                row_insert(c, tab, mask, tsize, uniq, hdr, S.err);
             }
-            n += tot;
         }
-        if (S.set_diag && r < S.ncols) {
-            if (lane == 0 && n < cap) s[n] = (int)r;
-            n += 1;
-        }
-        if (n > cap) {  // cannot happen: cap >= the largest candidate count
-            if (lane == 0) atomicOr(S.err, OP2G_DEVERR_CAPACITY);
-            continue;
-        }
-        int P2 = 1;
-        while (P2 < n) P2 <<= 1;
-        for (int i = n + lane; i < P2; i += 32) s[i] = INT_MAX;
+        if (S.set_diag && r < S.ncols && lane == 0)
+            row_insert((int)r, tab, mask, tsize, uniq, hdr, S.err);
         __syncwarp();
-        for (int k = 2; k <= P2; k <<= 1)
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                for (int i = lane; i < P2; i += 32) {
-                    const int ixj = i ^ j;
-                    if (ixj > i) {
-                        const int a = s[i], b = s[ixj];
-                        const bool up = (i & k) == 0;
-                        if ((a > b) == up) {
-                            s[i] = b;
-                            s[ixj] = a;
+        const int u = hdr[0];
+        int *out = tmp + candptr[r];
+        if (u <= 32) {
+            const int x = lane < u ? uniq[lane] : INT_MAX;
+            int rank = 0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) rank += __shfl_sync(0xffffffffu, x, j) < x;
+            if (lane < u) out[rank] = x;
+        } else {
+            int P2 = 1;
+            while (P2 < u) P2 <<= 1;
+            for (int i = u + lane; i < P2; i += 32) uniq[i] = INT_MAX;
+            __syncwarp();
+            for (int k = 2; k <= P2; k <<= 1)
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    for (int i = lane; i < P2; i += 32) {
+                        const int ixj = i ^ j;
+                        if (ixj > i) {
+                            const int a = uniq[i], b = uniq[ixj];
+                            if ((a > b) == ((i & k) == 0)) {
+                                uniq[i] = b;
+                                uniq[ixj] = a;
+                            }
                         }
                     }
+                    __syncwarp();
                 }
-                __syncwarp();
-            }
-        long long run = 0;
-        const long long out0 = pass ? rowptr[r] : 0;
-        for (int i0 = 0; i0 < P2; i0 += 32) {
-            const int i = i0 + lane;
-            const int x = i < P2 ? s[i] : INT_MAX;
-            const bool keep = x != INT_MAX && (i == 0 || s[i - 1] != x);
-            const unsigned b = __ballot_sync(0xffffffffu, keep);
-            if (pass && keep) colidx[out0 + run + __popc(b & ((1u << lane) - 1u))] = x;
-            run += __popc(b);
+            for (int i = lane; i < u; i += 32) out[i] = uniq[i];
         }
-        if (!pass && lane == 0) rowcount[r] = run;
+        if (lane == 0) rowcount[r] = u;
         __syncwarp();
+    }
+}
+
+// candptr[r] = cand[r] + (diagonal entry of row r), to be scanned.
+__global__ void k_cand_sizes(const int *__restrict__ cand, long long n, long long ncols, int diag,
+                             long long *__restrict__ candptr) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += stride)
+        candptr[r] = cand[r] + ((diag && r < ncols) ? 1 : 0);
+}
+
+// One warp per row: copy the sorted distinct columns to the CSR column array.
+__global__ void k_rows_copy(long long nrows, const long long *__restrict__ candptr,
+                            const int *__restrict__ tmp, const long long *__restrict__ rowptr,
+                            int *__restrict__ colidx) {
+    const int lane = threadIdx.x & 31;
+    const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long r = w0; r < nrows; r += nw) {
+        const long long o = rowptr[r], n = rowptr[r + 1] - o, c0 = candptr[r];
+        for (long long i = lane; i < n; i += 32) colidx[o + i] = tmp[c0 + i];
     }
 }
 
@@ -300,8 +333,9 @@ op2g_status scan_exclusive(long long *d, long long n, long long *tmp, cudaStream
 
 // ------------------------------------------------------- sparsity driver
 struct SpLayout {
-    size_t off_cnt, off_cand, off_fill, off_tlist, off_scan, off_pairs, off_misc, total;
-    long long ninc;
+    size_t off_cnt, off_cand, off_fill, off_tlist, off_scan, off_pairs, off_misc, off_candptr,
+        off_tmp, total;
+    long long ninc, ncand;
 };
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -324,6 +358,7 @@ op2g_status sp_prepare(const op2g_sparsity_desc *d, std::vector<PairDev> &pairs,
     S.slots = d->extruded ? (d->layer_slots > 0 ? d->layer_slots : 1) : 1;
     if (d->extruded && !d->layers) return op2g::fail(OP2G_ERR_INVALID, "extruded sparsity needs layers");
     L.ninc = 0;
+    L.ncand = 0;
     pairs.resize(d->npairs);
     for (int p = 0; p < d->npairs; ++p) {
         const op2g_sparsity_pair &q = d->pairs[p];
@@ -366,7 +401,9 @@ op2g_status sp_prepare(const op2g_sparsity_desc *d, std::vector<PairDev> &pairs,
         }
         P.nvirt = q.nent * S.slots;
         L.ninc += P.nvirt * P.tr;
+        L.ncand += P.nvirt * P.tr * P.tc;
     }
+    L.ncand += d->nrows;  // diagonal entries
     const long long n1 = d->nrows + 1;
     size_t off = 0;
     L.off_cnt = off; off = align256(off + sizeof(long long) * n1);
@@ -376,6 +413,8 @@ op2g_status sp_prepare(const op2g_sparsity_desc *d, std::vector<PairDev> &pairs,
     L.off_scan = off; off = align256(off + sizeof(long long) * scan_tmp_elems(n1));
     L.off_pairs = off; off = align256(off + sizeof(PairDev) * (d->npairs ? d->npairs : 1));
     L.off_misc = off; off = align256(off + 64);
+    L.off_candptr = off; off = align256(off + sizeof(long long) * n1);
+    L.off_tmp = off; off = align256(off + sizeof(int) * (L.ncand > 0 ? L.ncand : 1));
     L.total = off;
     return OP2G_OK;
 }
@@ -388,24 +427,36 @@ int sms_of_current() {
 }
 
 op2g_status sp_rows_launch(const SpDev &S, const PairDev *pd, const long long *tptr,
-                           const long long *tlist, int cap, int pass, long long *rowcount,
-                           const long long *rowptr, int *colidx, cudaStream_t st) {
+                           const long long *tlist, int max_cand, const long long *candptr,
+                           int *tmp, long long *rowcount, cudaStream_t st) {
     if (S.nrows == 0) return OP2G_OK;
-    const size_t per = (size_t)cap * sizeof(int);
+    int tsize = 32;
+    while (tsize < 2 * max_cand) tsize <<= 1;
+    int ucap = 32;
+    while (ucap < max_cand) ucap <<= 1;
+    const size_t per = (size_t)(ROW_HDR + tsize + ucap) * sizeof(int);
     int wpb = (int)((48 * 1024) / per);
     if (wpb > 8) wpb = 8;
     if (wpb < 1) wpb = 1;
     const size_t smem = per * wpb;
     if (smem > 227 * 1024)
-        return op2g::fail(OP2G_ERR_CAPACITY, "a sparsity row has more than 58,000 candidate columns");
-    if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        return op2g::fail(OP2G_ERR_CAPACITY, "a sparsity row has more than 18,000 candidate columns");
+    if (smem > 48 * 1024)
+        CK(cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     long long blocks = (S.nrows + wpb - 1) / wpb;
     const long long capb = (long long)sms_of_current() * 32;
     if (blocks > capb) blocks = capb;
-    k_rows<<<(unsigned)blocks, 32 * wpb, smem, st>>>(S, pd, tptr, tlist, cap, pass, rowcount, rowptr,
-                                                     colidx);
+    k_rows<<<(unsigned)blocks, 32 * wpb, smem, st>>>(S, pd, tptr, tlist, tsize, ucap, candptr, tmp,
+                                                     rowcount);
     CK(cudaGetLastError());
     return OP2G_OK;
+}
+
+unsigned grid_for_rows(long long nrows) {
+    long long g = (nrows * 32 + 255) / 256;
+    const long long cap = (long long)sms_of_current() * 16;
+    if (g > cap) g = cap;
+    return (unsigned)(g < 1 ? 1 : g);
 }
 
 // State kept in the workspace between count and fill (the candidate capacity).
@@ -480,10 +531,23 @@ op2g_status op2g_sparsity_count(const op2g_sparsity_desc *d, void *ws, size_t ws
     CK(cudaStreamSynchronize(st));
     if (hm.err & OP2G_DEVERR_MAP_BOUNDS)
         return op2g::fail(OP2G_ERR_BOUNDS, "a map value is outside the row or column set");
-    int cap = 32;
-    while (cap < hm.max_cand) cap <<= 1;
+    // candidate offsets (upper bound of each row's distinct columns)
+    long long *candptr = (long long *)(w + L.off_candptr);
+    int *tmp = (int *)(w + L.off_tmp);
+    {
+        long long nb = (d->nrows + 255) / 256;
+        if (nb > capb) nb = capb;
+        if (nb < 1) nb = 1;
+        k_cand_sizes<<<(unsigned)nb, 256, 0, st>>>(cand, d->nrows, d->ncols, d->set_diag ? 1 : 0,
+                                                   candptr);
+        CK(cudaGetLastError());
+        CK(cudaMemsetAsync(candptr + d->nrows, 0, sizeof(long long), st));
+        s = scan_exclusive(candptr, n1, scan, st);
+        if (s != OP2G_OK) return s;
+    }
+    int cap = hm.max_cand > 1 ? hm.max_cand : 1;
     CK(cudaMemcpyAsync(&misc->cap, &cap, sizeof(int), cudaMemcpyHostToDevice, st));
-    s = sp_rows_launch(S, pd, cnt, tlist, cap, 0, (long long *)rowptr, nullptr, nullptr, st);
+    s = sp_rows_launch(S, pd, cnt, tlist, cap, candptr, tmp, (long long *)rowptr, st);
     if (s != OP2G_OK) return s;
     CK(cudaMemsetAsync(rowptr + d->nrows, 0, sizeof(long long), st));
     s = scan_exclusive((long long *)rowptr, n1, scan, st);
@@ -512,16 +576,18 @@ op2g_status op2g_sparsity_fill(const op2g_sparsity_desc *d, void *ws, size_t ws_
     if (!rowptr || (!colidx && d->nrows > 0)) return op2g::fail(OP2G_ERR_INVALID, "NULL output");
     cudaStream_t st = (cudaStream_t)stream;
     char *w = (char *)ws;
-    long long *cnt = (long long *)(w + L.off_cnt);
-    long long *tlist = (long long *)(w + L.off_tlist);
-    PairDev *pd = (PairDev *)(w + L.off_pairs);
     SpMisc *misc = (SpMisc *)(w + L.off_misc);
-    S.err = &misc->err;
+    const long long *candptr = (const long long *)(w + L.off_candptr);
+    const int *tmp = (const int *)(w + L.off_tmp);
     int cap = 0;
     CK(cudaMemcpyAsync(&cap, &misc->cap, sizeof cap, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (cap < 32) return op2g::fail(OP2G_ERR_INVALID, "op2g_sparsity_fill before op2g_sparsity_count");
-    return sp_rows_launch(S, pd, cnt, tlist, cap, 1, nullptr, (const long long *)rowptr, colidx, st);
+    if (cap < 1) return op2g::fail(OP2G_ERR_INVALID, "op2g_sparsity_fill before op2g_sparsity_count");
+    if (d->nrows == 0) return OP2G_OK;
+    k_rows_copy<<<grid_for_rows(d->nrows), 256, 0, st>>>(d->nrows, candptr, tmp,
+                                                         (const long long *)rowptr, colidx);
+    CK(cudaGetLastError());
+    return OP2G_OK;
 }
 
 }  // extern "C"
