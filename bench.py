@@ -94,6 +94,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(value, device=None):
+    """Max of a per-rank float over all ranks of the default process group
+    (identity without one): the job time is the slowest replica's."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, steps, max_ms, world):
+    """Whole-job throughput of `world` replicas (weak scaling)."""
+    return world * steps * units_per_rank / (max_ms * 1e-3)
+
+
 def _dist():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -470,13 +487,8 @@ def run_ours(args):
         barrier()
         wall = time.perf_counter() - t0
     kern_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(kern_ms)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps * C / (total_ms * 1e-3)
+    total_ms = max_over_ranks(sum(kern_ms), device=dev)
+    value = job_rate(C, args.steps, total_ms, world)
 
     # end to end through the public API with host buffers: x in from pinned
     # host memory, par_loop, y back to host, every step
@@ -498,13 +510,8 @@ def run_ours(args):
         y_host.copy_(yt, non_blocking=True)
     e1.record(st)
     barrier()
-    e2e_ms = e0.elapsed_time(e1)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e = world * args.steps * C / (e2e_ms * 1e-3)
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1), device=dev)
+    e2e = job_rate(C, args.steps, e2e_ms, world)
 
     # FP64 ceiling: measured DFMA throughput of this GPU
     import ctypes
