@@ -157,6 +157,16 @@ class Dat(AbstractDat):
     def data_wo_with_halos(self):
         return self.data_with_halos
 
+    @property
+    def _is_allocated(self):
+        """True once a host buffer exists (storage is allocated lazily)."""
+        return self._m.host_allocated()
+
+    @property
+    def _data(self):
+        """The full host array including ghost entries."""
+        return self._m.host(write=False)
+
     # ---- device access
     @property
     def tensor(self):
