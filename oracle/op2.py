@@ -70,7 +70,9 @@ class Set:
 class ExtrudedSet(Set):
     _extruded = True
 
-    def __init__(self, parent, layers, periodic=False):
+    def __init__(self, parent, layers, periodic=False, extruded_periodic=None):
+        if extruded_periodic is not None:
+            periodic = extruded_periodic
         self.parent = parent
         self.sizes = parent.sizes
         lay = np.asarray(layers, dtype=np.int32)

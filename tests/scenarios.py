@@ -648,3 +648,66 @@ def sc_extruded_sparsity(op2):
     m = op2.Map(xtr_elements, xtr_nodes, 6, vals, "xtr_elem_node", np.ones(6, dtype=np.int32))
     sp = op2.Sparsity((xtr_nodes ** 1, xtr_nodes ** 1), [(m, m, None)])
     return np.asarray(sp.nnz).copy()
+
+
+# ------------------------------------------------------------------------
+# test/unit/test_indirect_loop.py:365-468 (composed map over extruded sets)
+def sc_composed_map_extrusion(op2, variable=False, subset=False):
+    arity = 3
+    if variable:
+        setC = op2.ExtrudedSet(op2.Set(2), [[1, 3], [0, 3]])
+        nodesetC = op2.Set(8)
+        mapC = op2.Map(setC, nodesetC, arity, values=[[5, 6, 7], [0, 1, 2]], offset=[2, 2, 2])
+        setA = op2.ExtrudedSet(op2.Set(3), [[0, 3], [1, 3], [0, 3]])
+        nodesetA = op2.Set(13)
+        datA = op2.Dat(op2.DataSet(nodesetA, 1), np.arange(13, dtype=np.float64))
+        mapA0 = op2.Map(setA, nodesetA, arity, values=[[8, 9, 10], [5, 6, 7], [0, 1, 2]],
+                        offset=[2, 2, 2])
+        expected = [0., 1., 2., 3., 4., 0., 0., 0.] if subset else [0., 1., 2., 3., 4., 5., 6., 7.]
+    else:
+        setC = op2.ExtrudedSet(op2.Set(2), 3)
+        nodesetC = op2.Set(10)
+        mapC = op2.Map(setC, nodesetC, arity, values=[[5, 6, 7], [0, 1, 2]], offset=[2, 2, 2])
+        setA = op2.ExtrudedSet(op2.Set(3), 3)
+        nodesetA = op2.Set(15)
+        datA = op2.Dat(op2.DataSet(nodesetA, 1), np.arange(15, dtype=np.float64))
+        mapA0 = op2.Map(setA, nodesetA, arity, values=[[10, 11, 12], [5, 6, 7], [0, 1, 2]],
+                        offset=[2, 2, 2])
+        expected = ([0., 1., 2., 3., 4., 0., 0., 0., 0., 0.] if subset
+                    else [0., 1., 2., 3., 4., 5., 6., 7., 8., 9.])
+    datC = op2.Dat(op2.DataSet(nodesetC, 1), dtype=np.float64)
+    mapA1 = op2.Map(setC, setA, 1, values=[1, 2])
+    mapA = op2.ComposedMap(mapA0, mapA1)
+    k = op2.Kernel("""
+    void copy(double *to, const double * restrict from) {
+        for (int i = 0; i < 3; ++i) { to[i] = from[i]; }
+    }""", "copy")
+    it = op2.Subset(setC, np.array([1], dtype=np.int32)) if subset else setC
+    op2.par_loop(k, it, datC(op2.WRITE, mapC), datA(op2.READ, mapA))
+    assert np.all(np.asarray(datC.data) == np.array(expected))
+
+
+def sc_extruded_regions(op2, region, periodic=False, variable=False):
+    """INC through an offset map under each iteration region, with the layer
+    argument; returns the result for cross-implementation comparison."""
+    nb = 5
+    if variable:
+        layers = np.array([[0, 5], [1, 6], [0, 3], [2, 6], [0, 6]], dtype=np.int32)
+    else:
+        layers = 6
+    base = op2.Set(nb)
+    ext = op2.ExtrudedSet(base, layers, extruded_periodic=periodic) if periodic else \
+        op2.ExtrudedSet(base, layers)
+    L = 6
+    nodes = op2.Set((nb + 1) * L)
+    vals = np.array([[i * L, (i + 1) * L] for i in range(nb)], dtype=np.int32)
+    kw = dict(offset=[1, 1])
+    if periodic:
+        kw["offset_quotient"] = [0, 1]
+    m = op2.Map(ext, nodes, 2, vals, **kw)
+    d = op2.Dat(nodes, np.zeros((nb + 1) * L))
+    nf = 2 if region == op2.ON_INTERIOR_FACETS else 1
+    k = op2.Kernel("static void k(double *x, int layer) { for (int i = 0; i < %d; ++i) "
+                   "x[i] += (i + 1) * (layer + 1); }" % (2 * nf), "k")
+    op2.par_loop(k, ext, d(op2.INC, m), iteration_region=region, pass_layer_arg=True)
+    return np.asarray(d.data).copy()

@@ -49,3 +49,9 @@ def test_oracle_extruded_sparsity_rows(oracle_op2):
     assert nnz.shape == (44,)
     # node 0 (column 0) lies only in element 0: 3 base nodes x (1 or 2 levels)
     assert nnz[0] == 6 and nnz[10] == 6 and nnz[5] == 9
+
+
+@pytest.mark.parametrize("variable", [False, True])
+@pytest.mark.parametrize("subset", [False, True])
+def test_oracle_composed_map_extrusion(oracle_op2, variable, subset):
+    S.sc_composed_map_extrusion(oracle_op2, variable, subset)
