@@ -240,6 +240,135 @@ class Dat(AbstractDat):
             filename = filename + ".npy"
         self.data[:] = np.load(filename)
 
+    # ---- pointwise linear algebra (pyop2/types/dat.py:343-574), executed
+    # as generated direct par_loops over the owned entities, as the
+    # reference does
+    _kernel_cache = {}
+
+    def _kernel(self, key, body, name):
+        from pyop2_gb300.local_kernel import Kernel
+        k = Dat._kernel_cache.get(key)
+        if k is None:
+            k = Dat._kernel_cache[key] = Kernel(body, name)
+        return k
+
+    def _other(self, other):
+        from pyop2_gb300.types.glob import Global
+        if isinstance(other, Dat):
+            self._check_shape(other)
+            return other, False
+        return Global(1, data=other, dtype=self.dtype), True
+
+    def _check_shape(self, other):
+        if other.dataset.dim != self.dataset.dim:
+            raise ValueError("Mismatched shapes in operands %s and %s"
+                             % (self.dataset.dim, other.dataset.dim))
+
+    def _op(self, other, op, opname):
+        from pyop2_gb300.datatypes import as_cstr
+        from pyop2_gb300.parloop import par_loop
+        from pyop2_gb300.types.access import READ, WRITE
+        o, scalar = self._other(other)
+        t, to = as_cstr(self.dtype), as_cstr(o.dtype)
+        name = "op2g_dat_%s" % opname
+        key = ("op", opname, scalar, self.cdim, t, to)
+        k = self._kernel(key, "static void %s(const %s *a, const %s *b, %s *r) "
+                         "{ for (int i = 0; i < %d; ++i) r[i] = a[i] %s b[%s]; }"
+                         % (name, t, to, t, self.cdim, op, "0" if scalar else "i"), name)
+        ret = Dat(self.dataset, None, self.dtype)
+        par_loop(k, self.dataset.set, self(READ), o(READ), ret(WRITE))
+        return ret
+
+    def _iop(self, other, op, opname):
+        from pyop2_gb300.datatypes import as_cstr
+        from pyop2_gb300.parloop import par_loop
+        from pyop2_gb300.types.access import READ, RW
+        o, scalar = self._other(other)
+        t, to = as_cstr(self.dtype), as_cstr(o.dtype)
+        name = "op2g_dat_i%s" % opname
+        key = ("iop", opname, scalar, self.cdim, t, to)
+        k = self._kernel(key, "static void %s(%s *a, const %s *b) "
+                         "{ for (int i = 0; i < %d; ++i) a[i] %s= b[%s]; }"
+                         % (name, t, to, self.cdim, op, "0" if scalar else "i"), name)
+        if o is self:
+            o = Dat(self)
+        par_loop(k, self.dataset.set, self(RW), o(READ))
+        return self
+
+    def __add__(self, other):
+        return self._op(other, "+", "add")
+
+    def __radd__(self, other):
+        return self + other
+
+    def __sub__(self, other):
+        return self._op(other, "-", "sub")
+
+    def __rsub__(self, other):
+        ret = -self
+        ret += other
+        return ret
+
+    def __mul__(self, other):
+        return self._op(other, "*", "mul")
+
+    def __rmul__(self, other):
+        return self * other
+
+    def __truediv__(self, other):
+        return self._op(other, "/", "div")
+
+    def __iadd__(self, other):
+        return self._iop(other, "+", "add")
+
+    def __isub__(self, other):
+        return self._iop(other, "-", "sub")
+
+    def __imul__(self, other):
+        return self._iop(other, "*", "mul")
+
+    def __itruediv__(self, other):
+        return self._iop(other, "/", "div")
+
+    def __pos__(self):
+        return Dat(self)
+
+    def __neg__(self):
+        from pyop2_gb300.datatypes import as_cstr
+        from pyop2_gb300.parloop import par_loop
+        from pyop2_gb300.types.access import READ, WRITE
+        t = as_cstr(self.dtype)
+        k = self._kernel(("neg", self.cdim, t),
+                         "static void op2g_dat_neg(const %s *a, %s *r) "
+                         "{ for (int i = 0; i < %d; ++i) r[i] = -a[i]; }" % (t, t, self.cdim),
+                         "op2g_dat_neg")
+        ret = Dat(self.dataset, None, self.dtype)
+        par_loop(k, self.dataset.set, self(READ), ret(WRITE))
+        return ret
+
+    def inner(self, other):
+        """Euclidean inner product over the owned entities (a Global INC
+        reduction on the device)."""
+        from pyop2_gb300.datatypes import as_cstr
+        from pyop2_gb300.parloop import par_loop
+        from pyop2_gb300.types.access import INC, READ
+        from pyop2_gb300.types.glob import Global
+        self._check_shape(other)
+        t = as_cstr(self.dtype)
+        k = self._kernel(("inner", self.cdim, t),
+                         "static void op2g_dat_inner(const %s *a, const %s *b, %s *r) "
+                         "{ for (int i = 0; i < %d; ++i) r[0] += a[i] * b[i]; }"
+                         % (t, t, t, self.cdim), "op2g_dat_inner")
+        ret = Global(1, data=0, dtype=self.dtype)
+        par_loop(k, self.dataset.set, self(READ), other(READ), ret(INC))
+        return ret.data_ro[0]
+
+    @property
+    def norm(self):
+        """The l2 norm of the owned values."""
+        from math import sqrt
+        return sqrt(self.inner(self))
+
     def __iter__(self):
         yield self
 

@@ -73,15 +73,29 @@ class _Validator:
 
     def __call__(self, f):
         sig = inspect.signature(f)
+        params = list(sig.parameters.values())
+        # (name, position, default, check args) resolved once, not per call
+        plan = []
+        for name, *rest in self.checks:
+            if name not in sig.parameters:
+                continue
+            pos = next(i for i, p in enumerate(params) if p.name == name)
+            default = sig.parameters[name].default
+            plan.append((name, pos, default, rest))
 
         @functools.wraps(f)
         def wrapper(*args, **kwargs):
             if configuration["type_check"]:
-                bound = sig.bind(*args, **kwargs)
-                bound.apply_defaults()
-                for name, *rest in self.checks:
-                    if name in bound.arguments:
-                        self.check(name, bound.arguments[name], *rest)
+                for name, pos, default, rest in plan:
+                    if pos < len(args):
+                        value = args[pos]
+                    elif name in kwargs:
+                        value = kwargs[name]
+                    elif default is not inspect.Parameter.empty:
+                        value = default
+                    else:
+                        continue
+                    self.check(name, value, *rest)
             return f(*args, **kwargs)
         return wrapper
 
