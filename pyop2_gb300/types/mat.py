@@ -468,6 +468,53 @@ class Mat(DataCarrier):
                       float(diag_val), self._err.data_ptr(), device.stream_handle())
         self.increment_dat_version()
 
+    def _insert(self, rows, cols, values, add):
+        """MatSetValuesBlockedLocal semantics from the host: rows/cols are
+        block indices, values a (len(rows) * rdim) x (len(cols) * cdim) array."""
+        rows = np.atleast_1d(np.asarray(rows, dtype=np.int64))
+        cols = np.atleast_1d(np.asarray(cols, dtype=np.int64))
+        rdim, cdim = self.dims[0][0]
+        vals = np.asarray(values, dtype=np.float64).reshape(len(rows) * rdim, len(cols) * cdim)
+        rp, ci = self._sparsity.csr()
+        pos = []
+        src = []
+        for a, r in enumerate(rows):
+            if r < 0:
+                continue
+            seg = ci[rp[r]:rp[r + 1]]
+            for b, c in enumerate(cols):
+                if c < 0:
+                    continue
+                k = np.searchsorted(seg, c)
+                if k >= len(seg) or seg[k] != c:
+                    raise RuntimeError("Mat %s: insertion outside the sparsity pattern "
+                                       "(new nonzero location)" % self._name)
+                base = (rp[r] + k) * rdim * cdim
+                for i in range(rdim):
+                    for j in range(cdim):
+                        pos.append(base + i * cdim + j)
+                        src.append(vals[a * rdim + i, b * cdim + j])
+        if not pos:
+            return
+        idx = torch.as_tensor(np.asarray(pos, dtype=np.int64), device=self._values.device)
+        v = torch.as_tensor(np.asarray(src), device=self._values.device)
+        if add:
+            self._values.index_add_(0, idx, v)
+        else:
+            self._values.index_copy_(0, idx, v)
+
+    def addto_values(self, rows, cols, values):
+        """Add a block of values (pyop2/types/mat.py:837-842)."""
+        self.change_assembly_state(Mat.ADD_VALUES)
+        if len(np.atleast_1d(values)) > 0:
+            self._insert(rows, cols, values, True)
+
+    def set_values(self, rows, cols, values):
+        """Set a block of values (pyop2/types/mat.py:844-849)."""
+        self.change_assembly_state(Mat.INSERT_VALUES)
+        if len(np.atleast_1d(values)) > 0:
+            self._insert(rows, cols, values, False)
+
     # ---- exports
     def csr(self):
         """(rowptr, block colidx, values[nblocks, rdim, cdim]) on the host."""

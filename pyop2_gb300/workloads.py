@@ -553,6 +553,11 @@ static void prism_elasticity_mat(double A[18][18], const double *restrict X,
                                  const double *restrict lame)
 {""" + _PRISM_GEOM + r"""
   const double lam = lame[0], mu = lame[1];
+  double B[6][6][3][3];
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j)
+      for (int c = 0; c < 3; ++c)
+        for (int d = 0; d < 3; ++d) B[i][j][c][d] = 0.0;
   for (int zq = 0; zq < 2; ++zq) {
     const double z1 = ZQ[zq], z0 = 1.0 - z1;
     for (int tq = 0; tq < 3; ++tq) {
@@ -561,16 +566,30 @@ static void prism_elasticity_mat(double A[18][18], const double *restrict X,
         G[a][0] = g[a][0] * z0; G[a][1] = g[a][1] * z0; G[a][2] = -TL[tq][a] * ih;
         G[a + 3][0] = g[a][0] * z1; G[a + 3][1] = g[a][1] * z1; G[a + 3][2] = TL[tq][a] * ih;
       }
+      double lG[6][3], mG[6][3];
       for (int i = 0; i < 6; ++i)
-        for (int j = 0; j < 6; ++j) {
-          const double dot = G[i][0] * G[j][0] + G[i][1] * G[j][1] + G[i][2] * G[j][2];
+        for (int c = 0; c < 3; ++c) {
+          lG[i][c] = wq * lam * G[i][c];
+          mG[i][c] = wq * mu * G[i][c];
+        }
+      /* K is symmetric: the (i, j) block is the transpose of the (j, i)
+         block, so only node pairs i <= j are computed */
+      for (int i = 0; i < 6; ++i)
+        for (int j = i; j < 6; ++j) {
+          const double dot = mG[i][0] * G[j][0] + mG[i][1] * G[j][1] + mG[i][2] * G[j][2];
           for (int c = 0; c < 3; ++c)
             for (int d = 0; d < 3; ++d)
-              A[3 * i + c][3 * j + d] += wq * (lam * G[i][c] * G[j][d] +
-                                               mu * ((c == d ? dot : 0.0) + G[i][d] * G[j][c]));
+              B[i][j][c][d] += lG[i][c] * G[j][d] + mG[i][d] * G[j][c] + (c == d ? dot : 0.0);
         }
     }
   }
+  for (int i = 0; i < 6; ++i)
+    for (int j = i; j < 6; ++j)
+      for (int c = 0; c < 3; ++c)
+        for (int d = 0; d < 3; ++d) {
+          A[3 * i + c][3 * j + d] += B[i][j][c][d];
+          if (j != i) A[3 * j + d][3 * i + c] += B[i][j][c][d];
+        }
 }
 """)
 

@@ -108,3 +108,23 @@ def test_gpu_new_nonzero_is_reported(gpu_op2):
     op2.par_loop(k, s, MatLegacyArg(mat, (m3, m3), op2.INC))
     with pytest.raises(RuntimeError):
         mat.assemble()
+
+
+def test_gpu_addto_and_set_values_state_machine(gpu_op2):
+    """test/unit/test_matrices.py:775-862 on a single block: addto/set change
+    the assembly state, mixing them works, values land where expected."""
+    op2 = gpu_op2
+    s = op2.Set(3)
+    m = op2.Map(s, s, 1, [0, 1, 2])
+    mat = op2.Mat(op2.Sparsity((s ** 1, s ** 1), [(m, m, None)]))
+    assert mat.assembly_state is op2.Mat.ASSEMBLED
+    mat.addto_values(0, 0, [1])
+    assert mat.assembly_state is op2.Mat.ADD_VALUES
+    mat.set_values(1, 1, [4])
+    assert mat.assembly_state is op2.Mat.INSERT_VALUES
+    mat.addto_values(0, 0, [3])
+    mat.assemble()
+    assert mat.assembly_state is op2.Mat.ASSEMBLED
+    assert np.allclose(mat.values, np.diag([4, 4, 0]))
+    with pytest.raises(RuntimeError):
+        mat.set_values(0, 2, [1])      # outside the (diagonal) pattern
