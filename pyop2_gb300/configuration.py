@@ -35,6 +35,8 @@ class Configuration(dict):
         "autotune": ("OP2G_AUTOTUNE", bool, False),
         # CUDA device used by this process
         "device": ("OP2G_DEVICE", int, 0),
+        # NVTX ranges + CUDA-event timing of named regions (profiling.summary())
+        "profiling": ("OP2G_PROFILING", bool, False),
     }
 
     def __init__(self):

@@ -438,6 +438,15 @@ class Parloop:
                     a.data.halo_valid = False
 
     def compute(self):
+        if configuration["profiling"]:
+            from pyop2_gb300.profiling import timed_region
+            # same region name as the reference's per-loop event
+            # (pyop2/parloop.py:221-232)
+            with timed_region("Parloop_%s_%s" % (self.iterset.name, self.local_kernel.name)):
+                return self._compute()
+        return self._compute()
+
+    def _compute(self):
         D = self.launch_desc()
         scatter, bs, k, table, argdescs = self._built
         st = device.stream_handle()

@@ -70,7 +70,9 @@ class Sparsity:
         self._dims = (((rset.cdim, cset.cdim),),)
         self._nested = False
         self.comm = rset.comm
-        self._build()
+        from pyop2_gb300.profiling import timed_region
+        with timed_region("CreateSparsity"):      # pyop2/types/mat.py:105-113
+            self._build()
         self._initialized = True
 
     @classmethod

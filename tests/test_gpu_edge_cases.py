@@ -127,3 +127,27 @@ def test_debug_bounds_check_reports_bad_map(gpu_op2):
     finally:
         configuration["debug"] = False
     assert d2.data_ro.sum() == 3.0       # the out-of-range contribution was skipped
+
+
+def test_profiling_regions(gpu_op2):
+    """Named timed regions: the per-loop region carries the reference's
+    Parloop_<set>_<kernel> name and accumulates device time."""
+    from pyop2_gb300 import profiling
+    from pyop2_gb300.configuration import configuration
+    op2 = gpu_op2
+    s = op2.Set(1000, "cells")
+    d = op2.Dat(s, np.zeros(1000))
+    configuration["profiling"] = True
+    try:
+        profiling.reset()
+        for _ in range(3):
+            op2.par_loop(op2.Kernel("static void k(double *x) { x[0] += 1; }", "k"), s,
+                         d(op2.INC))
+        m = op2.Map(s, s, 1, np.arange(1000))
+        op2.Sparsity((s ** 1, s ** 1), [(m, m, None)])
+        summ = profiling.summary()
+    finally:
+        configuration["profiling"] = False
+    assert summ["Parloop_cells_k"][0] == 3 and summ["Parloop_cells_k"][1] > 0
+    assert summ["CreateSparsity"][0] == 1
+    assert np.all(d.data_ro == 3)
