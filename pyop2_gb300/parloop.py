@@ -493,6 +493,24 @@ class ColourPlan:
     def order_for_subset(self, subset_indices):
         raise NotImplementedError
 
+    def validate(self, maps):
+        """True if no two entities of one colour share a target through any
+        of ``maps`` (the plan's correctness property; checked on the device)."""
+        import torch
+        for c in range(self.ncolours):
+            seg = self.order[self.ptr[c]:self.ptr[c + 1]].long()
+            if seg.numel() == 0:
+                continue
+            if not bool((self.colour[seg] == c).all()):
+                return False
+            for m in maps:
+                vals = m._device_values()[:m.values_with_halo.nbytes].view(torch.int32)
+                t = vals.view(-1, m.arity)[seg].reshape(-1)
+                t = t[t >= 0]
+                if torch.unique(t).numel() != t.numel():
+                    return False
+        return True
+
 
 def colour_plan(loop, max_colours=256):
     """Colouring of ``loop.iterset`` (cached on the set per map tuple)."""

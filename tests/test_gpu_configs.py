@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 from pyop2_gb300 import workloads
+from pyop2_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
 
@@ -63,3 +64,21 @@ def test_config2a_full_size_properties(gpu_op2, permute):
     p["y"].zero()
     p["run"]()
     assert np.abs(p["y"].data_ro).max() <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("permute", [False, True])
+def test_full_size_colouring_is_valid(gpu_op2, permute):
+    """Jones-Plassmann colouring of the 12.58 M tets: no two cells of one colour
+    share a vertex; every cell appears exactly once."""
+    import torch
+    from pyop2_gb300.parloop import colour_plan
+    op2 = gpu_op2
+    p = W.build_p1_3d(op2, n=128, permute=permute, seed=0)
+    lp = op2.ParLoop(p["kernel"], p["cells"], p["y"](op2.INC, p["c2v"]),
+                     p["X"](op2.READ, p["c2v"]), p["x"](op2.READ, p["c2v"]))
+    plan = colour_plan(lp)
+    assert plan is not None and 8 <= plan.ncolours <= 256
+    assert plan.ptr[-1] == p["cells"].size
+    order = plan.order[:p["cells"].size].long()
+    assert torch.unique(order).numel() == p["cells"].size
+    assert plan.validate([p["c2v"]])
