@@ -186,11 +186,18 @@ class _Compiled:
         return buf.value.decode()
 
 
+def signature_key(code, name, loop, args, maps, arch=None):
+    """What identifies a compiled wrapper: kernel code and name, loop flags,
+    argument kinds/access/dtype/dims, map shapes with map identity reduced to
+    first-seen order (as pyop2/global_kernel.py:304-312 keys GlobalKernel)."""
+    return (code, name, tuple(sorted(loop.items())), tuple(args), tuple(maps), arch)
+
+
 def compile_signature(code, name, loop, args, maps, arch=None):
     """Compile (or fetch) the wrapper for a signature given as plain tuples:
     loop = dict of LoopDesc fields, args = list of ArgDesc field tuples,
     maps = list of _MapTable entries."""
-    key = (code, name, tuple(sorted(loop.items())), tuple(args), tuple(maps), arch)
+    key = signature_key(code, name, loop, args, maps, arch)
     c = _KERNELS.get(key)
     if c is not None:
         return c
@@ -325,6 +332,12 @@ class Parloop:
                 if any(isinstance(m, ComposedMap) for m in a.maps):
                     return False
         return True
+
+    def cache_key(self, scatter=_lib.SCATTER_ATOMIC, block_size=256):
+        """Key of the compiled wrapper this loop uses (needs no device)."""
+        table, argdescs = self._signature()
+        return signature_key(self.local_kernel.source, self.local_kernel.name,
+                             self._loop_desc(scatter, block_size), argdescs, table.key())
 
     def build(self, scatter=None, block_size=None):
         """Compile the wrapper for this loop (idempotent per strategy)."""
