@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define OP2G_ABI_VERSION 1
+#define OP2G_ABI_VERSION 2
 
 /* ---------------------------------------------------------------- status */
 typedef int32_t op2g_status;
@@ -122,6 +122,12 @@ typedef struct op2g_arg_desc {
     int32_t cmap;     /* MAT: column map index                                       */
     int32_t rdim;     /* MAT: rows per block                                          */
     int32_t cdim;     /* MAT: columns per block                                       */
+    int32_t group;    /* 0, or an id > 0 shared by CONSECUTIVE arguments that form one
+                         kernel parameter: the components of a MixedDat (their packs
+                         concatenated in order, pyop2/codegen/builder.py:413-498) or the
+                         blocks of a mixed Mat in row-major block order (one element
+                         matrix over all blocks, pyop2/codegen/builder.py:609-680)      */
+    int32_t group_cols; /* MAT groups: number of block columns                         */
 } op2g_arg_desc;
 
 typedef struct op2g_loop_desc {

@@ -109,6 +109,54 @@ class DataSet:
         self.cdim = int(np.prod(self.dim))
 
 
+class MixedSet:
+    """Tuple of Sets (pyop2/types/set.py:540-662)."""
+
+    def __init__(self, sets):
+        self.split = tuple(sets)
+
+    def __iter__(self):
+        return iter(self.split)
+
+    def __len__(self):
+        return len(self.split)
+
+    def __getitem__(self, i):
+        return self.split[i]
+
+    def __pow__(self, dim):
+        return MixedDataSet([s ** dim for s in self.split])
+
+
+class MixedDataSet:
+    """Tuple of DataSets (pyop2/types/dataset.py:304-460)."""
+
+    def __init__(self, dsets, dims=None):
+        if dims is not None:
+            sets = dsets.split if isinstance(dsets, MixedSet) else tuple(dsets)
+            dims = (dims,) * len(sets) if isinstance(dims, int) else tuple(dims)
+            dsets = [DataSet(s, d) for s, d in zip(sets, dims)]
+        self.split = tuple(d if isinstance(d, DataSet) else DataSet(d, 1) for d in dsets)
+
+    def __iter__(self):
+        return iter(self.split)
+
+    def __len__(self):
+        return len(self.split)
+
+    def __getitem__(self, i):
+        return self.split[i]
+
+
+def _same_space(a, b):
+    """Row and column spaces coincide (the reference compares DataSets)."""
+    if a is b:
+        return True
+    sa = a.split if isinstance(a, MixedDataSet) else (a,)
+    sb = b.split if isinstance(b, MixedDataSet) else (b,)
+    return len(sa) == len(sb) and all(x.set is y.set and x.dim == y.dim for x, y in zip(sa, sb))
+
+
 # ------------------------------------------------------------------- maps
 class Map:
     def __init__(self, iterset, toset, arity, values, name=None, offset=None,
@@ -145,6 +193,23 @@ class ComposedMap:
         self.offset_quotient = flat[0].offset_quotient
 
 
+class MixedMap:
+    """Tuple of Maps from one iteration set (pyop2/types/map.py:297-434)."""
+
+    def __init__(self, maps):
+        self.split = tuple(maps)
+        self.iterset = self.split[0].iterset
+
+    def __iter__(self):
+        return iter(self.split)
+
+    def __len__(self):
+        return len(self.split)
+
+    def __getitem__(self, i):
+        return self.split[i]
+
+
 # ------------------------------------------------------------------- data
 class Dat:
     def __init__(self, dataset, data=None, dtype=None, name=None):
@@ -167,6 +232,35 @@ class Dat:
 
     def zero(self):
         self.data[...] = 0
+
+
+class MixedDat:
+    """Tuple of Dats (pyop2/types/dat.py:787-1151); accessed through a
+    MixedMap as one kernel argument."""
+
+    def __init__(self, items):
+        items = items.split if isinstance(items, (MixedSet, MixedDataSet)) else items
+        self.split = tuple(d if isinstance(d, Dat) else Dat(d) for d in items)
+
+    def __iter__(self):
+        return iter(self.split)
+
+    def __len__(self):
+        return len(self.split)
+
+    def __getitem__(self, i):
+        return self.split[i]
+
+    def __call__(self, access, map_):
+        return ("mdat", self.split, access, tuple(map_))
+
+    @property
+    def data(self):
+        return tuple(d.data for d in self.split)
+
+    @property
+    def data_ro(self):
+        return self.data
 
 
 class Global:
@@ -226,9 +320,23 @@ def _outer_values(m):
 
 
 class Sparsity:
-    """Block pattern from (rmap, cmap, regions) triples (oracle/sparsity.c)."""
+    """Block pattern from (rmap, cmap, regions) triples (oracle/sparsity.c).
 
-    def __init__(self, dsets, maps_and_regions, block_sparse=True, diagonal_block=True):
+    Between MixedDataSets the sparsity is a grid of block sparsities, block
+    (i, j) built from ``maps_and_regions[(i, j)]`` with the diagonal on
+    i == j when the row and column spaces coincide (pyop2/types/mat.py:86-95,
+    pyop2/sparsity.pyx:144-159).  ``nnz`` is the tuple of the blocks' counts
+    when nested, else the dof-row counts of the whole (blocks of a block row
+    side by side)."""
+
+    def __init__(self, dsets, maps_and_regions, block_sparse=True, diagonal_block=True,
+                 nest=True):
+        if isinstance(dsets[0], MixedDataSet) or isinstance(dsets[1], MixedDataSet):
+            self._init_mixed(dsets, maps_and_regions, block_sparse, diagonal_block, nest)
+            return
+        if isinstance(maps_and_regions, dict):
+            maps_and_regions = maps_and_regions.get((0, 0), [])
+        self.shape = (1, 1)
         rds, cds = dsets
         self.dsets = dsets
         self.dims = (rds.cdim, cds.cdim)
@@ -296,28 +404,69 @@ class Sparsity:
             counts = np.repeat(counts * cdim, rdim).astype(np.int32)
         self.nnz = counts
 
+    def _init_mixed(self, dsets, maps_and_regions, block_sparse, diagonal_block, nest):
+        rsets = dsets[0].split if isinstance(dsets[0], MixedDataSet) else (dsets[0],)
+        csets = dsets[1].split if isinstance(dsets[1], MixedDataSet) else (dsets[1],)
+        self.dsets = dsets
+        self.shape = (len(rsets), len(csets))
+        same = _same_space(dsets[0], dsets[1])
+        self.blocks = [[Sparsity((r, c), maps_and_regions.get((i, j), []),
+                                 block_sparse=block_sparse,
+                                 diagonal_block=(i == j and same and (nest or diagonal_block)))
+                        for j, c in enumerate(csets)] for i, r in enumerate(rsets)]
+        if nest:
+            self.nnz = tuple(b.nnz for row in self.blocks for b in row)
+        else:
+            rows = []
+            for i, row in enumerate(self.blocks):
+                acc = np.zeros(rsets[i].set.size, dtype=np.int64)
+                for j, b in enumerate(row):
+                    acc += np.diff(b.rowptr) * csets[j].cdim
+                rows.append(np.repeat(acc, rsets[i].cdim))
+            self.nnz = np.concatenate(rows).astype(np.int32)
+
+    def __getitem__(self, ij):
+        i, j = ij
+        return self.blocks[i][j]
+
 
 class Mat:
     """Block-CSR values on an oracle Sparsity (row-major blocks)."""
 
     def __init__(self, sparsity):
         self.sparsity = sparsity
+        if sparsity.shape != (1, 1):
+            self.blocks = [[Mat(b) for b in row] for row in sparsity.blocks]
+            return
+        self.blocks = [[self]]
         rdim, cdim = sparsity.dims
         self.values_bcsr = np.zeros((len(sparsity.colidx), rdim, cdim))
         self.err = np.zeros(1, dtype=np.int32)
 
     def __call__(self, access, maps):
+        if self.sparsity.shape != (1, 1):
+            return ("mmat", self.blocks, access, (tuple(maps[0]), tuple(maps[1])))
         return ("mat", self, access, tuple(maps))
 
+    def __getitem__(self, ij):
+        i, j = ij
+        return self.blocks[i][j]
+
     def zero(self):
-        self.values_bcsr[...] = 0
+        for row in self.blocks:
+            for b in row:
+                b.values_bcsr[...] = 0
 
     def assemble(self):
-        if self.err[0]:
-            raise RuntimeError("oracle Mat: insertion outside the sparsity pattern")
+        for row in self.blocks:
+            for b in row:
+                if b.err[0]:
+                    raise RuntimeError("oracle Mat: insertion outside the sparsity pattern")
 
     def to_scipy(self):
         import scipy.sparse as sps
+        if self.sparsity.shape != (1, 1):
+            return sps.bmat([[b.to_scipy() for b in row] for row in self.blocks], format="csr")
         rdim, cdim = self.sparsity.dims
         sp = self.sparsity
         shape = ((len(sp.rowptr) - 1) * rdim, sp.dsets[1].set.size * cdim)
@@ -451,6 +600,46 @@ def _generate(kernel, sig):
                 o.append(ind + "  if (b >= 0) b += op2o_off%d[%s] * %s;" % (src, oidx, e))
             o.append(ind + "  x%d_%d[i] = b;" % (mi, f))
             o.append(ind + "}")
+    # Mixed arguments (pyop2/codegen/builder.py:413-498, 609-680): the
+    # components of one group share one kernel parameter.  Dat components'
+    # packs are concatenated; a mixed Mat's blocks are sub-blocks of one
+    # element matrix, copied out block by block before insertion.
+    first, off, gsize, mrc = {}, {}, {}, {}
+    ai = 0
+    while ai < len(args):
+        g = args[ai][6]
+        bj = ai + 1
+        while g and bj < len(args) and args[bj][6] == g:
+            bj += 1
+        a0 = args[ai]
+        if a0[0] == "dat":
+            o_ = 0
+            for k in range(ai, bj):
+                first[k], off[k] = ai, o_
+                if args[k][5] is not None:
+                    o_ += nf * maps[args[k][5]][1] * args[k][4]
+            gsize[ai] = o_
+        elif a0[0] == "mat":
+            ncols = a0[7] if g else 1
+            nrows = (bj - ai) // ncols
+
+            def rows_of(k):
+                return nf * maps[args[k][5][0]][1] * args[k][3][0]
+
+            def cols_of(k):
+                return nf * maps[args[k][5][1]][1] * args[k][3][1]
+            roffs = [sum(rows_of(ai + q * ncols) for q in range(i)) for i in range(nrows)]
+            coffs = [sum(cols_of(ai + q) for q in range(j)) for j in range(ncols)]
+            R = sum(rows_of(ai + q * ncols) for q in range(nrows))
+            C = sum(cols_of(ai + q) for q in range(ncols))
+            for k in range(ai, bj):
+                i, j = divmod(k - ai, ncols)
+                first[k] = ai
+                mrc[k] = (roffs[i], coffs[j], rows_of(k), cols_of(k), C, g != 0)
+            gsize[ai] = R * C
+        else:
+            first[ai] = ai
+        ai = bj
     # packs
     kargs = []
     for ai, a in enumerate(args):
@@ -469,28 +658,31 @@ def _generate(kernel, sig):
                              % (dim, ai, ct, ai))
                 kargs.append("g%d" % ai)
         elif kind == "dat":
-            _, _, acc, dt, dim, mi = a
+            _, _, acc, dt, dim, mi = a[:6]
             ct = _CTYPE[dt]
             if mi is None:
                 kargs.append("((%s *)a%d) + (int64_t)n * %d" % (ct, ai, dim))
                 continue
             ar = maps[mi][1]
-            tot = nf * ar * dim
-            o.append(ind + "%s t%d[%d];" % (ct, ai, tot))
+            tp, po = first[ai], off[ai]
+            if tp == ai:
+                o.append(ind + "%s t%d[%d];" % (ct, ai, gsize[ai]))
             if acc in (INC, WRITE):
-                o.append(ind + "for (int k = 0; k < %d; ++k) t%d[k] = 0;" % (tot, ai))
+                if tp == ai:
+                    o.append(ind + "for (int k = 0; k < %d; ++k) t%d[k] = 0;" % (gsize[ai], ai))
             else:
                 for f in range(nf):
                     o.append(ind + "for (int i = 0; i < %d; ++i) for (int j = 0; j < %d; ++j) "
-                             "t%d[(%d + i) * %d + j] = x%d_%d[i] >= 0 ? ((%s *)a%d)[(int64_t)x%d_%d[i] * %d + j] : 0;"
-                             % (ar, dim, ai, f * ar, dim, mi, f, ct, ai, mi, f, dim))
-            kargs.append("t%d" % ai)
+                             "t%d[%d + (%d + i) * %d + j] = x%d_%d[i] >= 0 ? ((%s *)a%d)[(int64_t)x%d_%d[i] * %d + j] : 0;"
+                             % (ar, dim, tp, po, f * ar, dim, mi, f, ct, ai, mi, f, dim))
+            if tp == ai:
+                kargs.append("t%d" % ai)
         elif kind == "mat":
-            _, _, acc, (rd, cd), _, (rm, cm) = a
-            tot = nf * maps[rm][1] * rd * nf * maps[cm][1] * cd
-            o.append(ind + "double t%d[%d]; for (int k = 0; k < %d; ++k) t%d[k] = 0;"
-                     % (ai, tot, tot, ai))
-            kargs.append("t%d" % ai)
+            if first[ai] == ai:
+                tot = gsize[ai]
+                o.append(ind + "double t%d[%d]; for (int k = 0; k < %d; ++k) t%d[k] = 0;"
+                         % (ai, tot, tot, ai))
+                kargs.append("t%d" % ai)
     if pass_layer:
         kargs.append("layer")
     o.append(ind + "%s(%s);" % (kernel.name, ", ".join(kargs)))
@@ -507,14 +699,14 @@ def _generate(kernel, sig):
                 o.append(ind + "for (int j = 0; j < %d; ++j) { %s *G = (%s *)a%d; "
                          "if (g%d[j] %s G[j]) G[j] = g%d[j]; }" % (dim, ct, ct, ai, ai, cmp, ai))
         elif kind == "dat":
-            _, _, acc, dt, dim, mi = a
+            _, _, acc, dt, dim, mi = a[:6]
             if mi is None or acc == READ:
                 continue
             ct = _CTYPE[dt]
             ar = maps[mi][1]
             for f in range(nf):
                 dst = "((%s *)a%d)[(int64_t)x%d_%d[i] * %d + j]" % (ct, ai, mi, f, dim)
-                src = "t%d[(%d + i) * %d + j]" % (ai, f * ar, dim)
+                src = "t%d[%d + (%d + i) * %d + j]" % (first[ai], off[ai], f * ar, dim)
                 if acc == INC:
                     stmt = "%s += %s;" % (dst, src)
                 elif acc == MIN:
@@ -526,18 +718,27 @@ def _generate(kernel, sig):
                 o.append(ind + "for (int i = 0; i < %d; ++i) { if (x%d_%d[i] < 0) continue; "
                          "for (int j = 0; j < %d; ++j) { %s } }" % (ar, mi, f, dim, stmt))
         elif kind == "mat":
-            _, _, acc, (rd, cd), _, (rm, cm) = a
+            _, _, acc, (rd, cd), _, (rm, cm) = a[:6]
             ra, ca = maps[rm][1], maps[cm][1]
             rows = "rr%d" % ai
             cols = "cc%d" % ai
+            r0, c0, nr_, nc_, C, grouped = mrc[ai]
+            vals = "t%d" % ai
+            if grouped:
+                # mixed element matrix -> this block's local matrix
+                vals = "tb%d" % ai
+                o.append(ind + "double %s[%d];" % (vals, nr_ * nc_))
+                o.append(ind + "for (int i = 0; i < %d; ++i) for (int j = 0; j < %d; ++j) "
+                         "%s[i * %d + j] = t%d[(%d + i) * %d + %d + j];"
+                         % (nr_, nc_, vals, nc_, first[ai], r0, C, c0))
             o.append(ind + "int %s[%d], %s[%d];" % (rows, nf * ra, cols, nf * ca))
             for f in range(nf):
                 o.append(ind + "for (int i = 0; i < %d; ++i) %s[%d + i] = x%d_%d[i];"
                          % (ra, rows, f * ra, rm, f))
                 o.append(ind + "for (int i = 0; i < %d; ++i) %s[%d + i] = x%d_%d[i];"
                          % (ca, cols, f * ca, cm, f))
-            o.append(ind + "op2o_matset(mv%d, mrp%d, mci%d, %d, %d, %d, %s, %d, %s, t%d, %d, merr%d);"
-                     % (ai, ai, ai, rd, cd, nf * ra, rows, nf * ca, cols, ai,
+            o.append(ind + "op2o_matset(mv%d, mrp%d, mci%d, %d, %d, %d, %s, %d, %s, %s, %d, merr%d);"
+                     % (ai, ai, ai, rd, cd, nf * ra, rows, nf * ca, cols, vals,
                         1 if acc == INC else 0, ai))
     if extr:
         o.append("    }")
@@ -616,16 +817,31 @@ class ParLoop:
                  profile="parity"):
         table = _Table()
         sig_args = []
+        group = 0
         for a in args:
             kind, obj, acc, m = a
             if kind == "glob":
-                sig_args.append(("glob", obj, acc, obj.data.dtype.name, obj.dim))
+                sig_args.append(("glob", obj, acc, obj.data.dtype.name, obj.dim, None, 0, 0))
             elif kind == "dat":
                 mi = table.add(m) if m is not None else None
-                sig_args.append(("dat", obj, acc, obj.data.dtype.name, obj.cdim, mi))
+                sig_args.append(("dat", obj, acc, obj.data.dtype.name, obj.cdim, mi, 0, 0))
+            elif kind == "mdat":
+                # ("mdat", [Dat, ...], access, [Map, ...]): one mixed argument
+                group += 1
+                for d, mm in zip(obj, m):
+                    sig_args.append(("dat", d, acc, d.data.dtype.name, d.cdim, table.add(mm),
+                                     group, 0))
+            elif kind == "mmat":
+                # ("mmat", [[Mat, ...], ...], access, ([rmap, ...], [cmap, ...]))
+                group += 1
+                rms, cms = m
+                for i, row in enumerate(obj):
+                    for j, mat in enumerate(row):
+                        sig_args.append(("mat", mat, acc, mat.sparsity.dims, None,
+                                         (table.add(rms[i]), table.add(cms[j])), group, len(cms)))
             else:
                 sig_args.append(("mat", obj, acc, obj.sparsity.dims, None,
-                                 (table.add(m[0]), table.add(m[1]))))
+                                 (table.add(m[0]), table.add(m[1])), 0, 0))
         self.iterset = iterset
         extr = bool(iterset._extruded)
         const = bool(extr and iterset.constant_layers)

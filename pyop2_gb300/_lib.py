@@ -18,6 +18,7 @@ ERR_INVALID, ERR_COMPILE, ERR_CUDA, ERR_BOUNDS, ERR_NEW_NONZERO, ERR_CAPACITY, \
 DEVERR_MAP_BOUNDS, DEVERR_NEW_NONZERO, DEVERR_CAPACITY = 1, 2, 4
 
 F64, F32, I32, U32, I64, U64, I16, U16, I8, U8 = range(10)
+ABI_VERSION = 2
 ARG_DAT, ARG_GLOBAL, ARG_MAT, ARG_PASSTHROUGH = range(4)
 MAP_PLAIN, MAP_PERMUTED, MAP_COMPOSED = range(3)
 SCATTER_ATOMIC, SCATTER_WARP, SCATTER_PLAIN = range(3)
@@ -39,7 +40,8 @@ class MapDesc(ctypes.Structure):
 
 class ArgDesc(ctypes.Structure):
     _fields_ = [("kind", _i32), ("access", _i32), ("dtype", _i32), ("dim", _i32),
-                ("map", _i32), ("cmap", _i32), ("rdim", _i32), ("cdim", _i32)]
+                ("map", _i32), ("cmap", _i32), ("rdim", _i32), ("cdim", _i32),
+                ("group", _i32), ("group_cols", _i32)]
 
 
 class LoopDesc(ctypes.Structure):
@@ -125,7 +127,7 @@ def lib():
             f = getattr(L, name)
             f.restype = res
             f.argtypes = args
-        if L.op2g_abi_version() != 1:
+        if L.op2g_abi_version() != ABI_VERSION:
             raise RuntimeError("pyop2_gb300: libop2g ABI version mismatch")
         _lib = L
     return _lib

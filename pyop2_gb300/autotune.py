@@ -27,7 +27,7 @@ def candidates(loop):
 
 def _written(loop):
     out = []
-    for a in loop.args:
+    for a in loop._components:
         if a.access is Access.READ or not hasattr(a.data, "_m") and not hasattr(a.data, "_values"):
             continue
         out.append(a.data)

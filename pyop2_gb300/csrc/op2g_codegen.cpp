@@ -73,8 +73,73 @@ struct Gen {
     std::ostringstream o;
     int nf = 1;  // 2 for ON_INTERIOR_FACETS (packs span two cells of a column)
 
+    // Kernel-parameter layout.  Consecutive arguments with one group id are
+    // one kernel parameter: a MixedDat's component packs concatenated
+    // (pyop2/codegen/builder.py:413-498), or a mixed Mat's blocks as
+    // sub-blocks of one element matrix (pyop2/codegen/builder.py:609-680).
+    std::vector<int> first;   // first argument of the parameter
+    std::vector<int> poff;    // DAT: offset of this component's pack
+    std::vector<int> roff, coff, rstride;  // MAT: sub-block origin, element-matrix width
+    std::vector<int> psize;   // at first: size of the parameter's pack
+    bool has_groups = false;
+
     explicit Gen(const Signature &s) : S(s) {
         nf = (S.loop.extruded && S.loop.iteration_region == OP2G_ON_INTERIOR_FACETS) ? 2 : 1;
+        layout();
+    }
+
+    int dat_pack(size_t a) const {
+        const op2g_arg_desc &d = S.args[a].d;
+        return d.map >= 0 ? nf * S.maps[d.map].arity * d.dim : d.dim;
+    }
+    int mat_rows(size_t a) const {
+        const op2g_arg_desc &d = S.args[a].d;
+        return nf * S.maps[d.map].arity * d.rdim;
+    }
+    int mat_cols(size_t a) const {
+        const op2g_arg_desc &d = S.args[a].d;
+        return nf * S.maps[d.cmap].arity * d.cdim;
+    }
+
+    void layout() {
+        const size_t n = S.args.size();
+        first.assign(n, 0);
+        poff.assign(n, 0);
+        roff.assign(n, 0);
+        coff.assign(n, 0);
+        rstride.assign(n, 0);
+        psize.assign(n, 0);
+        for (size_t a = 0; a < n;) {
+            const op2g_arg_desc &d0 = S.args[a].d;
+            size_t b = a + 1;
+            if (d0.group > 0) {
+                has_groups = true;
+                while (b < n && S.args[b].d.group == d0.group) ++b;
+            }
+            for (size_t k = a; k < b; ++k) first[k] = (int)a;
+            if (d0.kind == OP2G_ARG_DAT) {
+                int off = 0;
+                for (size_t k = a; k < b; ++k) {
+                    poff[k] = off;
+                    off += dat_pack(k);
+                }
+                psize[a] = off;
+            } else if (d0.kind == OP2G_ARG_MAT) {
+                const int C = d0.group > 0 ? d0.group_cols : 1;
+                const int R = (int)(b - a) / C;
+                std::vector<int> co(C), ro(R);
+                int tc = 0, tr = 0;
+                for (int j = 0; j < C; ++j) { co[j] = tc; tc += mat_cols(a + j); }
+                for (int i = 0; i < R; ++i) { ro[i] = tr; tr += mat_rows(a + (size_t)i * C); }
+                for (size_t k = a; k < b; ++k) {
+                    roff[k] = ro[(k - a) / C];
+                    coff[k] = co[(k - a) % C];
+                    rstride[k] = tc;
+                }
+                psize[a] = tr * tc;
+            }
+            a = b;
+        }
     }
 
     // Map used for the outermost indexing of map m (PERMUTED -> its base).
@@ -245,6 +310,7 @@ struct Gen {
                 direct_written = true;
         const bool varlay = extr && (!S.loop.constant_layers || plain || direct_written);
         if (varlay) warp = false;  // lanes of a warp run different layer counts
+        if (has_groups) warp = false;  // grouped packs scatter by atomics
 
         // ----- the run function: a strided sweep of [start, end) plus reductions
         O << "__device__ __forceinline__ void op2g_run(const op2g_params_t &p, long long start, "
@@ -449,13 +515,18 @@ struct Gen {
                     continue;
                 }
                 const int ar = S.maps[A.d.map].arity;
-                const int tot = nf * ar * D;
+                const bool lead = first[a] == (int)a;
+                const int tot = psize[first[a]];
+                const std::string tn = "t" + std::to_string(first[a]);
+                const std::string po = std::to_string(poff[a]) + " + ";
                 const bool decl_outside = warp && A.d.access == OP2G_INC;
-                if (!decl_outside) O << J << T << " t" << an << "[" << tot << "];\n";
+                if (lead && !decl_outside) O << J << T << " " << tn << "[" << tot << "];\n";
                 if (A.d.access == OP2G_INC || A.d.access == OP2G_WRITE) {
-                    O << J << "#pragma unroll\n";
-                    O << J << "for (int k = 0; k < " << tot << "; ++k) t" << an << "[k] = (" << T
-                      << ")0;\n";
+                    if (lead) {
+                        O << J << "#pragma unroll\n";
+                        O << J << "for (int k = 0; k < " << tot << "; ++k) " << tn << "[k] = ("
+                          << T << ")0;\n";
+                    }
                 } else {
                     O << J << "{ const " << T << " *d_ = (const " << T << " *)p.ptr[" << A.slot
                       << "];\n";
@@ -464,17 +535,17 @@ struct Gen {
                         O << J << "  for (int i = 0; i < " << ar << "; ++i) {\n";
                         O << J << "    const int x_ = " << idx_arr(A.d.map, f) << "[i];\n";
                         O << J << "#pragma unroll\n";
-                        O << J << "    for (int j = 0; j < " << D << "; ++j) t" << an << "[("
-                          << f * ar << " + i) * " << D << " + j] = x_ >= 0 ? d_[(long long)x_ * "
+                        O << J << "    for (int j = 0; j < " << D << "; ++j) " << tn << "[" << po
+                          << "(" << f * ar << " + i) * " << D << " + j] = x_ >= 0 ? d_[(long long)x_ * "
                           << D << " + j] : (" << T << ")0;\n";
                         O << J << "  }\n";
                     }
                     O << J << "}\n";
                 }
-                kargs.push_back("op2g::ptr(t" + an + ")");
+                if (lead) kargs.push_back("op2g::ptr(" + tn + ")");
             } else if (A.d.kind == OP2G_ARG_MAT) {
-                const int ra = S.maps[A.d.map].arity, ca = S.maps[A.d.cmap].arity;
-                const int tot = nf * ra * A.d.rdim * nf * ca * A.d.cdim;
+                if (first[a] != (int)a) continue;   // a later block of a mixed Mat
+                const int tot = psize[a];
                 O << J << T << " t" << an << "[" << tot << "];\n";
                 O << J << "#pragma unroll\n";
                 O << J << "for (int k = 0; k < " << tot << "; ++k) t" << an << "[k] = (" << T
@@ -521,8 +592,9 @@ struct Gen {
                     O << J << "#pragma unroll\n";
                     O << J << "    for (int j = 0; j < " << D << "; ++j) {\n";
                     std::string dst = "d_[(long long)x_ * " + std::to_string(D) + " + j]";
-                    std::string src = "t" + an + "[(" + std::to_string(f * ar) + " + i) * " +
-                                      std::to_string(D) + " + j]";
+                    std::string src = "t" + std::to_string(first[a]) + "[" +
+                                      std::to_string(poff[a]) + " + (" + std::to_string(f * ar) +
+                                      " + i) * " + std::to_string(D) + " + j]";
                     switch (A.d.access) {
                         case OP2G_INC:
                             if (plain) O << J << "      " << dst << " += " << src << ";\n";
@@ -547,7 +619,8 @@ struct Gen {
                 // MatSetValuesBlockedLocal(ADD|INSERT) on block-CSR storage.
                 const int ra = S.maps[A.d.map].arity, ca = S.maps[A.d.cmap].arity;
                 const int RD = A.d.rdim, CD = A.d.cdim;
-                const int ncolv = nf * ca * CD;
+                const int ncolv = rstride[a];
+                const std::string tn = "t" + std::to_string(first[a]);
                 O << J << "{ " << T << " *v_ = (" << T << " *)p.ptr[" << A.slot << "];\n";
                 O << J << "  const long long *rp_ = (const long long *)p.ptr[" << A.slot + 1 << "];\n";
                 O << J << "  const int *ci_ = (const int *)p.ptr[" << A.slot + 2 << "];\n";
@@ -565,9 +638,9 @@ struct Gen {
                         O << J << "      for (int ri = 0; ri < " << RD << "; ++ri)\n";
                         O << J << "#pragma unroll\n";
                         O << J << "        for (int cj = 0; cj < " << CD << "; ++cj) {\n";
-                        O << J << "          const " << T << " w_ = t" << an << "[((" << fr * ra
-                          << " + i) * " << RD << " + ri) * " << ncolv << " + (" << fc * ca
-                          << " + j) * " << CD << " + cj];\n";
+                        O << J << "          const " << T << " w_ = " << tn << "[(" << roff[a]
+                          << " + (" << fr * ra << " + i) * " << RD << " + ri) * " << ncolv << " + "
+                          << coff[a] << " + (" << fc * ca << " + j) * " << CD << " + cj];\n";
                         std::string dst = "v_[q_ * " + std::to_string(RD * CD) + " + ri * " +
                                           std::to_string(CD) + " + cj]";
                         if (A.d.access == OP2G_INC) {
@@ -641,6 +714,49 @@ std::string validate_signature(const Signature &S) {
             default:
                 return an + "unknown kind";
         }
+    }
+    // Groups (mixed arguments): contiguous, homogeneous, consistent block shapes.
+    for (size_t a = 0; a < S.args.size();) {
+        const op2g_arg_desc &d0 = S.args[a].d;
+        if (d0.group < 0) return "argument " + std::to_string(a) + ": negative group id";
+        size_t b = a + 1;
+        if (d0.group > 0) {
+            while (b < S.args.size() && S.args[b].d.group == d0.group) ++b;
+            for (size_t k = b; k < S.args.size(); ++k)
+                if (S.args[k].d.group == d0.group)
+                    return "group " + std::to_string(d0.group) + " is not contiguous";
+            for (size_t k = a; k < b; ++k) {
+                const op2g_arg_desc &d = S.args[k].d;
+                std::string an = "argument " + std::to_string(k) + ": ";
+                if (d.kind != d0.kind || d.access != d0.access || d.dtype != d0.dtype)
+                    return an + "grouped arguments need one kind, access and dtype";
+                if (d.kind == OP2G_ARG_DAT && d.map < 0)
+                    return an + "grouped Dat components must be indirect";
+                if (d.kind != OP2G_ARG_DAT && d.kind != OP2G_ARG_MAT)
+                    return an + "only Dats and Mats can be grouped";
+                if (d.kind == OP2G_ARG_MAT && d.group_cols != d0.group_cols)
+                    return an + "group_cols differs within the group";
+            }
+            if (d0.kind == OP2G_ARG_MAT) {
+                const int C = d0.group_cols;
+                if (C <= 0 || (b - a) % (size_t)C != 0)
+                    return "argument " + std::to_string(a) + ": group_cols must divide the block count";
+                auto rows = [&](size_t k) {
+                    const op2g_arg_desc &d = S.args[k].d;
+                    return S.maps[d.map].arity * d.rdim;
+                };
+                auto cols = [&](size_t k) {
+                    const op2g_arg_desc &d = S.args[k].d;
+                    return S.maps[d.cmap].arity * d.cdim;
+                };
+                for (size_t k = a; k < b; ++k) {
+                    size_t i = (k - a) / C, j = (k - a) % C;
+                    if (rows(k) != rows(a + i * C) || cols(k) != cols(a + j))
+                        return "argument " + std::to_string(k) + ": block shape does not match its block row/column";
+                }
+            }
+        }
+        a = b;
     }
     if (S.loop.pass_layer_arg && !S.loop.extruded) return "layer argument needs an extruded loop";
     return "";

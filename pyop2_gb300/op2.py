@@ -8,18 +8,19 @@ from pyop2_gb300.logger import debug, info, warning, error, critical, set_log_le
 from pyop2_gb300.types import (  # noqa: F401
     Set, ExtrudedSet, MixedSet, Subset, DataSet, MixedDataSet, GlobalDataSet,
     Map, MixedMap, PermutedMap, ComposedMap, Sparsity,
-    Global, Constant, Dat, Mat,
+    Global, Constant, Dat, MixedDat, Mat,
     READ, WRITE, RW, INC, MIN, MAX, ON_BOTTOM, ON_TOP, ON_INTERIOR_FACETS, ALL)
 from pyop2_gb300.local_kernel import CStringLocalKernel, Kernel  # noqa: F401
 from pyop2_gb300.parloop import (Parloop, ParLoop, LegacyParloop, parloop, par_loop,  # noqa: F401
-                                 GlobalLegacyArg, DatLegacyArg, MatLegacyArg, PassthroughArg)
+                                 GlobalLegacyArg, DatLegacyArg, MatLegacyArg, PassthroughArg,
+                                 MixedDatLegacyArg, MixedMatLegacyArg)
 
 __all__ = ['configuration', 'READ', 'WRITE', 'RW', 'INC', 'MIN', 'MAX',
            'ON_BOTTOM', 'ON_TOP', 'ON_INTERIOR_FACETS', 'ALL',
            'debug', 'info', 'warning', 'error', 'critical', 'initialised',
            'set_log_level', 'init', 'exit', 'Kernel', 'Set', 'ExtrudedSet',
            'MixedSet', 'Subset', 'DataSet', 'GlobalDataSet', 'MixedDataSet',
-           'Dat', 'Mat', 'Global', 'Constant', 'Map', 'MixedMap',
+           'Dat', 'MixedDat', 'Mat', 'Global', 'Constant', 'Map', 'MixedMap',
            'Sparsity', 'parloop', 'Parloop', 'ParLoop', 'par_loop',
            'PermutedMap', 'ComposedMap']
 

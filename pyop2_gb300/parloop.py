@@ -27,7 +27,7 @@ from pyop2_gb300.local_kernel import CStringLocalKernel, LocalKernel
 from pyop2_gb300.types.access import ALL, Access, IterationRegion
 from pyop2_gb300.types.dat import Dat
 from pyop2_gb300.types.glob import Constant, Global
-from pyop2_gb300.types.map import ComposedMap, Map, PermutedMap
+from pyop2_gb300.types.map import ComposedMap, Map, MixedMap, PermutedMap
 from pyop2_gb300.types.mat import Mat
 from pyop2_gb300.types.set import ExtrudedSet, MixedSet, Set, Subset
 
@@ -80,6 +80,48 @@ class MatLegacyArg(LegacyArg):
 
 
 @dataclass
+class MixedDatLegacyArg(LegacyArg):
+    """A MixedDat through a MixedMap (pyop2/parloop.py:600-621): one kernel
+    argument whose pack concatenates the components' packs."""
+    data: Any
+    map_: Any
+    access: Access
+
+    @property
+    def dtype(self):
+        return self.data.dtype
+
+    @property
+    def maps(self):
+        return tuple(self.map_)
+
+    def components(self):
+        return [DatLegacyArg(d, m, self.access) for d, m in zip(self.data, self.map_)]
+
+
+@dataclass
+class MixedMatLegacyArg(LegacyArg):
+    """A mixed Mat through a pair of MixedMaps (pyop2/parloop.py:649-678):
+    one element matrix over all blocks, block (i, j) inserted into
+    ``mat[i, j]`` through ``(rmap.split[i], cmap.split[j])``."""
+    data: Mat
+    maps: Tuple[Any, Any]
+    access: Access
+    lgmaps: Optional[Tuple[Any, Any]] = None
+    needs_unrolling: Optional[bool] = False
+
+    @property
+    def dtype(self):
+        return self.data.dtype
+
+    def components(self):
+        rm, cm = self.maps
+        nr, nc = self.data.sparsity.shape
+        return [MatLegacyArg(self.data[i, j], (rm.split[i], cm.split[j]), self.access)
+                for i in range(nr) for j in range(nc)]
+
+
+@dataclass
 class PassthroughArg(LegacyArg):
     """A raw device pointer handed to the kernel untouched (dtype for codegen)."""
     dtype: Any
@@ -94,7 +136,10 @@ class PassthroughArg(LegacyArg):
 # ------------------------------------------------------------- validation
 def _check_map(m):
     if configuration["type_check"]:
-        if isinstance(m, ComposedMap):
+        if isinstance(m, MixedMap):
+            for m_ in m.split:
+                _check_map(m_)
+        elif isinstance(m, ComposedMap):
             for m_ in m.maps_:
                 _check_map(m_)
         elif isinstance(m, PermutedMap):
@@ -241,7 +286,7 @@ class Parloop:
         if pass_layer_arg and not iterset._extruded:
             raise ValueError("Cannot request layer argument for non-extruded iteration")
         for a in args:
-            for m in (a.maps if not isinstance(a, MatLegacyArg) else a.maps):
+            for m in a.maps:
                 _check_map(m)
             if isinstance(a, GlobalLegacyArg) and isinstance(a.data, Constant) \
                     and a.access is not Access.READ:
@@ -253,6 +298,20 @@ class Parloop:
         self.iteration_region = IterationRegion(iteration_region or ALL)
         self.pass_layer_arg = bool(pass_layer_arg)
         self._built = None
+        # Arguments as the wrapper sees them: mixed arguments become their
+        # components, tagged with a group id (one kernel parameter per group)
+        # and, for Mats, the number of block columns.
+        flat = []
+        group = 0
+        for a in self.args:
+            if isinstance(a, (MixedDatLegacyArg, MixedMatLegacyArg)):
+                group += 1
+                cols = a.data.sparsity.shape[1] if isinstance(a, MixedMatLegacyArg) else 0
+                flat += [(c, group, cols) for c in a.components()]
+            else:
+                flat.append((a, 0, 0))
+        self._flat = flat
+        self._components = [c for c, _, _ in flat]
 
     @property
     def accesses(self):
@@ -266,25 +325,23 @@ class Parloop:
     def _signature(self):
         table = _MapTable()
         argdescs = []
-        for a in self.args:
+        for a, group, gcols in self._flat:
             if isinstance(a, GlobalLegacyArg):
-                argdescs.append((_lib.ARG_GLOBAL, int(a.access), as_code(a.data.dtype),
-                                 a.data.cdim, -1, -1, 0, 0))
+                d = (_lib.ARG_GLOBAL, int(a.access), as_code(a.data.dtype), a.data.cdim, -1, -1,
+                     0, 0)
             elif isinstance(a, DatLegacyArg):
                 mi = table.add(a.map_) if a.map_ is not None else -1
-                argdescs.append((_lib.ARG_DAT, int(a.access), as_code(a.data.dtype),
-                                 a.data.cdim, mi, -1, 0, 0))
+                d = (_lib.ARG_DAT, int(a.access), as_code(a.data.dtype), a.data.cdim, mi, -1, 0, 0)
             elif isinstance(a, MatLegacyArg):
                 rm = table.add(a.maps[0])
                 cm = table.add(a.maps[1])
                 rdim, cdim = a.data.dims[0][0]
-                argdescs.append((_lib.ARG_MAT, int(a.access), as_code(a.data.dtype), 1, rm, cm,
-                                 rdim, cdim))
+                d = (_lib.ARG_MAT, int(a.access), as_code(a.data.dtype), 1, rm, cm, rdim, cdim)
             elif isinstance(a, PassthroughArg):
-                argdescs.append((_lib.ARG_PASSTHROUGH, int(Access.RW), as_code(a.dtype), 1,
-                                 -1, -1, 0, 0))
+                d = (_lib.ARG_PASSTHROUGH, int(Access.RW), as_code(a.dtype), 1, -1, -1, 0, 0)
             else:
                 raise ValueError("Unhandled argument type %r" % type(a))
+            argdescs.append(d + (group, gcols))
         return table, argdescs
 
     def _loop_desc(self, scatter, block_size):
@@ -301,7 +358,7 @@ class Parloop:
     def _needs_conflict_handling(self):
         return any(isinstance(a, (DatLegacyArg, MatLegacyArg)) and
                    (isinstance(a, MatLegacyArg) or a.map_ is not None) and
-                   a.access in (Access.INC, Access.MIN, Access.MAX) for a in self.args)
+                   a.access in (Access.INC, Access.MIN, Access.MAX) for a in self._components)
 
     def _choose_strategy(self):
         mode = configuration["scatter"]
@@ -323,7 +380,7 @@ class Parloop:
     def _colourable(self):
         if self.iterset._extruded or isinstance(self.iterset, Subset):
             return False
-        for a in self.args:
+        for a in self._components:
             if isinstance(a, DatLegacyArg) and a.map_ is not None and \
                     a.access in (Access.INC, Access.MIN, Access.MAX, Access.WRITE, Access.RW):
                 if isinstance(a.map_, ComposedMap):
@@ -359,7 +416,7 @@ class Parloop:
         error-word pointer."""
         ptrs = []
         err = None
-        for a in self.args:
+        for a in self._components:
             if isinstance(a, (GlobalLegacyArg, DatLegacyArg)):
                 ptrs.append(a.data._device_ptr())
             elif isinstance(a, MatLegacyArg):
@@ -401,7 +458,7 @@ class Parloop:
             self.build()
         scatter, bs, k, table, argdescs = self._built
         it = self.iterset
-        for a in self.args:
+        for a in self._components:
             if isinstance(a, MatLegacyArg):
                 a.data.change_assembly_state(Mat.ADD_VALUES if a.access is Access.INC
                                              else Mat.INSERT_VALUES)
@@ -419,7 +476,7 @@ class Parloop:
         toset = (ctypes.c_int64 * max(1, len(table.objs)))()
         for i in range(len(table.entries)):
             toset[i] = 2**62
-        for a in self.args:
+        for a in self._components:
             if isinstance(a, DatLegacyArg) and a.map_ is not None:
                 toset[table.add(a.map_)] = a.data.dataset.total_size
         D = _lib.LaunchDesc()
@@ -438,6 +495,11 @@ class Parloop:
     def mark_written(self):
         """State updates after a launch (pyop2/parloop.py:454-468)."""
         for a in self.args:
+            if isinstance(a, MixedMatLegacyArg) and a.access is not Access.READ:
+                a.data.assembly_state = (Mat.ADD_VALUES if a.access is Access.INC
+                                         else Mat.INSERT_VALUES)
+                a.data.increment_dat_version()
+        for a in self._components:
             if a.access is Access.READ or isinstance(a, PassthroughArg):
                 continue
             if isinstance(a, MatLegacyArg):
@@ -531,7 +593,7 @@ def colour_plan(loop, max_colours=256):
     if isinstance(it, Subset):
         raise NotImplementedError("coloured execution of subsets")
     maps = []
-    for a in loop.args:
+    for a in loop._components:
         if a.access is Access.READ:
             continue
         if isinstance(a, DatLegacyArg) and a.map_ is not None:

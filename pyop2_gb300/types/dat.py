@@ -393,3 +393,231 @@ class Dat(AbstractDat):
 
     def local_to_global_end(self, insert_mode):
         pass
+
+
+class MixedDat(AbstractDat):
+    """A tuple of Dats over the components of a MixedDataSet
+    (pyop2/types/dat.py:787-1151).
+
+    ``MixedDat(mdset_or_sets_or_dats)``: a MixedDataSet, MixedSet or iterable
+    of DataSets/Sets makes new zeroed Dats; an iterable of Dats is used as
+    is; a MixedDat is copied.  ``mdat(access, mixed_map)`` hands the kernel
+    one pack that concatenates the components' packs.
+    """
+
+    def __init__(self, mdset_or_dats):
+        from pyop2_gb300.types.glob import Global
+
+        def make(x):
+            if isinstance(x, (Dat, Global)):
+                return x
+            if isinstance(x, (DataSet, Set)):
+                return Dat(x)
+            raise ex.DataSetTypeError("MixedDat components must be Dats, DataSets or Sets, "
+                                      "not %r" % type(x))
+        if isinstance(mdset_or_dats, MixedDat):
+            self._dats = tuple(Dat(d) for d in mdset_or_dats)
+        else:
+            self._dats = tuple(make(d) for d in mdset_or_dats)
+        if not all(d.dtype == self._dats[0].dtype for d in self._dats):
+            raise ex.DataValueError("MixedDat with different dtypes is not supported")
+        self.comm = None
+
+    @utils.validate_in(('access', AbstractDat._modes, ex.ModeValueError))
+    def __call__(self, access, path=None):
+        from pyop2_gb300.parloop import MixedDatLegacyArg
+        from pyop2_gb300.types.map import MixedMap
+        if not isinstance(path, MixedMap):
+            raise ex.MapTypeError("A MixedDat is accessed through a MixedMap")
+        if len(path) != len(self._dats):
+            raise ex.MapValueError("MixedMap has %d maps for %d Dats" % (len(path), len(self._dats)))
+        for d, m in zip(self._dats, path):
+            # the reference does not compare tosets here; a map reaching
+            # past its Dat's storage is still refused (it would address
+            # outside the device buffer)
+            if m.toset.total_size > d.dataset.total_size:
+                raise ex.MapValueError("Map %s reaches beyond Dat %s" % (m.name, d.name))
+        return MixedDatLegacyArg(self, path, access)
+
+    @property
+    def dat_version(self):
+        return sum(d.dat_version for d in self._dats)
+
+    def increment_dat_version(self):
+        for d in self._dats:
+            d.increment_dat_version()
+
+    def __getitem__(self, idx):
+        return self._dats[idx]
+
+    def __iter__(self):
+        yield from self._dats
+
+    def __len__(self):
+        return len(self._dats)
+
+    @property
+    def split(self):
+        return self._dats
+
+    @property
+    def dtype(self):
+        return self._dats[0].dtype
+
+    @property
+    def dataset(self):
+        from pyop2_gb300.types.dataset import MixedDataSet
+        return MixedDataSet(tuple(d.dataset for d in self._dats))
+
+    @property
+    def name(self):
+        return tuple(d.name for d in self._dats)
+
+    @property
+    def nbytes(self):
+        return int(sum(d.nbytes for d in self._dats))
+
+    @property
+    def data(self):
+        return tuple(d.data for d in self._dats)
+
+    @property
+    def data_with_halos(self):
+        return tuple(d.data_with_halos for d in self._dats)
+
+    @property
+    def data_ro(self):
+        return tuple(d.data_ro for d in self._dats)
+
+    @property
+    def data_ro_with_halos(self):
+        return tuple(d.data_ro_with_halos for d in self._dats)
+
+    @property
+    def data_wo(self):
+        return tuple(d.data_wo for d in self._dats)
+
+    @property
+    def data_wo_with_halos(self):
+        return tuple(d.data_wo_with_halos for d in self._dats)
+
+    @property
+    def _data(self):
+        return tuple(d._data for d in self._dats)
+
+    @property
+    def halo_valid(self):
+        return all(d.halo_valid for d in self._dats)
+
+    @halo_valid.setter
+    def halo_valid(self, val):
+        for d in self._dats:
+            d.halo_valid = val
+
+    def zero(self, subset=None):
+        if subset is not None:
+            raise NotImplementedError("Subsets of mixed sets not implemented")
+        for d in self._dats:
+            d.zero()
+
+    def copy(self, other, subset=None):
+        if subset is not None:
+            raise NotImplementedError("MixedDat.copy with a Subset is not supported")
+        for s, o in zip(self, other):
+            s.copy(o)
+
+    def save(self, filename):
+        """Write the components' owned values to ``filename`` as one NumPy
+        array (components of one shape, as the reference's file format)."""
+        np.save(filename, self.data_ro)
+
+    def load(self, filename):
+        if filename[-4:] != ".npy":
+            filename = filename + ".npy"
+        for d, v in zip(self._dats, np.load(filename)):
+            d.data[:] = v
+
+    def _check_shape(self, other):
+        if tuple(d.dataset.dim for d in other) != tuple(d.dataset.dim for d in self):
+            raise ValueError("Mismatched shapes in operands")
+
+    def _op(self, other, fn):
+        if np.isscalar(other):
+            return MixedDat([fn(s, other) for s in self])
+        self._check_shape(other)
+        return MixedDat([fn(s, o) for s, o in zip(self, other)])
+
+    def _iop(self, other, fn):
+        if np.isscalar(other):
+            for s in self:
+                fn(s, other)
+        else:
+            self._check_shape(other)
+            for s, o in zip(self, other):
+                fn(s, o)
+        return self
+
+    def inner(self, other):
+        return sum(s.inner(o) for s, o in zip(self, other))
+
+    @property
+    def norm(self):
+        from math import sqrt
+        return sqrt(self.inner(self))
+
+    def __pos__(self):
+        return MixedDat([+s for s in self])
+
+    def __neg__(self):
+        return MixedDat([-s for s in self])
+
+    def __add__(self, other):
+        return self._op(other, lambda a, b: a + b)
+
+    def __radd__(self, other):
+        return self._op(other, lambda a, b: b + a)
+
+    def __sub__(self, other):
+        return self._op(other, lambda a, b: a - b)
+
+    def __rsub__(self, other):
+        return self._op(other, lambda a, b: b - a)
+
+    def __mul__(self, other):
+        return self._op(other, lambda a, b: a * b)
+
+    def __rmul__(self, other):
+        return self._op(other, lambda a, b: b * a)
+
+    def __truediv__(self, other):
+        return self._op(other, lambda a, b: a / b)
+
+    def __iadd__(self, other):
+        return self._iop(other, lambda a, b: a.__iadd__(b))
+
+    def __isub__(self, other):
+        return self._iop(other, lambda a, b: a.__isub__(b))
+
+    def __imul__(self, other):
+        return self._iop(other, lambda a, b: a.__imul__(b))
+
+    def __itruediv__(self, other):
+        return self._iop(other, lambda a, b: a.__itruediv__(b))
+
+    def __str__(self):
+        return "OP2 MixedDat composed of Dats: %s" % (self._dats,)
+
+    def __repr__(self):
+        return "MixedDat(%r)" % (self._dats,)
+
+    def global_to_local_begin(self, access_mode):
+        pass
+
+    def global_to_local_end(self, access_mode):
+        pass
+
+    def local_to_global_begin(self, insert_mode):
+        pass
+
+    def local_to_global_end(self, insert_mode):
+        pass

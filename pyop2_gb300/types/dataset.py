@@ -106,19 +106,51 @@ class GlobalDataSet(DataSet):
 
 
 class MixedDataSet(DataSet):
-    """A tuple of DataSets (container only)."""
+    """A tuple of DataSets (pyop2/types/dataset.py:304-460).
+
+    ``MixedDataSet(mset_or_sets, dims)`` with one dim or one per set, or
+    ``MixedDataSet(iterable of DataSets and/or Sets)`` (Sets become dim 1).
+    Cached per tuple of component DataSets.
+    """
+
+    def __new__(cls, arg, dims=None):
+        dsets = cls._process_args(arg, dims)
+        key = ("MixedDataSet", dsets)
+        holder = dsets[0].set._cache
+        obj = holder.get(key)
+        if obj is None:
+            obj = object.__new__(cls)
+            obj._initialized = False
+            obj._pending = dsets
+            holder[key] = obj
+        return obj
+
+    @staticmethod
+    def _process_args(arg, dims=None):
+        from pyop2_gb300.types.set import MixedSet
+        if dims is not None:
+            sets = arg.split if isinstance(arg, MixedSet) else tuple(arg)
+            dims = (dims,) * len(sets) if isinstance(dims, numbers.Integral) else tuple(dims)
+            if len(sets) != len(dims):
+                raise ValueError("Got MixedSet of %d Sets but %s dims" % (len(sets), len(dims)))
+            return tuple(s ** d for s, d in zip(sets, dims))
+        out = tuple(s if isinstance(s, DataSet) else s ** 1 for s in arg)
+        for d in out:
+            if not isinstance(d, DataSet):
+                raise TypeError("MixedDataSet components must be DataSets or Sets")
+        return out
 
     def __init__(self, arg, dims=None):
-        sets = tuple(arg)
-        if dims is None:
-            self._dsets = tuple(s if isinstance(s, DataSet) else s ** 1 for s in sets)
-        else:
-            dims = dims if isinstance(dims, (tuple, list)) else (dims,) * len(sets)
-            self._dsets = tuple(s ** d for s, d in zip(sets, dims))
+        if self._initialized:
+            return
+        self._dsets = self._pending
         self._set = None
-        self._initialized = True
         self._name = "mdset_#x%x" % id(self)
         self.comm = None
+        self._initialized = True
+
+    def __getattr__(self, name):
+        raise AttributeError(name)
 
     def __getitem__(self, idx):
         return self._dsets[idx]
@@ -140,3 +172,37 @@ class MixedDataSet(DataSet):
     @property
     def cdim(self):
         return sum(s.cdim for s in self._dsets)
+
+    @property
+    def name(self):
+        return tuple(s.name for s in self._dsets)
+
+    @property
+    def set(self):
+        from pyop2_gb300.types.set import MixedSet
+        return MixedSet(s.set for s in self._dsets)
+
+    @property
+    def size(self):
+        return sum(s.size for s in self._dsets)
+
+    @property
+    def total_size(self):
+        return sum(s.total_size for s in self._dsets)
+
+    @property
+    def offsets(self):
+        """Start of each component in the concatenated dof numbering."""
+        o = [0]
+        for s in self._dsets:
+            o.append(o[-1] + s.size * s.cdim)
+        return tuple(o)
+
+    def __contains__(self, dat):
+        return dat.dataset == self
+
+    def __str__(self):
+        return "OP2 MixedDataSet composed of DataSets: %s" % (self._dsets,)
+
+    def __repr__(self):
+        return "MixedDataSet(%r)" % (self._dsets,)

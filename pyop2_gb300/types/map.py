@@ -1,5 +1,5 @@
 """Maps (pyop2/types/map.py): Map :17-168, PermutedMap :171-215,
-ComposedMap :218-294, MixedMap :297-434 (container only).
+ComposedMap :218-294, MixedMap :297-434.
 
 Map values live on the device as int32 ``[iterset.total_size, arity]``; the
 host copy is kept read-only so the two can never diverge.
@@ -237,13 +237,35 @@ class ComposedMap(Map):
 
 
 class MixedMap(Map):
-    """A tuple of Maps (container only)."""
+    """A tuple of Maps from one iteration set (pyop2/types/map.py:297-434).
+    Cached per tuple of component maps.  Used with a MixedDat (one pack
+    concatenating the components' packs) or as a mixed Mat's row/column map."""
+
+    def __new__(cls, maps):
+        maps = tuple(maps)
+        key = ("MixedMap", maps)
+        holder = maps[0]._cache
+        obj = holder.get(key)
+        if obj is None:
+            obj = object.__new__(cls)
+            obj._initialized = False
+            holder[key] = obj
+        return obj
 
     def __init__(self, maps):
-        self._maps = tuple(maps)
+        if self._initialized:
+            return
+        maps = tuple(maps)
+        for m in maps:
+            if not isinstance(m, Map):
+                raise ex.MapTypeError("MixedMap components must be Maps, not %r" % type(m))
+        if len(set(id(m.iterset) for m in maps)) != 1:
+            raise RuntimeError("Found multiple itersets.")
+        self._maps = maps
         self.comm = None
         self._name = "mmap_#x%x" % id(self)
         self._cache = {}
+        self._initialized = True
 
     @property
     def split(self):
@@ -255,9 +277,17 @@ class MixedMap(Map):
     def __len__(self):
         return len(self._maps)
 
+    def __getitem__(self, idx):
+        return self._maps[idx]
+
     @property
     def iterset(self):
         return self._maps[0].iterset
+
+    @property
+    def toset(self):
+        from pyop2_gb300.types.set import MixedSet
+        return MixedSet(tuple(m.toset for m in self._maps))
 
     @property
     def arity(self):
@@ -266,3 +296,40 @@ class MixedMap(Map):
     @property
     def arities(self):
         return tuple(m.arity for m in self._maps)
+
+    @property
+    def arange(self):
+        return (0,) + tuple(int(x) for x in np.cumsum(self.arities))
+
+    @property
+    def values(self):
+        return tuple(m.values for m in self._maps)
+
+    @property
+    def values_with_halo(self):
+        return tuple(m.values_with_halo for m in self._maps)
+
+    @property
+    def name(self):
+        return tuple(m.name for m in self._maps)
+
+    @property
+    def offset(self):
+        return tuple(0 if m.offset is None else m.offset for m in self._maps)
+
+    @property
+    def offset_quotient(self):
+        return tuple(0 if m.offset_quotient is None else m.offset_quotient for m in self._maps)
+
+    @property
+    def flattened_maps(self):
+        raise NotImplementedError("flattened_maps is not defined for a MixedMap")
+
+    def __le__(self, o):
+        return self is o or all(m <= om for m, om in zip(self, o))
+
+    def __str__(self):
+        return "OP2 MixedMap composed of Maps: %s" % (self._maps,)
+
+    def __repr__(self):
+        return "MixedMap(%r)" % (self._maps,)

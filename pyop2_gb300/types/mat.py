@@ -25,6 +25,11 @@ from pyop2_gb300.types.dataset import DataSet, GlobalDataSet, MixedDataSet
 from pyop2_gb300.types.map import ComposedMap, Map, PermutedMap
 
 
+def _is_mixed_map(m):
+    from pyop2_gb300.types.map import MixedMap
+    return isinstance(m, MixedMap)
+
+
 def _flatten_map(m):
     """(base plain Map, permutation or None) of a Map/PermutedMap."""
     if isinstance(m, PermutedMap):
@@ -45,7 +50,7 @@ class Sparsity:
         dsets_p, mr, kw = cls._process_args(dsets, maps_and_regions, name, nest, block_sparse,
                                             diagonal_block)
         key = ("Sparsity", dsets_p, tuple(sorted(mr.items(), key=lambda kv: kv[0])),
-               kw["block_sparse"], kw["diagonal_block"])
+               kw["block_sparse"], kw["diagonal_block"], kw["nest"])
         cache = dsets_p[0].set._cache if not isinstance(dsets_p[0], GlobalDataSet) else {}
         obj = cache.get(key)
         if obj is None:
@@ -67,13 +72,57 @@ class Sparsity:
         self._name = kw["name"] or "sparsity_#x%x" % id(self)
         rset, cset = dsets
         self._has_diagonal = (rset == cset) and self._diagonal_block
+        self.comm = rset.comm
+        self._nest = bool(kw["nest"])
+        if isinstance(rset, MixedDataSet) or isinstance(cset, MixedDataSet):
+            self._init_mixed()
+            self._initialized = True
+            return
         self._dims = (((rset.cdim, cset.cdim),),)
         self._nested = False
-        self.comm = rset.comm
+        self._blocks = [[self]]
         from pyop2_gb300.profiling import timed_region
         with timed_region("CreateSparsity"):      # pyop2/types/mat.py:105-113
             self._build()
         self._initialized = True
+
+    def _init_mixed(self):
+        """Blocks of a sparsity between MixedDataSets (pyop2/types/mat.py:86-95,
+        pyop2/sparsity.pyx:144-159).  Every block (i, j) is built on the GPU
+        from its own map pairs; block (i, i) carries the diagonal.  Nested:
+        ``nnz`` is the tuple of the blocks' ``nnz``.  Monolithic: ``nnz``
+        counts the dof columns of each row of the assembled whole, i.e. the
+        blocks of a block row laid side by side."""
+        rset, cset = self._dsets
+        rsets = tuple(rset) if isinstance(rset, MixedDataSet) else (rset,)
+        csets = tuple(cset) if isinstance(cset, MixedDataSet) else (cset,)
+        self._dims = tuple(tuple((r.cdim, c.cdim) for c in csets) for r in rsets)
+        self._nested = self._nest
+        self._blocks = []
+        for i, rds in enumerate(rsets):
+            row = []
+            for j, cds in enumerate(csets):
+                pairs = tuple(self._maps_and_regions.get((i, j), ()))
+                if self._nested:
+                    diag = rset is cset and i == j
+                else:
+                    diag = i == j and self._has_diagonal
+                row.append(Sparsity((rds, cds), pairs, block_sparse=self._block_sparse,
+                                    diagonal_block=diag, nest=False))
+            self._blocks.append(row)
+        if self._nested:
+            self._d_nnz = tuple(b._d_nnz for row in self._blocks for b in row)
+            self._o_nnz = tuple(b._o_nnz for row in self._blocks for b in row)
+        else:
+            rows = []
+            for i, row in enumerate(self._blocks):
+                rdim = rsets[i].cdim
+                acc = np.zeros(rsets[i].size, dtype=np.int64)
+                for j, b in enumerate(row):
+                    acc += np.diff(b.rowptr.cpu().numpy()) * csets[j].cdim
+                rows.append(np.repeat(acc, rdim))
+            self._d_nnz = np.concatenate(rows).astype(IntType)
+            self._o_nnz = np.zeros_like(self._d_nnz)
 
     @classmethod
     def _process_args(cls, dsets, maps_and_regions, name, nest, block_sparse, diagonal_block):
@@ -83,16 +132,17 @@ class Sparsity:
         for d in dsets:
             if not isinstance(d, DataSet) and d is not None:
                 raise ex.DataSetTypeError("All data sets must be of type DataSet, not type %r" % type(d))
-        if isinstance(dsets[0], MixedDataSet) or isinstance(dsets[1], MixedDataSet):
-            raise NotImplementedError("mixed sparsities are not part of the GPU path")
         if isinstance(maps_and_regions, Sequence):
             maps_and_regions = {(0, 0): maps_and_regions}
         elif not isinstance(maps_and_regions, dict):
             raise TypeError("maps_and_regions must be dict or Sequence: got %s" % type(maps_and_regions))
+        nr, nc = len(dsets[0]), len(dsets[1])
         out = {}
         for key, val in maps_and_regions.items():
-            if key != (0, 0):
-                raise RuntimeError("(i, j) must be < (1, 1): got %s" % (key,))
+            i, j = key
+            if i >= nr or j >= nc:
+                raise RuntimeError("(i, j) must be < %s: got %s" % ((nr, nc), (i, j)))
+            rds, cds = dsets[0][i], dsets[1][j]
             processed = set()
             for item in set(val):
                 rmap, cmap, regions = item
@@ -102,7 +152,7 @@ class Sparsity:
                     if not isinstance(m, ComposedMap) and len(m.values_with_halo) == 0 \
                             and m.iterset.total_size > 0:
                         raise ex.MapValueError("Unpopulated map values when trying to build sparsity.")
-                if rmap.toset is not dsets[0].set or cmap.toset is not dsets[1].set:
+                if rmap.toset is not rds.set or cmap.toset is not cds.set:
                     raise RuntimeError("Map toset must be the same as DataSet set")
                 if rmap.iterset is not cmap.iterset:
                     raise RuntimeError("Iterset of both maps in a pair must be the same")
@@ -112,6 +162,8 @@ class Sparsity:
                 out[key] = frozenset(processed)
         if nest is None:
             nest = configuration["matnest"]
+        if not (isinstance(dsets[0], MixedDataSet) or isinstance(dsets[1], MixedDataSet)):
+            nest = False      # only meaningful between mixed spaces
         if block_sparse is None:
             block_sparse = configuration["block_sparsity"]
         return tuple(dsets), out, {"name": name, "nest": nest, "block_sparse": block_sparse,
@@ -239,7 +291,8 @@ class Sparsity:
 
     @property
     def shape(self):
-        return (1, 1)
+        """Number of block rows and columns."""
+        return (len(self._dsets[0]), len(self._dsets[1]))
 
     @property
     def nested(self):
@@ -284,17 +337,28 @@ class Sparsity:
         return self._rowptr.cpu().numpy(), self.colidx.cpu().numpy()
 
     def __getitem__(self, idx):
-        return self
+        """Block (i, j), or block row i."""
+        try:
+            i, j = idx
+            return self._blocks[i][j]
+        except TypeError:
+            return self._blocks[idx]
 
     def __iter__(self):
-        yield self
+        """Blocks by row, then by column."""
+        for row in self._blocks:
+            yield from row
 
     def __contains__(self, other):
-        rm, cm = other
-        for pr, pc in self.rcmaps.get((0, 0), []):
-            if (rm, cm) == (pr, pc):
-                return True
-        return False
+        """True if the (row map, column map) pair -- of MixedMaps for a mixed
+        sparsity -- is one this sparsity was built from (block by block)."""
+        rmaps = tuple(other[0]) if len(self._dsets[0]) > 1 or _is_mixed_map(other[0]) else (other[0],)
+        cmaps = tuple(other[1]) if len(self._dsets[1]) > 1 or _is_mixed_map(other[1]) else (other[1],)
+        for i, rm in enumerate(rmaps):
+            for j, cm in enumerate(cmaps):
+                if not any((rm, cm) == (pr, pc) for pr, pc in self.rcmaps.get((i, j), [])):
+                    return False
+        return True
 
     def __str__(self):
         return "OP2 Sparsity: dsets %s, name %s" % (self._dsets, self._name)
@@ -326,6 +390,19 @@ class Mat(DataCarrier):
         self._name = name or "mat_#x%x" % id(self)
         self.mat_type = mat_type
         self.comm = sparsity.comm
+        if sparsity.shape != (1, 1):
+            # A mixed Mat: one device matrix per block (MatNest-like for both
+            # nested and monolithic sparsities; pyop2/types/mat.py:572-666).
+            self._blocks = [[Mat(sparsity[i, j], self._datatype,
+                                 "_".join([self._name, str(i), str(j)]))
+                             for j in range(sparsity.shape[1])]
+                            for i in range(sparsity.shape[0])]
+            self._values = None
+            self._err = None
+            self.assembly_state = Mat.ASSEMBLED
+            self._version = 0
+            return
+        self._blocks = [[self]]
         rdim, cdim = sparsity.dims[0][0]
         self._values = torch.zeros(max(sparsity.nblocks * rdim * cdim, 1), dtype=torch.float64,
                                    device=device.device())
@@ -335,7 +412,18 @@ class Mat(DataCarrier):
 
     @utils.validate_in(('access', _modes, ex.ModeValueError))
     def __call__(self, access, path, lgmaps=None, unroll_map=False):
-        from pyop2_gb300.parloop import MatLegacyArg
+        from pyop2_gb300.parloop import MatLegacyArg, MixedMatLegacyArg
+        if self._mixed:
+            rm, cm = path
+            if not (_is_mixed_map(rm) and _is_mixed_map(cm)):
+                raise ex.MapTypeError("A mixed Mat is accessed through a pair of MixedMaps")
+            if (len(rm), len(cm)) != self._sparsity.shape:
+                raise ex.MapValueError("MixedMaps do not match the Mat's block shape")
+            if configuration["type_check"] and (rm, cm) not in self.sparsity:
+                raise ex.MapValueError("Path maps not in sparsity maps")
+            if unroll_map:
+                raise NotImplementedError("unrolled (MatSetValuesLocal) insertion is not supported")
+            return MixedMatLegacyArg(self, (rm, cm), access, lgmaps, unroll_map)
         path_maps = utils.as_tuple(path, Map, 2)
         if configuration["type_check"] and tuple(path_maps) not in self.sparsity:
             raise ex.MapValueError("Path maps not in sparsity maps")
@@ -361,12 +449,16 @@ class Mat(DataCarrier):
         return self._name
 
     @property
+    def _mixed(self):
+        return self._sparsity.shape != (1, 1)
+
+    @property
     def nrows(self):
-        return self._sparsity.dsets[0].size * self.dims[0][0][0]
+        return sum(d.size * d.cdim for d in self._sparsity.dsets[0])
 
     @property
     def ncols(self):
-        return self._sparsity.dsets[1].size * self.dims[0][0][1]
+        return sum(d.size * d.cdim for d in self._sparsity.dsets[1])
 
     @property
     def nblock_rows(self):
@@ -378,6 +470,8 @@ class Mat(DataCarrier):
 
     @property
     def nbytes(self):
+        if self._mixed:
+            return sum(b.nbytes for b in self)
         rdim, cdim = self.dims[0][0]
         return self._sparsity.nblocks * rdim * cdim * self.dtype.itemsize
 
@@ -400,14 +494,21 @@ class Mat(DataCarrier):
         return b
 
     def __iter__(self):
-        yield self
+        """Blocks by row, then by column (the Mat itself when not mixed)."""
+        for row in self._blocks:
+            yield from row
 
     def __getitem__(self, idx):
-        return self
+        """Block (i, j), or block row i."""
+        try:
+            i, j = idx
+            return self._blocks[i][j]
+        except TypeError:
+            return self._blocks[idx]
 
     @property
     def blocks(self):
-        return [[self]]
+        return self._blocks
 
     # ---- assembly state machine (pyop2/types/mat.py:488-501, 820-835)
     def change_assembly_state(self, new_state):
@@ -421,6 +522,10 @@ class Mat(DataCarrier):
         self._check_err()
 
     def _check_err(self):
+        if self._mixed:
+            for b in self:
+                b._check_err()
+            return
         err = int(self._err.item())
         if err:
             self._err.zero_()
@@ -431,18 +536,30 @@ class Mat(DataCarrier):
                 raise ex.MapValueError("Mat %s: map value out of range" % self._name)
 
     def assemble(self):
+        if self._mixed:
+            for b in self:
+                b.assemble()
         self._check_err()
         self.change_assembly_state(Mat.ASSEMBLED)
 
     def zero(self):
         self.assemble()
-        self._values.zero_()
+        if self._mixed:
+            for b in self:
+                b.zero()
+        else:
+            self._values.zero_()
         self.increment_dat_version()
+
+    def _not_mixed(self, what):
+        if self._mixed:
+            raise NotImplementedError("%s on a mixed Mat: call it on a block, mat[i, j]" % what)
 
     def zero_rows(self, rows, diag_val=1.0):
         """Zero the given (dof) rows keeping the pattern; put diag_val on the
         diagonal (PETSc zeroRowsLocal)."""
         from pyop2_gb300.types.set import Subset
+        self._not_mixed("zero_rows")
         self.assemble()
         rows = rows.indices if isinstance(rows, Subset) else rows
         r = torch.as_tensor(np.asarray(rows, dtype=IntType).reshape(-1), device=device.device())
@@ -454,6 +571,7 @@ class Mat(DataCarrier):
     def set_local_diagonal_entries(self, rows, diag_val=1.0, idx=None):
         """INSERT diag_val at the diagonal of the given rows
         (pyop2/types/mat.py:806-827 semantics for block rows)."""
+        self._not_mixed("set_local_diagonal_entries")
         rows = np.asarray(rows, dtype=IntType)
         rbs, _ = self.dims[0][0]
         if rbs > 1:
@@ -473,6 +591,7 @@ class Mat(DataCarrier):
     def _insert(self, rows, cols, values, add):
         """MatSetValuesBlockedLocal semantics from the host: rows/cols are
         block indices, values a (len(rows) * rdim) x (len(cols) * cdim) array."""
+        self._not_mixed("addto_values/set_values")
         rows = np.atleast_1d(np.asarray(rows, dtype=np.int64))
         cols = np.atleast_1d(np.asarray(cols, dtype=np.int64))
         rdim, cdim = self.dims[0][0]
@@ -520,6 +639,7 @@ class Mat(DataCarrier):
     # ---- exports
     def csr(self):
         """(rowptr, block colidx, values[nblocks, rdim, cdim]) on the host."""
+        self._not_mixed("csr")
         rp, ci = self._sparsity.csr()
         rdim, cdim = self.dims[0][0]
         v = self.tensor.cpu().numpy().reshape(-1, rdim, cdim)
@@ -528,6 +648,11 @@ class Mat(DataCarrier):
     def to_scipy(self):
         """scipy.sparse BSR (or CSR for 1x1 blocks) copy of the matrix."""
         import scipy.sparse as sps
+        if self._mixed:
+            # the monolithic view: blocks laid out by the dof offsets of the
+            # mixed spaces
+            return sps.bmat([[b.to_scipy() for b in row] for row in self._blocks],
+                            format="csr")
         rp, ci, v = self.csr()
         rdim, cdim = self.dims[0][0]
         shape = (self.nrows, self.ncols)
@@ -545,7 +670,27 @@ class Mat(DataCarrier):
         return self.to_scipy().toarray()
 
     def mult(self, x, y, transpose=False):
-        """y = A x (or A^T x) for float64 Dats x, y."""
+        """y = A x (or A^T x) for float64 Dats x, y (MixedDats for a mixed
+        Mat: y_i = sum_j A_ij x_j)."""
+        if self._mixed:
+            self.assemble()
+            nr, nc = self._sparsity.shape
+            outer, inner = (nc, nr) if transpose else (nr, nc)
+            for i in range(outer):
+                acc = None
+                for j in range(inner):
+                    b = self._blocks[j][i] if transpose else self._blocks[i][j]
+                    if b.sparsity.nblocks == 0:
+                        continue
+                    t = y[i].__class__(y[i].dataset, None, y[i].dtype)
+                    b.mult(x[j], t, transpose=transpose)
+                    acc = t.tensor.clone() if acc is None else acc.add_(t.tensor)
+                if acc is None:
+                    y[i].tensor.zero_()
+                else:
+                    y[i].tensor.copy_(acc)
+                y[i].mark_device_modified()
+            return
         self.assemble()
         b = self._bcsr()
         if transpose:

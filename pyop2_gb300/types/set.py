@@ -1,5 +1,5 @@
 """Iteration sets (pyop2/types/set.py): Set :16-226, ExtrudedSet :305-391,
-Subset :394-530, SetPartition :533-537, MixedSet :540-662 (container only)."""
+Subset :394-530, SetPartition :533-537, MixedSet :540-662."""
 import numbers
 
 import numpy as np
@@ -354,14 +354,33 @@ class Subset(ExtrudedSet):
 
 
 class MixedSet(Set):
-    """A tuple of Sets (container semantics only; mixed par_loops are not
-    part of the GPU path)."""
+    """A tuple of Sets (pyop2/types/set.py:540-662).  Never iterated over;
+    it shapes MixedDataSets, MixedDats and mixed Mats.  Cached per tuple of
+    component sets, so equal constructions return the same object."""
+
+    def __new__(cls, sets):
+        sets = tuple(sets)
+        key = ("MixedSet", sets)
+        holder = sets[0]._cache if sets and sets[0] is not None else {}
+        obj = holder.get(key)
+        if obj is None:
+            obj = super().__new__(cls)
+            obj._initialized = False
+            holder[key] = obj
+        return obj
 
     def __init__(self, sets):
-        self._sets = tuple(sets)
+        if self._initialized:
+            return
+        sets = tuple(sets)
+        for s in sets:
+            if s is not None and not isinstance(s, Set):
+                raise ex.SetTypeError("MixedSet components must be Sets, not %r" % type(s))
+        self._sets = sets
         self.comm = None
         self._name = "mset_#x%x" % id(self)
         self._cache = {}
+        self._initialized = True
 
     def __getitem__(self, idx):
         return self._sets[idx]
@@ -378,11 +397,49 @@ class MixedSet(Set):
 
     @property
     def _sizes(self):
-        return tuple(sum(s.sizes[i] for s in self._sets) for i in range(3))
+        return tuple(sum(s.sizes[i] for s in self._sets if s is not None) for i in range(3))
+
+    @property
+    def core_size(self):
+        return self._sizes[0]
+
+    @property
+    def size(self):
+        return self._sizes[1]
+
+    @property
+    def total_size(self):
+        return self._sizes[2]
+
+    @property
+    def sizes(self):
+        return self._sizes
+
+    @property
+    def name(self):
+        return tuple(s.name for s in self._sets)
+
+    @property
+    def halo(self):
+        return None
+
+    @property
+    def _extruded(self):
+        return isinstance(self._sets[0], ExtrudedSet)
+
+    @property
+    def layers(self):
+        return self._sets[0].layers if self._extruded else None
 
     def __pow__(self, e):
         from pyop2_gb300.types.dataset import MixedDataSet
         return MixedDataSet(self._sets, e)
+
+    def __str__(self):
+        return "OP2 MixedSet composed of Sets: %s" % (self._sets,)
+
+    def __repr__(self):
+        return "MixedSet(%r)" % (self._sets,)
 
 
 class GlobalSet(Set):

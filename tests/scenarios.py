@@ -711,3 +711,145 @@ def sc_extruded_regions(op2, region, periodic=False, variable=False):
                    "x[i] += (i + 1) * (layer + 1); }" % (2 * nf), "k")
     op2.par_loop(k, ext, d(op2.INC, m), iteration_region=region, pass_layer_arg=True)
     return np.asarray(d.data).copy()
+
+
+# ------------------------------------------------------------------------
+# Mixed spaces: test/unit/test_indirect_loop.py:235-269 (TestMixedIndirectLoop)
+def _mixed_indirect_fixture(op2, sizes=SIZES[0]):
+    iterset = op2.Set(sizes, "iterset")
+    indset = op2.Set(NELEMS, "indset")
+    unitset = op2.Set(1, "unitset")
+    mapd = np.arange(NELEMS)[::-1].astype(np.uint32)
+    i2ind = op2.Map(iterset, indset, 1, mapd, "iterset2indset")
+    i2unit = op2.Map(iterset, unitset, 1, np.zeros(NELEMS, dtype=np.uint32), "iterset2unitset")
+    mset = op2.MixedSet((indset, unitset))
+    return iterset, op2.MixedDat(mset), op2.MixedMap((i2ind, i2unit))
+
+
+def sc_mixed_non_mixed_dat(op2, sizes=SIZES[0], itspace=False):
+    """Increment into a MixedDat from a non-mixed Dat (both reference variants)."""
+    iterset, mdat, mmap = _mixed_indirect_fixture(op2, sizes)
+    d = op2.Dat(iterset, np.ones(NELEMS))
+    if itspace:
+        k = """static void inc(double *d, double *x) {
+          for (int i=0; i<2; ++i) d[i] += x[0]; }"""
+    else:
+        k = "static void inc(double *d, double *x) { d[0] += x[0]; d[1] += x[0]; }"
+    op2.par_loop(op2.Kernel(k, "inc"), iterset, mdat(op2.INC, mmap), d(op2.READ))
+    assert np.all(mdat[0].data == 1.0) and mdat[1].data[0] == float(NELEMS)
+
+
+# test/unit/test_matrices.py:500-530 (fixtures), 864-938 (TestMixedMatrices)
+MIXED_OD = np.array([[1.0, 2.0, 0.0, 0.0],
+                     [0.0, 4.0, 6.0, 0.0],
+                     [0.0, 0.0, 9.0, 12.0]])
+MIXED_LL = (np.diag([1.0, 8.0, 18.0, 16.0]) + np.diag([2.0, 6.0, 12.0], -1)
+            + np.diag([2.0, 6.0, 12.0], 1))
+
+
+def _mixed_mat_fixture(op2):
+    elem, node = op2.Set(3), op2.Set(4)
+    mset = op2.MixedSet((elem, node))
+    rdata = lambda n: np.arange(1, n + 1, dtype=np.float64)
+    mdat = op2.MixedDat([op2.Dat(s, rdata(s.size)) for s in mset])
+    mmap = op2.MixedMap((op2.Map(elem, elem, 1, [0, 1, 2]),
+                         op2.Map(elem, node, 2, [0, 1, 1, 2, 2, 3])))
+    return elem, node, mset, mdat, mmap, rdata
+
+
+def sc_mixed_mat(op2, nest=True):
+    """Assemble into a matrix on a mixed sparsity (block values asserted by
+    test_assemble_mixed_mat); ``nest`` selects nested or monolithic."""
+    elem, node, mset, mdat, mmap, rdata = _mixed_mat_fixture(op2)
+    blocks = {(i, j): [(rm, cm, None)] for i, rm in enumerate(mmap) for j, cm in enumerate(mmap)}
+    sp = op2.Sparsity((mset ** 1, mset ** 1), blocks, nest=nest)
+    mat = op2.Mat(sp)
+    k = """static void addone_mat(double v[9], double d[3]) {
+        for (int i = 0; i < 3; i++)
+           for (int j = 0; j < 3; j++)
+              v[i*3 + j] += d[i]*d[j];
+    }"""
+    op2.par_loop(op2.Kernel(k, "addone_mat"), elem, mat(op2.INC, (mmap, mmap)),
+                 mdat(op2.READ, mmap))
+    mat.assemble()
+    eps = 1.e-12
+    assert_allclose(mat[0, 0].values, np.diag([1.0, 4.0, 9.0]), eps)
+    assert_allclose(mat[0, 1].values, MIXED_OD, eps)
+    assert_allclose(mat[1, 0].values, MIXED_OD.T, eps)
+    assert_allclose(mat[1, 1].values, MIXED_LL, eps)
+    whole = np.block([[np.diag([1.0, 4.0, 9.0]), MIXED_OD], [MIXED_OD.T, MIXED_LL]])
+    assert_allclose(mat.values, whole, eps)
+    return sp, mat
+
+
+def sc_mixed_rhs(op2):
+    """test_assemble_mixed_rhs."""
+    elem, node, mset, mdat, mmap, rdata = _mixed_mat_fixture(op2)
+    dat = op2.MixedDat(mset)
+    k = """static void addone_rhs(double v[3], double d[3]) {
+      for (int i=0; i<3; ++i) v[i] += d[i]; }"""
+    op2.par_loop(op2.Kernel(k, "addone_rhs"), elem, dat(op2.INC, mmap), mdat(op2.READ, mmap))
+    eps = 1.e-12
+    assert_allclose(dat[0].data_ro, rdata(3), eps)
+    assert_allclose(dat[1].data_ro, [1.0, 4.0, 6.0, 4.0], eps)
+
+
+def sc_mixed_rhs_vector(op2):
+    """test_assemble_mixed_rhs_vector: dim-2 components."""
+    elem, node, mset, mdat, mmap, rdata = _mixed_mat_fixture(op2)
+    mvdat = op2.MixedDat([op2.Dat(s ** 2, np.stack([rdata(s.size), rdata(s.size)], 1))
+                          for s in mset])
+    dat = op2.MixedDat(mset ** 2)
+    k = """static void addone_rhs_vec(double v[6], double d[3][2]) {
+      for (int i=0; i<3; ++i) { v[i*2+0] += d[i][0]; v[i*2+1] += d[i][1]; } }"""
+    op2.par_loop(op2.Kernel(k, "addone_rhs_vec"), elem, dat(op2.INC, mmap),
+                 mvdat(op2.READ, mmap))
+    eps = 1.e-12
+    exp = np.kron(np.array([1.0, 4.0, 6.0, 4.0])[:, None], np.ones(2))
+    assert_allclose(dat[0].data_ro, np.kron(rdata(3)[:, None], np.ones(2)), eps)
+    assert_allclose(dat[1].data_ro, exp, eps)
+
+
+# ------------------------------------------------------------------------
+# A larger mixed problem for oracle-vs-GPU parity: P1 (vertices, dim 2) x
+# P0 (cells, dim 1) on the jittered split-square mesh; one mixed element
+# matrix (7 x 7) INC'd into a mixed Mat, and its action on a mixed vector
+# INC'd into a MixedDat.
+MIXED_P1P0 = """
+static void mixed_p1p0(double A[7][7], double b[7], const double *u, const double X[3][2])
+{
+  const double det = fabs((X[1][0] - X[0][0]) * (X[2][1] - X[0][1])
+                          - (X[2][0] - X[0][0]) * (X[1][1] - X[0][1]));
+  for (int i = 0; i < 7; ++i)
+    for (int j = 0; j < 7; ++j)
+      A[i][j] += det * (1.0 + 0.1 * i + 0.01 * j + (i == j ? 2.0 : 0.0)) * (X[i % 3][0] + 0.5);
+  for (int i = 0; i < 7; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < 7; ++j) s += A[i][j] * u[j];
+    b[i] += s;
+  }
+}
+"""
+
+
+def sc_mixed_p1p0(op2, n=16, nest=True, seed=3):
+    from pyop2_gb300.meshes import unit_square_tris
+    coords, tris = unit_square_tris(n, seed=seed)
+    V, C = coords.shape[0], tris.shape[0]
+    verts, cells = op2.Set(V, "verts"), op2.Set(C, "cells")
+    c2v = op2.Map(cells, verts, 3, tris, "c2v")
+    c2c = op2.Map(cells, cells, 1, np.arange(C, dtype=np.int32), "c2c")
+    mset = op2.MixedSet((verts, cells))
+    mdset = op2.MixedDataSet(mset, (2, 1))
+    mmap = op2.MixedMap((c2v, c2c))
+    X = op2.Dat(verts ** 2, coords, np.float64, "X")
+    rng = np.random.default_rng(seed)
+    u = op2.MixedDat([op2.Dat(verts ** 2, rng.uniform(-1, 1, (V, 2))),
+                      op2.Dat(cells, rng.uniform(-1, 1, C))])
+    b = op2.MixedDat(mdset)
+    blocks = {(i, j): [(rm, cm, None)] for i, rm in enumerate(mmap) for j, cm in enumerate(mmap)}
+    A = op2.Mat(op2.Sparsity((mdset, mdset), blocks, nest=nest))
+    op2.par_loop(op2.Kernel(MIXED_P1P0, "mixed_p1p0"), cells, A(op2.INC, (mmap, mmap)),
+                 b(op2.INC, mmap), u(op2.READ, mmap), X(op2.READ, c2v))
+    A.assemble()
+    return A, b

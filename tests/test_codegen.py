@@ -104,3 +104,64 @@ def test_compile_error_is_a_compilation_error(op2):
     with pytest.raises(CompilationError) as e:
         compile_loop(pl)
     assert "generated source" in str(e.value)
+
+
+def test_mixed_arguments_share_one_parameter(op2):
+    """MixedDat and mixed-Mat components form one kernel parameter
+    (pyop2/codegen/builder.py:413-498, 609-680)."""
+    from pyop2_gb300.parloop import MixedMatLegacyArg
+    elem, node = op2.Set(3), op2.Set(4)
+    mmap = op2.MixedMap((op2.Map(elem, elem, 1, [0, 1, 2]),
+                         op2.Map(elem, node, 2, [0, 1, 1, 2, 2, 3])))
+    mdat = op2.MixedDat([op2.Dat(elem), op2.Dat(node)])
+
+    class Block:
+        dtype = np.dtype(np.float64)
+
+        def __init__(self, rd, cd):
+            self.dims = (((rd, cd),),)
+
+    class FakeMixedMat:
+        dtype = np.dtype(np.float64)
+
+        class sparsity:
+            shape = (2, 2)
+
+        def __getitem__(self, ij):
+            return Block(1, 1)
+    k = op2.Kernel("static void addone_mat(double v[9], double d[3]) {}", "addone_mat")
+    pl = LegacyParloop(k, elem, MixedMatLegacyArg(FakeMixedMat(), (mmap, mmap), op2.INC),
+                       mdat(op2.READ, mmap))
+    src = compile_loop(pl).source()
+    # one 3 x 3 element matrix and one 3-entry pack reach the kernel
+    assert "double t0[9];" in src and "double t4[3];" in src
+    assert "addone_mat(op2g::ptr(t0), op2g::ptr(t4));" in src
+    # block (1, 1) reads rows 1.. and columns 1.. of the 3-wide element matrix
+    assert "t0[(1 + (0 + i) * 1 + ri) * 3 + 1 + (0 + j) * 1 + cj]" in src
+
+
+def _raw_compile(args, maps=((_lib.MAP_PLAIN, 2, -1, (), None, None, None),)):
+    loop = dict(extruded=0, constant_layers=0, extruded_periodic=0, indexed=0,
+                iteration_region=4, pass_layer_arg=0, scatter=0, block_size=256,
+                debug_checks=0, batched=0)
+    return compile_signature("static void k(double *a) {}", "k", loop, args, list(maps),
+                             arch="sm_103a")
+
+
+@pytest.mark.parametrize("args,msg", [
+    # a group split by another argument
+    ([(0, 4, 0, 1, 0, -1, 0, 0, 1, 0), (0, 1, 0, 1, -1, -1, 0, 0, 0, 0),
+      (0, 4, 0, 1, 0, -1, 0, 0, 1, 0)], "not contiguous"),
+    # components of one group with different access
+    ([(0, 4, 0, 1, 0, -1, 0, 0, 1, 0), (0, 1, 0, 1, 0, -1, 0, 0, 1, 0)], "one kind"),
+    # a direct component
+    ([(0, 4, 0, 1, 0, -1, 0, 0, 1, 0), (0, 4, 0, 1, -1, -1, 0, 0, 1, 0)], "indirect"),
+    # three Mat blocks cannot form two block columns
+    ([(2, 4, 0, 1, 0, 0, 1, 1, 1, 2)] * 3, "group_cols"),
+    # a grouped Global
+    ([(1, 4, 0, 1, -1, -1, 0, 0, 1, 0)] * 2, "only Dats and Mats"),
+])
+def test_bad_groups_are_rejected(op2, args, msg):
+    with pytest.raises(_lib.Op2gError) as e:
+        _raw_compile(args)
+    assert msg in str(e.value)
