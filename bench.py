@@ -37,19 +37,81 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+class _Nvml:
+    """Read-only NVML queries through ctypes: SM clock, maximum SM clock and
+    the clock-event (throttle) reason bits of the GPU behind CUDA ordinal
+    ``ordinal`` (matched by PCI bus id, so CUDA_VISIBLE_DEVICES is honoured).
+    Nothing is ever set."""
+
+    SM = 1   # NVML_CLOCK_SM
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, ordinal):
+        import ctypes
+        self.c = ctypes
+        self.nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.nv.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        cu = ctypes.CDLL("libcuda.so.1")
+        cu.cuInit(0)
+        dev = ctypes.c_int()
+        if cu.cuDeviceGet(ctypes.byref(dev), int(ordinal)) != 0:
+            raise RuntimeError("cuDeviceGet failed")
+        bus = ctypes.create_string_buffer(64)
+        if cu.cuDeviceGetPCIBusId(bus, 64, dev) != 0:
+            raise RuntimeError("cuDeviceGetPCIBusId failed")
+        self.h = ctypes.c_void_p()
+        if self.nv.nvmlDeviceGetHandleByPciBusId_v2(bus.value, ctypes.byref(self.h)) != 0:
+            raise RuntimeError("no NVML handle for %s" % bus.value)
+        self._reasons = getattr(self.nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.nv.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sm_mhz(self):
+        v = self.c.c_uint()
+        self.nv.nvmlDeviceGetClockInfo(self.h, self.SM, self.c.byref(v))
+        return v.value
+
+    def sm_max_mhz(self):
+        v = self.c.c_uint()
+        self.nv.nvmlDeviceGetMaxClockInfo(self.h, self.SM, self.c.byref(v))
+        return v.value
+
+    def reasons(self):
+        v = self.c.c_ulonglong()
+        self._reasons(self.h, self.c.byref(v))
+        return [nm for bit, nm in self.REASONS.items() if v.value & bit]
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """SM clocks and throttle reasons sampled DURING the timed region: an NVML
+    poller thread (every 2 ms, first sample taken before the region starts);
+    ``nvidia-smi -lms 200`` when NVML cannot be opened."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, period_s=0.002):
         self.gpu = gpu_index
+        self.period = period_s
         self.proc = None
         self.lines = []
+        self.samples = []      # (sm_mhz, [reasons]) from NVML
+        self.nvml = None
+        self.smax = None
 
     def __enter__(self):
+        try:
+            self.nvml = _Nvml(self.gpu)
+            self.smax = self.nvml.sm_max_mhz()
+            self._stop = threading.Event()
+            self.samples.append((self.nvml.sm_mhz(), self.nvml.reasons()))
+            self._t = threading.Thread(target=self._poll, daemon=True)
+            self._t.start()
+            return self
+        except Exception:
+            self.nvml = None
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
@@ -61,11 +123,25 @@ class ClockSampler:
             self.proc = None
         return self
 
+    def _poll(self):
+        while not self._stop.wait(self.period):
+            try:
+                self.samples.append((self.nvml.sm_mhz(), self.nvml.reasons()))
+            except Exception:
+                return
+
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        if self.nvml is not None:
+            self._stop.set()
+            self._t.join(timeout=5)
+            try:
+                self.samples.append((self.nvml.sm_mhz(), self.nvml.reasons()))
+            except Exception:
+                pass
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -74,6 +150,11 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml is not None and self.samples:
+            reasons = sorted(set(r for _, rs in self.samples for r in rs))
+            return {"sm_mhz": statistics.median(m for m, _ in self.samples),
+                    "sm_max_mhz": self.smax, "reasons": reasons,
+                    "samples": len(self.samples), "source": "nvml, 2 ms poll"}
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
@@ -91,7 +172,7 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi -lms 200"}
 
 
 def max_over_ranks(value, device=None):
@@ -494,6 +575,62 @@ def measure_prisms(op2, steps, warmup, n=256):
     return out
 
 
+def measure_data_path(op2, p, steps, warmup):
+    """Loops with (almost) no arithmetic on the benchmark mesh, to show the
+    wrapper's memory path against HBM where FP64 is not the limit: a direct
+    copy, a gather through the map, an INC scatter through the map.  Bytes
+    are compulsory ones (map read once, per-cell Dats once, vertex Dats
+    once; INC targets read and written)."""
+    import numpy as np
+    import torch
+    from pyop2_gb300.parloop import LegacyParloop
+    cells, c2v, x, y = p["cells"], p["c2v"], p["x"], p["y"]
+    C, V = cells.size, p["verts"].size
+    w = op2.Dat(cells, np.random.default_rng(3).uniform(0, 1, C))
+    out = op2.Dat(cells, np.zeros(C))
+    K = op2.Kernel
+    loops = {
+        "direct_copy": (LegacyParloop(K("static void cp(double *o, const double *w) { o[0] = w[0]; }",
+                                        "cp"), cells, out(op2.WRITE), w(op2.READ)), 16 * C),
+        "gather": (LegacyParloop(K("static void ga(double *o, const double *x) "
+                                   "{ o[0] = x[0] + x[1] + x[2] + x[3]; }", "ga"),
+                                 cells, out(op2.WRITE), x(op2.READ, c2v)), 24 * C + 8 * V),
+        "scatter_inc": (LegacyParloop(K("static void sc(double *y, const double *w) "
+                                        "{ for (int i = 0; i < 4; ++i) y[i] += w[0]; }", "sc"),
+                                      cells, y(op2.INC, c2v), w(op2.READ)), 24 * C + 16 * V),
+    }
+    peak, _ = _peaks()
+    st = torch.cuda.current_stream()
+    res = {}
+    for name, (pl, alg) in loops.items():
+        for _ in range(warmup):
+            pl.compute()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        torch.cuda.synchronize()
+        for a, b in ev:
+            a.record(st)
+            pl.compute()
+            b.record(st)
+        torch.cuda.synchronize()
+        ms = statistics.median(a.elapsed_time(b) for a, b in ev)
+        res[name] = {"ms": ms, "alg_bytes": alg, "gbs": alg / ms / 1e6,
+                     "frac_hbm": alg / ms / 1e6 / peak}
+    y.zero()
+    return res
+
+
+def _profile_number(name, key):
+    """A number recorded in a profiles/ summary as ``key: value``."""
+    import re
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        m = re.search(key + r":\s*([0-9.]+)", f.read())
+    return float(m.group(1)) if m else None
+
+
 def run_ours(args):
     import torch
     world, rank, local = _dist()
@@ -572,12 +709,20 @@ def run_ours(args):
         with open(tf) as f:
             m = re.search(r"dram_bytes_per_launch:\s*(\d+)", f.read())
         traffic = int(m.group(1)) if m else None
+    # FP64 issue roofline: the kernel's FP64 instructions per cell (ncu
+    # instruction mix, recorded in the profile) at the sampled clock
+    clocks = clk.summary()
+    fp64_ipc = _profile_number("op2g_wrap_p1_laplace_3d_128cube.md", "fp64_instructions_per_cell")
+    issue_frac = None
+    if fp64_ipc and clocks.get("sm_mhz"):
+        issue_frac = fp64_ipc * C / (per_launch_ms * 1e-3) / (304 * clocks["sm_mhz"] * 1e6)
     strategies = None
     if not args.skip_extras:
         strategies = {"lexicographic": measure_strategies(op2, p, 5, 2)}
         pr = workloads.build_p1_3d(op2, n=N_CUBE, permute=True, seed=0)
         strategies["random_permutation"] = measure_strategies(op2, pr, 5, 2)
         del pr
+    data_path = measure_data_path(op2, p, 10, 3) if not args.skip_extras else None
     sparsity = measure_sparsity_assembly(op2, p, 5, 3) if not args.skip_extras else None
     adjoint = measure_adjoint(op2, max(args.steps, 5), 3) if not args.skip_extras else None
     batch = measure_batch(op2, 5, 3) if not args.skip_extras else None
@@ -611,7 +756,11 @@ def run_ours(args):
                           "frac_of_nominal": fp64_achieved / (304 * 2 * 2.07e9 / 1e12),
                           "nominal_source": "ncu sm__sass_thread_inst_executed_op_dfma peak "
                                             "304 DFMA/clk x 2 flop x 2.07 GHz",
-                          "fp64_pipe_active_ncu": 0.887},
+                          "fp64_pipe_active_ncu": 0.887,
+                          "fp64_instr_per_cell_ncu": fp64_ipc,
+                          "issue_frac": issue_frac,
+                          "issue_peak_source": "304 FP64 instructions/clk x median SM clock "
+                                               "sampled in the timed region"},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "cells/s", "h2d_bytes_per_step": 8 * V,
                 "d2h_bytes_per_step": 8 * V},
@@ -620,8 +769,9 @@ def run_ours(args):
         "adjoint": adjoint,
         "batch": batch,
         "prisms": prisms,
+        "data_path": data_path,
         "gpu_launches": args.steps,
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "wall_s_timed": wall,
     }
     print(json.dumps(line), flush=True)

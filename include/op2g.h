@@ -100,7 +100,12 @@ enum {
 
 /* One map of the loop.  Host arrays are copied during op2g_kernel_create and
  * baked into the generated code as constants (as the reference bakes map
- * offsets as named literals, pyop2/codegen/builder.py:55-62). */
+ * offsets as named literals, pyop2/codegen/builder.py:55-62).
+ * The device array of a plain map (int32 [entities, arity], row-major, passed
+ * in the launch's pointer slots) must be 16-byte aligned when arity is a
+ * multiple of 4 and 8-byte aligned when it is even: rows are read with
+ * vector loads, and every launch checks the alignment.  It must not change
+ * while a launch runs. */
 typedef struct op2g_map_desc {
     int32_t kind;          /* OP2G_MAP_*                                                */
     int32_t arity;
@@ -141,6 +146,12 @@ typedef struct op2g_loop_desc {
     int32_t block_size;        /* threads per CTA (0 = 256)                               */
     int32_t debug_checks;      /* bounds-check every map value, report via error word     */
     int32_t batched;           /* build the persistent multi-loop variant (see _batch)    */
+    int32_t prefetch;          /* 1: each thread loads the map rows (and subset index) of
+                                  its next iteration before running the current one
+                                  (non-extruded loops; more memory-level parallelism)   */
+    int32_t nc_reads;          /* 1: READ Dat gathers use the read-only data path; the
+                                  caller guarantees that no argument of the loop writes
+                                  a Dat that a READ argument reads                      */
 } op2g_loop_desc;
 
 typedef struct op2g_kernel op2g_kernel;
@@ -182,7 +193,10 @@ typedef struct op2g_launch_desc {
     const int64_t *map_toset;  /* host array, toset size per map (bounds checks) or NULL */
     int64_t layers_per_entity; /* constant-layer extrusion: layers iterated per entity,
                                   used only to size the grid (0 = 1)                     */
-    int32_t grid;              /* CTAs (0 = derived from occupancy and the range)        */
+    int32_t grid;              /* CTAs.  0: one per block_size iterations, at most 4 x the
+                                  CTAs the GPU holds at once (threads then stride over
+                                  the rest); -1: one per block_size iterations, no cap;
+                                  > 0: exactly this many                               */
 } op2g_launch_desc;
 
 /* Launch the wrapper over [start, end) on `stream`.  Asynchronous. */

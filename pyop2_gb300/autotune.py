@@ -11,17 +11,24 @@ _CHOICES = {}
 
 
 def candidates(loop):
+    """(scatter, block size, prefetch, grid) tuples worth timing for this
+    loop: every INC strategy that applies, three CTA sizes, for non-extruded
+    loops the map-row prefetch on and off (the staging depth), and the two
+    grid policies (up to 4 resident waves, or one CTA per block of cells)."""
     it = loop.iterset
+    pfs = (0, 1) if not it._extruded else (0,)
     out = []
     for bs in (128, 256, 512):
-        out.append((_lib.SCATTER_ATOMIC, bs))
-        if loop._needs_conflict_handling():
-            if not (it._extruded and not it.constant_layers):
-                out.append((_lib.SCATTER_WARP, bs))
-            if loop._colourable():
-                from pyop2_gb300.parloop import colour_plan
-                if colour_plan(loop) is not None:
-                    out.append((_lib.SCATTER_PLAIN, bs))
+        for pf in pfs:
+            for grid in (0, -1):
+                out.append((_lib.SCATTER_ATOMIC, bs, pf, grid))
+                if loop._needs_conflict_handling():
+                    if not (it._extruded and not it.constant_layers):
+                        out.append((_lib.SCATTER_WARP, bs, pf, grid))
+                    if loop._colourable():
+                        from pyop2_gb300.parloop import colour_plan
+                        if colour_plan(loop) is not None:
+                            out.append((_lib.SCATTER_PLAIN, bs, pf, grid))
     return out
 
 
@@ -59,8 +66,8 @@ def choose(loop, reps=3):
         return cands[0]
     snaps = _snapshot(_written(loop))
     best = None
-    for sc, bs in cands:
-        loop.build(sc, bs)
+    for sc, bs, pf, grid in cands:
+        loop.build(sc, bs, pf, grid)
         loop.compute()   # warm-up (and compilation, colouring plan)
         _restore(snaps)
         ev0 = torch.cuda.Event(enable_timing=True)
@@ -75,7 +82,7 @@ def choose(loop, reps=3):
             _restore(snaps)
         t = min(times)
         if best is None or t < best[0]:
-            best = (t, (sc, bs))
+            best = (t, (sc, bs, pf, grid))
     loop._built = None
     for o, t, s in snaps:
         if hasattr(o, "_m"):

@@ -31,8 +31,13 @@ class Configuration(dict):
         "scatter": ("OP2G_SCATTER", str, "atomic"),
         # threads per CTA of generated wrappers
         "block_size": ("OP2G_BLOCK_SIZE", int, 256),
-        # let the autotuner pick scatter strategy and block size per kernel
+        # let the autotuner pick scatter strategy, block size and prefetch per kernel
         "autotune": ("OP2G_AUTOTUNE", bool, False),
+        # generated wrappers load the next iteration's map rows ahead (0 or 1)
+        "prefetch": ("OP2G_PREFETCH", int, 0),
+        # CTAs per launch: 0 = one per block of iterations up to 4 resident
+        # waves (threads stride over the rest), -1 = one per block, no cap
+        "grid": ("OP2G_GRID", int, 0),
         # CUDA device used by this process
         "device": ("OP2G_DEVICE", int, 0),
         # NVTX ranges + CUDA-event timing of named regions (profiling.summary())

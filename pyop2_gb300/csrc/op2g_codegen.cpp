@@ -181,15 +181,45 @@ struct Gen {
         return used;
     }
 
-    // Emit loading of the base row for plain map m at entity expression `ent`.
-    void emit_plain_row(int m, const std::string &ent, const std::string &ind) {
+    // Emit loading of the base row for plain map m at entity expression `ent`
+    // into `dst` (declared when `declare`).  Maps are read-only during a
+    // launch, so rows go through the non-coherent path, as 16- or 8-byte
+    // vectors when the arity allows (alignment is checked at launch).
+    void emit_plain_row(int m, const std::string &ent, const std::string &ind,
+                        std::string dst = "", bool declare = true) {
         const MapInfo &mi = S.maps[m];
-        o << ind << "int " << base_row(m) << "[" << mi.arity << "];\n";
+        if (dst.empty()) dst = base_row(m);
+        if (declare) o << ind << "int " << dst << "[" << mi.arity << "];\n";
         o << ind << "{ const int *r_ = (const int *)p.ptr[" << S.map_slot(m) << "] + (" << ent
           << ") * " << mi.arity << ";\n";
-        o << ind << "#pragma unroll\n";
-        o << ind << "  for (int i = 0; i < " << mi.arity << "; ++i) " << base_row(m)
-          << "[i] = r_[i]; }\n";
+        if (mi.arity % 4 == 0) {
+            for (int q = 0; q < mi.arity / 4; ++q)
+                o << ind << "  { const int4 v_ = __ldg((const int4 *)r_ + " << q << "); " << dst
+                  << "[" << 4 * q << "] = v_.x; " << dst << "[" << 4 * q + 1 << "] = v_.y; " << dst
+                  << "[" << 4 * q + 2 << "] = v_.z; " << dst << "[" << 4 * q + 3 << "] = v_.w; }\n";
+        } else if (mi.arity % 2 == 0) {
+            for (int q = 0; q < mi.arity / 2; ++q)
+                o << ind << "  { const int2 v_ = __ldg((const int2 *)r_ + " << q << "); " << dst
+                  << "[" << 2 * q << "] = v_.x; " << dst << "[" << 2 * q + 1 << "] = v_.y; }\n";
+        } else {
+            o << ind << "#pragma unroll\n";
+            o << ind << "  for (int i = 0; i < " << mi.arity << "; ++i) " << dst
+              << "[i] = __ldg(r_ + i);\n";
+        }
+        o << ind << "}\n";
+    }
+
+    // Plain maps whose rows an iteration loads (directly or for a permuted map).
+    std::vector<bool> row_maps() const {
+        std::vector<bool> used = used_maps();
+        std::vector<bool> need(S.maps.size(), false);
+        for (size_t m = 0; m < S.maps.size(); ++m) {
+            if (!used[m]) continue;
+            const MapInfo &mi = S.maps[m];
+            if (mi.kind == OP2G_MAP_PLAIN) need[m] = true;
+            else if (mi.kind == OP2G_MAP_PERMUTED) need[mi.base] = true;
+        }
+        return need;
     }
 
     // Emit index arrays mi<m>_<f>[arity] for map m (after base rows exist).
@@ -343,9 +373,36 @@ struct Gen {
         } else {
             O << "  const long long i0_ = start, i1_ = end;\n";
         }
+        // Prefetch (non-extruded loops): the map rows of a thread's next
+        // iteration are loaded before its current iteration runs.
+        const bool pf = S.loop.prefetch && !extr;
+        const std::vector<bool> rows = row_maps();
+        auto ent_of = [&](const std::string &itx) {
+            return S.loop.indexed ? "(long long)p.indices[" + itx + "]" : itx;
+        };
+        if (pf) {
+            O << "  const long long pit0_ = i0_ + first + threadIdx.x;\n";
+            for (size_t m = 0; m < S.maps.size(); ++m)
+                if (rows[m])
+                    O << "  int pf" << m << "[" << S.maps[m].arity << "] = {0};\n";
+            O << "  if (pit0_ < i1_) {\n    const long long pn_ = " << ent_of("pit0_") << ";\n";
+            for (size_t m = 0; m < S.maps.size(); ++m)
+                if (rows[m]) emit_plain_row((int)m, "pn_", "    ", "pf" + std::to_string(m), false);
+            O << "  }\n";
+        }
         O << "  for (long long base_ = i0_ + first; base_ < i1_; base_ += stride) {\n";
         O << "    const long long it = base_ + threadIdx.x;\n";
         O << "    const bool active = it < i1_;\n";
+        if (pf) {
+            for (size_t m = 0; m < S.maps.size(); ++m)
+                if (rows[m])
+                    O << "    int nx" << m << "[" << S.maps[m].arity << "] = {0};\n";
+            O << "    if (it + stride < i1_) {\n      const long long pn_ = "
+              << ent_of("(it + stride)") << ";\n";
+            for (size_t m = 0; m < S.maps.size(); ++m)
+                if (rows[m]) emit_plain_row((int)m, "pn_", "      ", "nx" + std::to_string(m), false);
+            O << "    }\n";
+        }
         // Pack declarations visible to the warp-aggregated unpack.
         std::string I = "    ";
         // Per-iteration declarations that warp scatter needs outside `if (active)`.
@@ -387,9 +444,15 @@ struct Gen {
             O << J << "}\n";
         } else {
             O << J << "const long long n = " << (S.loop.indexed ? "p.indices[it]" : "it") << ";\n";
-            emit_body(J, warp, plain);
+            emit_body(J, warp, plain, pf);
         }
         O << I << "}\n";
+        if (pf) {
+            for (size_t m = 0; m < S.maps.size(); ++m)
+                if (rows[m])
+                    O << I << "#pragma unroll\n" << I << "for (int i = 0; i < " << S.maps[m].arity
+                      << "; ++i) pf" << m << "[i] = nx" << m << "[i];\n";
+        }
         if (warp) {
             for (size_t a = 0; a < S.args.size(); ++a) {
                 const ArgInfo &A = S.args[a];
@@ -467,19 +530,20 @@ struct Gen {
     }
 
     // Pack, call, unpack for one iteration (entity n, and layer when extruded).
-    void emit_body(const std::string &J, bool warp, bool plain) {
+    void emit_body(const std::string &J, bool warp, bool plain, bool rows_prefetched = false) {
         std::ostringstream &O = o;
         std::vector<bool> used = used_maps();
-        // expand used to the plain maps that supply rows
-        std::vector<bool> need_row(S.maps.size(), false);
+        std::vector<bool> need_row = row_maps();
         for (size_t m = 0; m < S.maps.size(); ++m) {
-            if (!used[m]) continue;
-            const MapInfo &mi = S.maps[m];
-            if (mi.kind == OP2G_MAP_PLAIN) need_row[m] = true;
-            else if (mi.kind == OP2G_MAP_PERMUTED) need_row[mi.base] = true;
+            if (!need_row[m]) continue;
+            if (rows_prefetched) {
+                O << J << "int " << base_row((int)m) << "[" << S.maps[m].arity << "];\n";
+                O << J << "#pragma unroll\n" << J << "for (int i = 0; i < " << S.maps[m].arity
+                  << "; ++i) " << base_row((int)m) << "[i] = pf" << m << "[i];\n";
+            } else {
+                emit_plain_row((int)m, "n", J);
+            }
         }
-        for (size_t m = 0; m < S.maps.size(); ++m)
-            if (need_row[m]) emit_plain_row((int)m, "n", J);
         for (size_t m = 0; m < S.maps.size(); ++m)
             if (used[m]) emit_index_arrays((int)m, J);
 
@@ -535,9 +599,11 @@ struct Gen {
                         O << J << "  for (int i = 0; i < " << ar << "; ++i) {\n";
                         O << J << "    const int x_ = " << idx_arr(A.d.map, f) << "[i];\n";
                         O << J << "#pragma unroll\n";
+                        const bool nc = S.loop.nc_reads && A.d.access == OP2G_READ;
                         O << J << "    for (int j = 0; j < " << D << "; ++j) " << tn << "[" << po
-                          << "(" << f * ar << " + i) * " << D << " + j] = x_ >= 0 ? d_[(long long)x_ * "
-                          << D << " + j] : (" << T << ")0;\n";
+                          << "(" << f * ar << " + i) * " << D << " + j] = x_ >= 0 ? "
+                          << (nc ? "__ldg(&" : "") << "d_[(long long)x_ * " << D << " + j]"
+                          << (nc ? ")" : "") << " : (" << T << ")0;\n";
                         O << J << "  }\n";
                     }
                     O << J << "}\n";

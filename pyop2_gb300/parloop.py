@@ -344,8 +344,19 @@ class Parloop:
             argdescs.append(d + (group, gcols))
         return table, argdescs
 
-    def _loop_desc(self, scatter, block_size):
+    def _nc_reads(self):
+        """True when no Dat read by a READ argument is written by another
+        argument of this loop (READ gathers may then use the read-only path)."""
+        read, written = set(), set()
+        for a in self._components:
+            if isinstance(a, DatLegacyArg):
+                (read if a.access is Access.READ else written).add(id(a.data))
+        return not (read & written)
+
+    def _loop_desc(self, scatter, block_size, prefetch=None):
         it = self.iterset
+        if prefetch is None:
+            prefetch = int(configuration["prefetch"])
         return dict(extruded=int(it._extruded),
                     constant_layers=int(bool(it._extruded and it.constant_layers)),
                     extruded_periodic=int(bool(it._extruded_periodic)),
@@ -353,7 +364,9 @@ class Parloop:
                     iteration_region=int(self.iteration_region),
                     pass_layer_arg=int(self.pass_layer_arg),
                     scatter=scatter, block_size=block_size,
-                    debug_checks=int(bool(configuration["debug"])), batched=0)
+                    debug_checks=int(bool(configuration["debug"])), batched=0,
+                    prefetch=int(bool(prefetch) and not it._extruded),
+                    nc_reads=int(self._nc_reads()))
 
     def _needs_conflict_handling(self):
         return any(isinstance(a, (DatLegacyArg, MatLegacyArg)) and
@@ -361,21 +374,25 @@ class Parloop:
                    a.access in (Access.INC, Access.MIN, Access.MAX) for a in self._components)
 
     def _choose_strategy(self):
+        """(scatter, block size, prefetch) from the configuration, or from
+        the autotuner's measurements."""
         mode = configuration["scatter"]
         bs = int(configuration["block_size"])
+        pf = int(configuration["prefetch"])
+        grid = int(configuration["grid"])
         if mode == "auto" or configuration["autotune"]:
             from pyop2_gb300 import autotune
             return autotune.choose(self)
         if not self._needs_conflict_handling():
-            return _lib.SCATTER_ATOMIC, bs
+            return _lib.SCATTER_ATOMIC, bs, pf, grid
         if mode == "warp":
             it = self.iterset
             if it._extruded and not it.constant_layers:
-                return _lib.SCATTER_ATOMIC, bs
-            return _lib.SCATTER_WARP, bs
+                return _lib.SCATTER_ATOMIC, bs, pf, grid
+            return _lib.SCATTER_WARP, bs, pf, grid
         if mode == "colour" and self._colourable() and colour_plan(self) is not None:
-            return _lib.SCATTER_PLAIN, bs
-        return _lib.SCATTER_ATOMIC, bs
+            return _lib.SCATTER_PLAIN, bs, pf, grid
+        return _lib.SCATTER_ATOMIC, bs, pf, grid
 
     def _colourable(self):
         if self.iterset._extruded or isinstance(self.iterset, Subset):
@@ -396,12 +413,16 @@ class Parloop:
         return signature_key(self.local_kernel.source, self.local_kernel.name,
                              self._loop_desc(scatter, block_size), argdescs, table.key())
 
-    def build(self, scatter=None, block_size=None):
-        """Compile the wrapper for this loop (idempotent per strategy)."""
+    def build(self, scatter=None, block_size=None, prefetch=None, grid=None):
+        """Compile the wrapper for this loop (idempotent per strategy).
+        ``grid`` is the launch's CTA policy (``op2g_launch_desc.grid``)."""
         if scatter is None:
-            scatter, block_size = self._choose_strategy()
+            scatter, block_size, prefetch, grid = self._choose_strategy()
+        if block_size is None:
+            block_size = int(configuration["block_size"])
+        self._grid = int(configuration["grid"]) if grid is None else int(grid)
         table, argdescs = self._signature()
-        loop = self._loop_desc(scatter, block_size)
+        loop = self._loop_desc(scatter, block_size, prefetch)
         k = compile_signature(self.local_kernel.source, self.local_kernel.name, loop, argdescs,
                               table.key())
         device.require()
@@ -485,7 +506,7 @@ class Parloop:
         D.ptrs = P
         D.map_toset = toset
         D.layers_per_entity = self._layers_per_entity()
-        D.grid = 0
+        D.grid = getattr(self, "_grid", 0)
         D.indices = it._indices_mirror.dev().data_ptr() if isinstance(it, Subset) else None
         D.start, D.end = 0, it.size
         self._keep = (P, toset)

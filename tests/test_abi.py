@@ -45,7 +45,8 @@ STRUCTS = {
                                   "group", "group_cols"]),
     "op2g_loop_desc": ("LoopDesc", ["extruded", "constant_layers", "extruded_periodic", "indexed",
                                     "iteration_region", "pass_layer_arg", "scatter",
-                                    "block_size", "debug_checks", "batched"]),
+                                    "block_size", "debug_checks", "batched", "prefetch",
+                                    "nc_reads"]),
     "op2g_launch_desc": ("LaunchDesc", ["start", "end", "layers", "indices", "err", "ptrs",
                                         "map_toset", "layers_per_entity", "grid"]),
     "op2g_sparsity_pair": ("SparsityPair", ["rmap", "cmap", "rarity", "carity", "nent", "region",
