@@ -344,13 +344,13 @@ def e2e_pipelined(op2, p, loop0, steps, barrier):
 
 def measure_strategies(op2, p, steps, warmup):
     """The benchmark action under each INC conflict strategy (hardware
-    atomics, warp-aggregated atomics, greedy colouring), for the given
-    problem's numbering."""
+    atomics, warp-aggregated atomics, greedy colouring, per-CTA shared-memory
+    staging), for the given problem's numbering."""
     from pyop2_gb300.configuration import configuration
     out = {}
     old = configuration["scatter"]
     try:
-        for sc in ("atomic", "warp", "colour"):
+        for sc in ("atomic", "warp", "colour", "shared"):
             configuration["scatter"] = sc
             lp = op2.ParLoop(p["kernel"], p["cells"], p["y"](op2.INC, p["c2v"]),
                              p["X"](op2.READ, p["c2v"]), p["x"](op2.READ, p["c2v"]))
@@ -599,6 +599,23 @@ def measure_data_path(op2, p, steps, warmup):
                                         "{ for (int i = 0; i < 4; ++i) y[i] += w[0]; }", "sc"),
                                       cells, y(op2.INC, c2v), w(op2.READ)), 24 * C + 16 * V),
     }
+    from pyop2_gb300 import _lib
+    for sc, nm in ((_lib.SCATTER_WARP, "scatter_inc_warp"), (_lib.SCATTER_SHARED, "scatter_inc_shared")):
+        pl = LegacyParloop(K("static void sc(double *y, const double *w) "
+                             "{ for (int i = 0; i < 4; ++i) y[i] += w[0]; }", "sc"),
+                           cells, y(op2.INC, c2v), w(op2.READ))
+        pl.build(sc)
+        loops[nm] = (pl, 24 * C + 16 * V)
+    # contention extreme: every cell INCs one of 16 targets
+    hot_set = op2.Set(16)
+    hot = op2.Map(cells, hot_set, 1, (np.arange(C) % 16).astype(np.int32))
+    yh = op2.Dat(hot_set, np.zeros(16))
+    for sc, nm in ((_lib.SCATTER_ATOMIC, "hot16_atomic"), (_lib.SCATTER_WARP, "hot16_warp"),
+                   (_lib.SCATTER_SHARED, "hot16_shared")):
+        pl = LegacyParloop(K("static void hs(double *y, const double *w) { y[0] += w[0]; }",
+                             "hs"), cells, yh(op2.INC, hot), w(op2.READ))
+        pl.build(sc)
+        loops[nm] = (pl, 12 * C)
     peak, _ = _peaks()
     st = torch.cuda.current_stream()
     res = {}

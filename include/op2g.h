@@ -90,8 +90,12 @@ enum {
     OP2G_SCATTER_ATOMIC = 0,   /* one hardware atomic (RED) per contribution          */
     OP2G_SCATTER_WARP = 1,     /* __match_any_sync groups lanes on one target, one
                                   shuffle-reduced atomic per group                    */
-    OP2G_SCATTER_PLAIN = 2     /* plain read-modify-write: only legal when the caller
+    OP2G_SCATTER_PLAIN = 2,    /* plain read-modify-write: only legal when the caller
                                   launches one colour (conflict-free cell set) at a time */
+    OP2G_SCATTER_SHARED = 3    /* each CTA sums its INC contributions per target in a
+                                  shared-memory hash table, then adds each distinct
+                                  target once with a global atomic (non-extruded loops;
+                                  atomics elsewhere)                                    */
 };
 
 #define OP2G_MAX_ARGS 32

@@ -21,7 +21,7 @@ F64, F32, I32, U32, I64, U64, I16, U16, I8, U8 = range(10)
 ABI_VERSION = 2
 ARG_DAT, ARG_GLOBAL, ARG_MAT, ARG_PASSTHROUGH = range(4)
 MAP_PLAIN, MAP_PERMUTED, MAP_COMPOSED = range(3)
-SCATTER_ATOMIC, SCATTER_WARP, SCATTER_PLAIN = range(3)
+SCATTER_ATOMIC, SCATTER_WARP, SCATTER_PLAIN, SCATTER_SHARED = range(4)
 MAX_ARGS = 32
 MAX_MAPS = 32
 MAX_COMPOSED = 8

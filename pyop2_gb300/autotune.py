@@ -12,7 +12,8 @@ _CHOICES = {}
 
 def candidates(loop):
     """(scatter, block size, prefetch, grid) tuples worth timing for this
-    loop: every INC strategy that applies, three CTA sizes, for non-extruded
+    loop: every INC strategy that applies (atomics, warp aggregation,
+    shared-memory staging, colouring), three CTA sizes, for non-extruded
     loops the map-row prefetch on and off (the staging depth), and the two
     grid policies (up to 4 resident waves, or one CTA per block of cells)."""
     it = loop.iterset
@@ -25,6 +26,8 @@ def candidates(loop):
                 if loop._needs_conflict_handling():
                     if not (it._extruded and not it.constant_layers):
                         out.append((_lib.SCATTER_WARP, bs, pf, grid))
+                    if not it._extruded:
+                        out.append((_lib.SCATTER_SHARED, bs, pf, grid))
                     if loop._colourable():
                         from pyop2_gb300.parloop import colour_plan
                         if colour_plan(loop) is not None:

@@ -27,7 +27,8 @@ class Configuration(dict):
         "matnest": ("PYOP2_MATNEST", bool, True),
         "compute_kernel_flops": ("PYOP2_COMPUTE_KERNEL_FLOPS", bool, False),
         "print_cache_info": ("PYOP2_CACHE_INFO", bool, False),
-        # INC conflict resolution: "atomic", "warp", "colour" or "auto" (autotuner)
+        # INC conflict resolution: "atomic", "warp", "colour", "shared" (per-CTA
+        # shared-memory sums, one atomic per distinct target) or "auto" (autotuner)
         "scatter": ("OP2G_SCATTER", str, "atomic"),
         # threads per CTA of generated wrappers
         "block_size": ("OP2G_BLOCK_SIZE", int, 256),
@@ -82,8 +83,8 @@ class Configuration(dict):
                 value = int(value)
             except (TypeError, ValueError):
                 raise ConfigurationError("Option %r needs an int" % key)
-        if key == "scatter" and value not in ("atomic", "warp", "colour", "auto"):
-            raise ConfigurationError("scatter must be atomic, warp, colour or auto")
+        if key == "scatter" and value not in ("atomic", "warp", "colour", "shared", "auto"):
+            raise ConfigurationError("scatter must be atomic, warp, colour, shared or auto")
         super().__setitem__(key, value)
 
 

@@ -101,6 +101,35 @@ struct Gen {
         return nf * S.maps[d.cmap].arity * d.cdim;
     }
 
+    // Shared-memory staging of INC contributions (OP2G_SCATTER_SHARED):
+    // per INC-through-a-map argument, a table of 2 x (contributions per CTA)
+    // slots rounded to a power of two, shrunk to fit 40 KB of static shared
+    // memory in total; an argument that does not fit keeps global atomics.
+    std::vector<int> shared_ts;
+    bool any_shared = false;
+
+    void plan_shared(bool on) {
+        shared_ts.assign(S.args.size(), 0);
+        any_shared = false;
+        if (!on) return;
+        size_t budget = 40 * 1024;
+        for (size_t a = 0; a < S.args.size(); ++a) {
+            const op2g_arg_desc &d = S.args[a].d;
+            if (d.kind != OP2G_ARG_DAT || d.map < 0 || d.access != OP2G_INC) continue;
+            if (!atomic_capable(d.dtype)) continue;
+            const int contrib = S.block_size * nf * S.maps[d.map].arity;
+            int ts = 1;
+            while (ts < 2 * contrib) ts <<= 1;
+            const size_t elt = d.dtype == OP2G_F64 || d.dtype == OP2G_I64 || d.dtype == OP2G_U64 ? 8 : 4;
+            auto bytes = [&](int t) { return (size_t)t * (8 + elt * d.dim) + 8; };
+            while (ts > contrib && bytes(ts) > budget) ts >>= 1;
+            if (ts < contrib || bytes(ts) > budget) continue;
+            shared_ts[a] = ts;
+            budget -= bytes(ts);
+            any_shared = true;
+        }
+    }
+
     void layout() {
         const size_t n = S.args.size();
         first.assign(n, 0);
@@ -341,6 +370,7 @@ struct Gen {
         const bool varlay = extr && (!S.loop.constant_layers || plain || direct_written);
         if (varlay) warp = false;  // lanes of a warp run different layer counts
         if (has_groups) warp = false;  // grouped packs scatter by atomics
+        plan_shared(!extr && S.loop.scatter == OP2G_SCATTER_SHARED);
 
         // ----- the run function: a strided sweep of [start, end) plus reductions
         O << "__device__ __forceinline__ void op2g_run(const op2g_params_t &p, long long start, "
@@ -389,6 +419,30 @@ struct Gen {
             for (size_t m = 0; m < S.maps.size(); ++m)
                 if (rows[m]) emit_plain_row((int)m, "pn_", "    ", "pf" + std::to_string(m), false);
             O << "  }\n";
+        }
+        for (size_t a = 0; a < S.args.size(); ++a)
+            if (shared_ts[a]) {
+                // keys, sums, the list of claimed slots and its length (two
+                // counters used by alternate sweep steps)
+                O << "  __shared__ int sk" << a << "[" << shared_ts[a] << "];\n";
+                O << "  __shared__ " << ctype_of(S.args[a].d.dtype) << " sv" << a << "["
+                  << shared_ts[a] * S.args[a].d.dim << "];\n";
+                O << "  __shared__ int sl" << a << "[" << shared_ts[a] << "];\n";
+                O << "  __shared__ int sn" << a << "[2];\n";
+            }
+        if (any_shared) O << "  int par_ = 0;\n";
+        if (any_shared) {
+            // tables start empty; each sweep step's flush empties them again
+            for (size_t a = 0; a < S.args.size(); ++a)
+                if (shared_ts[a]) {
+                    const int D = S.args[a].d.dim;
+                    O << "  for (int s_ = threadIdx.x; s_ < " << shared_ts[a] << "; s_ += " << BS
+                      << ") { sk" << a << "[s_] = -1;";
+                    O << " for (int j = 0; j < " << D << "; ++j) sv" << a << "[s_ * " << D
+                      << " + j] = (" << ctype_of(S.args[a].d.dtype) << ")0; }\n";
+                    O << "  if (threadIdx.x == 0) { sn" << a << "[0] = 0; sn" << a << "[1] = 0; }\n";
+                }
+            O << "  __syncthreads();\n";
         }
         O << "  for (long long base_ = i0_ + first; base_ < i1_; base_ += stride) {\n";
         O << "    const long long it = base_ + threadIdx.x;\n";
@@ -472,6 +526,27 @@ struct Gen {
                     O << I << "  } }\n";
                 }
             }
+        }
+        if (any_shared) {
+            // The sweep step is uniform across the CTA (base_ depends on the
+            // block only), so these barriers are reached by every thread.
+            O << "    __syncthreads();\n";
+            for (size_t a = 0; a < S.args.size(); ++a)
+                if (shared_ts[a]) {
+                    const int D = S.args[a].d.dim;
+                    const char *T = ctype_of(S.args[a].d.dtype);
+                    O << "    { " << T << " *d_ = (" << T << " *)p.ptr[" << S.args[a].slot << "];\n";
+                    O << "      const int n_ = sn" << a << "[par_];\n";
+                    O << "      if (threadIdx.x == 0) sn" << a << "[par_ ^ 1] = 0;\n";
+                    O << "      for (int s_ = threadIdx.x; s_ < n_; s_ += " << BS
+                      << ") { const int h_ = sl" << a << "[s_]; const int k_ = sk" << a
+                      << "[h_]; sk" << a << "[h_] = -1;\n";
+                    O << "        for (int j = 0; j < " << D << "; ++j) { op2g::atomic_inc(&d_[(long long)k_ * "
+                      << D << " + j], sv" << a << "[h_ * " << D << " + j]); sv" << a << "[h_ * " << D
+                      << " + j] = (" << T << ")0; } } }\n";
+                }
+            O << "    __syncthreads();\n";
+            O << "    par_ ^= 1;\n";
         }
         O << "  }\n";  // sweep loop
         // Global reductions (pyop2/parloop.py:409-452 semantics on one device:
@@ -655,6 +730,21 @@ struct Gen {
                     O << J << "  for (int i = 0; i < " << ar << "; ++i) {\n";
                     O << J << "    const int x_ = " << idx_arr(A.d.map, f) << "[i];\n";
                     O << J << "    if (x_ < 0) continue;\n";
+                    if (shared_ts[a]) {
+                        // find or claim x_'s slot (bounded linear probing;
+                        // a full table sends the contribution to global memory)
+                        const int TS = shared_ts[a];
+                        O << J << "    int h_ = (int)(((unsigned)x_ * 2654435761u) & " << TS - 1
+                          << "u);\n";
+                        O << J << "    for (int q_ = 0; ; ++q_) {\n";
+                        O << J << "      if (q_ == " << TS << ") { h_ = -1; break; }\n";
+                        O << J << "      const int o_ = atomicCAS(&sk" << a << "[h_], -1, x_);\n";
+                        O << J << "      if (o_ == -1) { sl" << a << "[atomicAdd(&sn" << a
+                          << "[par_], 1)] = h_; break; }\n";
+                        O << J << "      if (o_ == x_) break;\n";
+                        O << J << "      h_ = (h_ + 1) & " << TS - 1 << ";\n";
+                        O << J << "    }\n";
+                    }
                     O << J << "#pragma unroll\n";
                     O << J << "    for (int j = 0; j < " << D << "; ++j) {\n";
                     std::string dst = "d_[(long long)x_ * " + std::to_string(D) + " + j]";
@@ -664,6 +754,10 @@ struct Gen {
                     switch (A.d.access) {
                         case OP2G_INC:
                             if (plain) O << J << "      " << dst << " += " << src << ";\n";
+                            else if (shared_ts[a])
+                                O << J << "      if (h_ >= 0) op2g::atomic_inc(&sv" << a << "[h_ * "
+                                  << D << " + j], " << src << "); else op2g::atomic_inc(&" << dst
+                                  << ", " << src << ");\n";
                             else O << J << "      op2g::atomic_inc(&" << dst << ", " << src << ");\n";
                             break;
                         case OP2G_MIN:
@@ -825,6 +919,8 @@ std::string validate_signature(const Signature &S) {
         a = b;
     }
     if (S.loop.pass_layer_arg && !S.loop.extruded) return "layer argument needs an extruded loop";
+    if (S.loop.scatter < OP2G_SCATTER_ATOMIC || S.loop.scatter > OP2G_SCATTER_SHARED)
+        return "unknown scatter strategy";
     return "";
 }
 

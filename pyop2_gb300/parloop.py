@@ -392,6 +392,8 @@ class Parloop:
             return _lib.SCATTER_WARP, bs, pf, grid
         if mode == "colour" and self._colourable() and colour_plan(self) is not None:
             return _lib.SCATTER_PLAIN, bs, pf, grid
+        if mode == "shared" and not self.iterset._extruded:
+            return _lib.SCATTER_SHARED, bs, pf, grid
         return _lib.SCATTER_ATOMIC, bs, pf, grid
 
     def _colourable(self):

@@ -8,7 +8,7 @@ from pyop2_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
 
-STRATEGIES = ["atomic", "warp", "colour"]
+STRATEGIES = ["atomic", "warp", "colour", "shared"]
 
 
 @pytest.fixture(params=STRATEGIES)

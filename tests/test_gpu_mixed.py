@@ -7,7 +7,7 @@ import scenarios as S
 
 pytestmark = pytest.mark.gpu
 
-STRATEGIES = ["atomic", "warp", "colour"]
+STRATEGIES = ["atomic", "warp", "colour", "shared"]
 
 
 @pytest.fixture(params=STRATEGIES)
