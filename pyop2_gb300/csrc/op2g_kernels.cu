@@ -88,18 +88,18 @@ __device__ __forceinline__ int ext_term(int layer, int k, int q, int nl) {
     return nl > 0 ? (eff % nl - q % nl) : (eff - q);
 }
 
-__device__ __forceinline__ int row_of(const SpDev &S, const PairDev &P, long long rent, int i,
-                                      int layer, int nl) {
-    const int k = i / P.rarity, ir = i - k * P.rarity;
-    int b = P.rmap[rent * P.rarity + ir];
+// Row (column) of local entry ir (jr) of facet k of a virtual cell: the
+// map value plus the extruded offset term.
+__device__ __forceinline__ int row_of(const SpDev &S, const PairDev &P, long long rent, int k,
+                                      int ir, int layer, int nl) {
+    int b = __ldg(P.rmap + rent * P.rarity + ir);
     if (S.extruded && P.has_roff) b += P.roff[ir] * ext_term(layer, k, P.rq[ir], nl);
     return b;
 }
 
-__device__ __forceinline__ int col_of(const SpDev &S, const PairDev &P, long long cent, int j,
-                                      int layer, int nl) {
-    const int k = j / P.carity, jr = j - k * P.carity;
-    int b = P.cmap[cent * P.carity + jr];
+__device__ __forceinline__ int col_of(const SpDev &S, const PairDev &P, long long cent, int k,
+                                      int jr, int layer, int nl) {
+    int b = __ldg(P.cmap + cent * P.carity + jr);
     if (S.extruded && P.has_coff) b += P.coff[jr] * ext_term(layer, k, P.cq[jr], nl);
     return b;
 }
@@ -114,8 +114,10 @@ __global__ void k_incidence(SpDev S, const PairDev *__restrict__ pairs, int p, i
         long long rent, cent;
         int layer, nl;
         if (!vcell(S, P, v, rent, cent, layer, nl)) continue;
+        const int ra = P.rarity, nfr = P.tr / ra;
         for (int i = 0; i < P.tr; ++i) {
-            const int r = row_of(S, P, rent, i, layer, nl);
+            const int k = nfr == 1 ? 0 : (i >= ra);
+            const int r = row_of(S, P, rent, k, i - k * ra, layer, nl);
             if (r < 0) continue;
             if (r >= S.nrows) {
                 atomicOr(S.err, OP2G_DEVERR_MAP_BOUNDS);
@@ -155,12 +157,14 @@ __device__ __forceinline__ unsigned col_hash(int c, unsigned mask) {
 }
 
 __device__ __forceinline__ void row_insert(int c, int *tab, unsigned mask, int tsize, int *uniq,
-                                           int *ucount, int *err) {
+                                           int *uslot, int *ucount, int *err) {
     unsigned h = col_hash(c, mask);
     for (int probe = 0; probe < tsize; ++probe) {
         const int old = atomicCAS(&tab[h], -1, c);
         if (old == -1) {
-            uniq[atomicAdd(ucount, 1)] = c;
+            const int k = atomicAdd(ucount, 1);
+            uniq[k] = c;
+            uslot[k] = (int)h;
             return;
         }
         if (old == c) return;
@@ -176,13 +180,16 @@ __global__ void k_rows(SpDev S, const PairDev *__restrict__ pairs,
     extern __shared__ int smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
-    int *hdr = smem + warp * (ROW_HDR + tsize + ucap);
+    int *hdr = smem + warp * (ROW_HDR + tsize + 2 * ucap);
     int *tab = hdr + ROW_HDR;
     int *uniq = tab + tsize;
+    int *uslot = uniq + ucap;     // table slot claimed by each distinct column
     const unsigned mask = (unsigned)tsize - 1u;
+    // the table is emptied once here and afterwards only at the slots a row
+    // claimed (~15 of tsize)
+    for (int i = lane; i < tsize; i += 32) tab[i] = -1;
     for (long long r = (long long)blockIdx.x * wpb + warp; r < S.nrows;
          r += (long long)gridDim.x * wpb) {
-        for (int i = lane; i < tsize; i += 32) tab[i] = -1;
         if (lane == 0) hdr[0] = 0;
         __syncwarp();
         const long long e0 = tptr[r], e1 = tptr[r + 1];
@@ -192,26 +199,28 @@ __global__ void k_rows(SpDev S, const PairDev *__restrict__ pairs,
             long long rent, cent;
             int layer, nl;
             if (!vcell(S, P, code & ((1ll << 56) - 1), rent, cent, layer, nl)) continue;
+            const int ca = P.carity, nfc = P.tc / ca;
             for (int j = 0; j < P.tc; ++j) {
-                const int c = col_of(S, P, cent, j, layer, nl);
+                const int k = nfc == 1 ? 0 : (j >= ca);
+                const int c = col_of(S, P, cent, k, j - k * ca, layer, nl);
                 if (c < 0) continue;
                 if (c >= S.ncols) {
                     atomicOr(S.err, OP2G_DEVERR_MAP_BOUNDS);
                     continue;
                 }
-                row_insert(c, tab, mask, tsize, uniq, hdr, S.err);
+                row_insert(c, tab, mask, tsize, uniq, uslot, hdr, S.err);
             }
         }
         if (S.set_diag && r < S.ncols && lane == 0)
-            row_insert((int)r, tab, mask, tsize, uniq, hdr, S.err);
+            row_insert((int)r, tab, mask, tsize, uniq, uslot, hdr, S.err);
         __syncwarp();
         const int u = hdr[0];
         int *out = tmp + candptr[r];
         if (u <= 32) {
+            // rank sort over the u distinct columns (u is warp-uniform)
             const int x = lane < u ? uniq[lane] : INT_MAX;
             int rank = 0;
-#pragma unroll
-            for (int j = 0; j < 32; ++j) rank += __shfl_sync(0xffffffffu, x, j) < x;
+            for (int j = 0; j < u; ++j) rank += __shfl_sync(0xffffffffu, x, j) < x;
             if (lane < u) out[rank] = x;
         } else {
             int P2 = 1;
@@ -235,6 +244,7 @@ __global__ void k_rows(SpDev S, const PairDev *__restrict__ pairs,
             for (int i = lane; i < u; i += 32) out[i] = uniq[i];
         }
         if (lane == 0) rowcount[r] = u;
+        for (int i = lane; i < u; i += 32) tab[uslot[i]] = -1;
         __syncwarp();
     }
 }
@@ -434,7 +444,7 @@ op2g_status sp_rows_launch(const SpDev &S, const PairDev *pd, const long long *t
     while (tsize < 2 * max_cand) tsize <<= 1;
     int ucap = 32;
     while (ucap < max_cand) ucap <<= 1;
-    const size_t per = (size_t)(ROW_HDR + tsize + ucap) * sizeof(int);
+    const size_t per = (size_t)(ROW_HDR + tsize + 2 * ucap) * sizeof(int);
     int wpb = (int)((48 * 1024) / per);
     if (wpb > 8) wpb = 8;
     if (wpb < 1) wpb = 1;
