@@ -109,9 +109,18 @@ class BatchedParLoop:
             lp.mark_written()
 
 
-def autotune_batch(loops, chunks=(512, 2048, 8192), block_sizes=(128, 256), reps=3):
-    """Pick the (chunk, block size) of a batch by timing graph replays on the
-    loops' own data; the written arguments are restored after each trial."""
+def autotune_batch(loops, chunks=(512, 2048, 8192), block_sizes=(128, 256), reps=3,
+                   scatters=None):
+    """Pick the (chunk, block size, INC strategy) of a batch by timing graph
+    replays on the loops' own data; the written arguments are restored after
+    each trial.  Strategies: hardware atomics, warp aggregation and
+    shared-memory staging (colouring cannot run in one launch)."""
+    if scatters is None:
+        scatters = (_lib.SCATTER_ATOMIC,)
+        if loops[0]._needs_conflict_handling():
+            scatters = (_lib.SCATTER_ATOMIC, _lib.SCATTER_WARP)
+            if not loops[0].iterset._extruded:
+                scatters += (_lib.SCATTER_SHARED,)
     from pyop2_gb300.autotune import _restore, _snapshot, _written
     objs = []
     seen = set()
@@ -122,23 +131,26 @@ def autotune_batch(loops, chunks=(512, 2048, 8192), block_sizes=(128, 256), reps
                 objs.append(o)
     snaps = _snapshot(objs)
     best = None
-    for bs in block_sizes:
-        for ch in chunks:
-            b = BatchedParLoop(loops, chunk=ch, block_size=bs)
-            b.capture()
-            b.replay()
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for _ in range(reps):
-                b._graph.replay()
-            e1.record()
-            e1.synchronize()
-            t = e0.elapsed_time(e1) / reps
-            _restore(snaps)
-            if best is None or t < best[0]:
-                best = (t, ch, bs, b)
+    trials = [(bs, ch, sc) for sc in scatters for bs in block_sizes for ch in chunks]
+    for bs, ch, sc in trials:
+        b = BatchedParLoop(loops, chunk=ch, block_size=bs, scatter=sc)
+        b.capture()
+        b.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            b._graph.replay()
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / reps
+        _restore(snaps)
+        if best is None or t < best[0]:
+            best = (t, ch, bs, b, sc)
     for o, t, s in snaps:
         if hasattr(o, "_m"):
             o._m.state = "device"
-    return best[3], {"chunk": best[1], "block_size": best[2], "ms": best[0]}
+    names = {_lib.SCATTER_ATOMIC: "atomic", _lib.SCATTER_WARP: "warp",
+             _lib.SCATTER_SHARED: "shared"}
+    return best[3], {"chunk": best[1], "block_size": best[2], "scatter": names[best[4]],
+                     "ms": best[0]}
