@@ -10,6 +10,7 @@
 // iterates one colour at a time.
 #include "op2g_internal.h"
 
+#include <cctype>
 #include <sstream>
 
 namespace op2g {
@@ -65,6 +66,30 @@ static std::string strip_system_includes(const std::string &src) {
             << "\n";
     }
     return out.str();
+}
+
+// True when the user kernel is declared with an empty parameter list,
+// `name()` or `name(void)`.  In C (the reference compiles kernels as C) an
+// empty list leaves the parameters unspecified, so the wrapper may pass the
+// packs anyway; in CUDA C++ it means "no parameters", so the call is then
+// made without arguments.
+static bool declared_without_parameters(const std::string &src, const std::string &name) {
+    auto is_ident = [](char c) { return std::isalnum((unsigned char)c) || c == '_'; };
+    for (size_t p = src.find(name); p != std::string::npos; p = src.find(name, p + 1)) {
+        if (p > 0 && is_ident(src[p - 1])) continue;
+        size_t q = p + name.size();
+        if (q < src.size() && is_ident(src[q])) continue;
+        while (q < src.size() && std::isspace((unsigned char)src[q])) ++q;
+        if (q >= src.size() || src[q] != '(') continue;
+        ++q;
+        while (q < src.size() && std::isspace((unsigned char)src[q])) ++q;
+        if (src.compare(q, 4, "void") == 0 && (q + 4 >= src.size() || !is_ident(src[q + 4]))) {
+            q += 4;
+            while (q < src.size() && std::isspace((unsigned char)src[q])) ++q;
+        }
+        if (q < src.size() && src[q] == ')') return true;
+    }
+    return false;
 }
 
 // ---------------------------------------------------------------------------
@@ -695,6 +720,7 @@ struct Gen {
             }
         }
         if (S.loop.pass_layer_arg) kargs.push_back("layer");
+        if (declared_without_parameters(S.user_src, S.kernel_name)) kargs.clear();
         // Call (pyop2/codegen/builder.py:964-977)
         O << J << S.kernel_name << "(";
         for (size_t i = 0; i < kargs.size(); ++i) O << (i ? ", " : "") << kargs[i];

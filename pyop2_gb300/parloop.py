@@ -312,6 +312,12 @@ class Parloop:
                 flat.append((a, 0, 0))
         self._flat = flat
         self._components = [c for c, _, _ in flat]
+        # pyop2/parloop.py:501-511
+        for a in self._components:
+            if isinstance(a, DatLegacyArg) and a.data._halo_frozen and \
+                    a.data._frozen_access_mode != a.access:
+                raise RuntimeError("Dats with frozen halos must always be accessed with the "
+                                   "same access mode")
 
     @property
     def accesses(self):

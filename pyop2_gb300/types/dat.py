@@ -381,6 +381,29 @@ class Dat(AbstractDat):
     def __repr__(self):
         return "Dat(%r, None, %r, %r)" % (self._dataset, self.dtype, self._name)
 
+    # ---- halo freezing (pyop2/types/dat.py:634-665, 1154-1175).  A single
+    # device has no halo exchanges to skip, but the bookkeeping is kept: a Dat
+    # frozen for one access mode may only be used with that mode.
+    _halo_frozen = False
+    _frozen_access_mode = None
+
+    def freeze_halo(self, access_mode):
+        if self._halo_frozen:
+            raise RuntimeError("Expected an unfrozen halo")
+        self._halo_frozen = True
+        self._frozen_access_mode = access_mode
+
+    def unfreeze_halo(self):
+        if not self._halo_frozen:
+            raise RuntimeError("Expected a frozen halo")
+        self._halo_frozen = False
+        self._frozen_access_mode = None
+
+    def frozen_halo(self, access_mode):
+        """Context manager: halo exchanges off, accesses restricted to
+        ``access_mode`` while it is active."""
+        return _FrozenHalo(self, access_mode)
+
     # halo operations are no-ops on one device (no MPI halos)
     def global_to_local_begin(self, access_mode):
         pass
@@ -393,6 +416,24 @@ class Dat(AbstractDat):
 
     def local_to_global_end(self, insert_mode):
         pass
+
+
+class _FrozenHalo:
+    """``with dat.frozen_halo(mode):`` (pyop2/types/dat.py:1154-1175)."""
+
+    def __init__(self, dat, access_mode):
+        self._dat = dat
+        self._access_mode = access_mode
+
+    def __enter__(self):
+        self._dat.global_to_local_begin(self._access_mode)
+        self._dat.global_to_local_end(self._access_mode)
+        self._dat.freeze_halo(self._access_mode)
+
+    def __exit__(self, *args):
+        self._dat.unfreeze_halo()
+        self._dat.local_to_global_begin(self._access_mode)
+        self._dat.local_to_global_end(self._access_mode)
 
 
 class MixedDat(AbstractDat):
@@ -468,6 +509,24 @@ class MixedDat(AbstractDat):
     def dataset(self):
         from pyop2_gb300.types.dataset import MixedDataSet
         return MixedDataSet(tuple(d.dataset for d in self._dats))
+
+    @property
+    def dim(self):
+        return tuple(d.dataset.dim for d in self._dats)
+
+    @property
+    def cdim(self):
+        return sum(d.cdim for d in self._dats)
+
+    def __hash__(self):
+        return hash(self._dats)
+
+    def __eq__(self, other):
+        """MixedDats of the same Dats are equal (pyop2/types/dat.py:1007-1016)."""
+        return type(self) is type(other) and self._dats == other._dats
+
+    def __ne__(self, other):
+        return not self.__eq__(other)
 
     @property
     def name(self):
@@ -609,6 +668,21 @@ class MixedDat(AbstractDat):
 
     def __repr__(self):
         return "MixedDat(%r)" % (self._dats,)
+
+    @property
+    def _halo_frozen(self):
+        return all(d._halo_frozen for d in self._dats)
+
+    def freeze_halo(self, access_mode):
+        for d in self._dats:
+            d.freeze_halo(access_mode)
+
+    def unfreeze_halo(self):
+        for d in self._dats:
+            d.unfreeze_halo()
+
+    def frozen_halo(self, access_mode):
+        return _FrozenHalo(self, access_mode)
 
     def global_to_local_begin(self, access_mode):
         pass

@@ -36,7 +36,6 @@ class Map:
         self._arity = int(arity)
         self._values = utils.verify_reshape(values, IntType, (iterset.total_size, arity),
                                             allow_none=True)
-        self._values.setflags(write=False)
         self.shape = (iterset.total_size, arity)
         self._name = name or "map_#x%x" % id(self)
         if offset is None or len(offset) == 0:
@@ -52,8 +51,10 @@ class Map:
 
     # ---- device
     def _device_values(self):
-        """Device int32 buffer of the values (uploaded once)."""
+        """Device int32 buffer of the values, uploaded at first use; from then
+        on the host array is read-only, so the two copies cannot diverge."""
         if self._mirror is None:
+            self._values.setflags(write=False)
             self._mirror = Mirror(IntType, self._values.shape, self._values)
         return self._mirror.dev()
 
@@ -243,6 +244,9 @@ class MixedMap(Map):
 
     def __new__(cls, maps):
         maps = tuple(maps)
+        for m in maps:
+            if not isinstance(m, Map):
+                raise ex.MapTypeError("MixedMap components must be Maps, not %r" % type(m))
         key = ("MixedMap", maps)
         holder = maps[0]._cache
         obj = holder.get(key)
@@ -315,11 +319,11 @@ class MixedMap(Map):
 
     @property
     def offset(self):
-        return tuple(0 if m.offset is None else m.offset for m in self._maps)
+        return tuple(m.offset for m in self._maps)
 
     @property
     def offset_quotient(self):
-        return tuple(0 if m.offset_quotient is None else m.offset_quotient for m in self._maps)
+        return tuple(m.offset_quotient for m in self._maps)
 
     @property
     def flattened_maps(self):

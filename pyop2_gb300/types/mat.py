@@ -127,6 +127,8 @@ class Sparsity:
     @classmethod
     def _process_args(cls, dsets, maps_and_regions, name, nest, block_sparse, diagonal_block):
         """Normalise the map pairs (pyop2/types/mat.py:118-176)."""
+        if name is not None and not isinstance(name, str):
+            raise ex.NameTypeError("Sparsity name must be a string, not %r" % type(name))
         if len(dsets) != 2:
             raise RuntimeError("dsets must be a tuple of two DataSets: got %s" % (dsets,))
         for d in dsets:
@@ -361,10 +363,15 @@ class Sparsity:
         return True
 
     def __str__(self):
-        return "OP2 Sparsity: dsets %s, name %s" % (self._dsets, self._name)
+        return ("OP2 Sparsity: dsets %s, maps_and_regions %s, name %s, nested %s, "
+                "block_sparse %s, diagonal_block %s") % (
+            self._dsets, self._maps_and_regions, self._name, self._nested, self._block_sparse,
+            self._diagonal_block)
 
     def __repr__(self):
-        return "Sparsity(%r, %r, name=%r)" % (self._dsets, self._maps_and_regions, self._name)
+        return "Sparsity(%r, %r, name=%r, nested=%r, block_sparse=%r, diagonal_block=%r)" % (
+            self._dsets, self._maps_and_regions, self._name, self._nested, self._block_sparse,
+            self._diagonal_block)
 
 
 class Mat(DataCarrier):

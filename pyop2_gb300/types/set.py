@@ -94,7 +94,8 @@ class Set:
 
     @property
     def layers(self):
-        return 1
+        """None: a plain Set is not extruded (pyop2/types/set.py:195-197)."""
+        return None
 
     def __iter__(self):
         yield self
@@ -108,6 +109,10 @@ class Set:
         return 1
 
     def __contains__(self, dset):
+        """A DataSet is in the Set it was built on (pyop2/types/set.py:181-187)."""
+        from pyop2_gb300.types.dataset import DataSet
+        if isinstance(dset, DataSet):
+            return dset.set is self
         return False
 
     def __str__(self):
@@ -361,7 +366,7 @@ class MixedSet(Set):
     def __new__(cls, sets):
         sets = tuple(sets)
         key = ("MixedSet", sets)
-        holder = sets[0]._cache if sets and sets[0] is not None else {}
+        holder = sets[0]._cache if sets and isinstance(sets[0], Set) else {}
         obj = holder.get(key)
         if obj is None:
             obj = super().__new__(cls)
@@ -376,6 +381,10 @@ class MixedSet(Set):
         for s in sets:
             if s is not None and not isinstance(s, Set):
                 raise ex.SetTypeError("MixedSet components must be Sets, not %r" % type(s))
+        # pyop2/types/set.py:548-549
+        assert all(s is None or not s._extruded or not sets[0]._extruded or
+                   np.array_equal(s.layers_array, sets[0].layers_array) for s in sets), \
+            "All components of a MixedSet must have the same number of layers."
         self._sets = sets
         self.comm = None
         self._name = "mset_#x%x" % id(self)

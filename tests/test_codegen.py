@@ -165,3 +165,17 @@ def test_bad_groups_are_rejected(op2, args, msg):
     with pytest.raises(_lib.Op2gError) as e:
         _raw_compile(args)
     assert msg in str(e.value)
+
+
+@pytest.mark.parametrize("decl", ["static void k()", "static void k( void )", "void k ( )"])
+def test_kernel_with_empty_parameter_list(op2, decl):
+    """C leaves the parameters of `k()` unspecified, so the reference may
+    pass arguments to it (test/unit/test_api.py:278-286); the wrapper then
+    calls it without arguments."""
+    cells, verts = op2.Set(4), op2.Set(5)
+    m = op2.Map(cells, verts, 2, np.arange(8) % 5)
+    d = op2.Dat(verts)
+    pl = LegacyParloop(op2.Kernel(decl + " { }", "k"), cells, d(op2.READ, m))
+    assert "k();" in compile_loop(pl).source()
+    pl2 = LegacyParloop(op2.Kernel("static void kk(double *x) { }", "kk"), cells, d(op2.READ, m))
+    assert "kk(op2g::ptr(t0));" in compile_loop(pl2).source()
