@@ -27,6 +27,23 @@ typedef unsigned long long uint64_t;
 #define NULL 0
 #endif
 
+// C++ kernels (Kernel(..., cpp=True)) may call the <cmath> / <algorithm>
+// names through std::.  NVRTC has no host standard headers (their #include
+// lines are commented out by the wrapper generator), so the device math
+// functions are made visible in namespace std here.
+namespace std {
+using ::abs; using ::fabs; using ::sqrt; using ::cbrt; using ::pow; using ::exp; using ::exp2;
+using ::expm1; using ::log; using ::log2; using ::log10; using ::log1p; using ::sin; using ::cos;
+using ::tan; using ::asin; using ::acos; using ::atan; using ::atan2; using ::sinh; using ::cosh;
+using ::tanh; using ::floor; using ::ceil; using ::round; using ::trunc; using ::fmod;
+using ::fmin; using ::fmax; using ::hypot; using ::erf; using ::erfc; using ::copysign;
+using ::isnan; using ::isinf; using ::isfinite;
+__device__ __forceinline__ double abs(double x) { return ::fabs(x); }
+__device__ __forceinline__ float abs(float x) { return ::fabsf(x); }
+template <class T> __device__ __forceinline__ const T &min(const T &a, const T &b) { return b < a ? b : a; }
+template <class T> __device__ __forceinline__ const T &max(const T &a, const T &b) { return a < b ? b : a; }
+}  // namespace std
+
 namespace op2g {
 
 // Kernel-argument pointer.  The reference passes every argument to the C

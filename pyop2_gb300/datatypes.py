@@ -16,7 +16,10 @@ _CODES = {
 
 
 def as_code(dtype):
-    """libop2g element-type code of a numpy dtype."""
+    """libop2g element-type code of a numpy dtype (an OpaqueType travels as
+    bytes: the kernel gets an untyped pointer)."""
+    if isinstance(dtype, OpaqueType):
+        return _CODES["uint8"]
     name = numpy.dtype(dtype).name
     try:
         return _CODES[name]
@@ -39,3 +42,16 @@ def dtype_limits(dtype):
     except ValueError:
         info = numpy.finfo(dtype)
     return info.min, info.max
+
+
+class OpaqueType:
+    """A C type the kernel knows by name (loopy's OpaqueType in the
+    reference, used with PassthroughArg for handles such as a PETSc Mat).
+    The wrapper hands the kernel the raw pointer; it converts to whatever
+    type the kernel's parameter declares."""
+
+    def __init__(self, name):
+        self.name = name
+
+    def __repr__(self):
+        return "OpaqueType(%r)" % self.name

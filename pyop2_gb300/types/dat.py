@@ -167,6 +167,13 @@ class Dat(AbstractDat):
         """The full host array including ghost entries."""
         return self._m.host(write=False)
 
+    @_data.setter
+    def _data(self, value):
+        """Overwrite every value, ghosts included (the reference's tests
+        assign ``dat._data`` directly)."""
+        self.increment_dat_version()
+        self._m.host(write=True)[...] = np.asarray(value).reshape(self._shape)
+
     # ---- device access
     @property
     def tensor(self):

@@ -400,21 +400,28 @@ class Mat(DataCarrier):
         if sparsity.shape != (1, 1):
             # A mixed Mat: one device matrix per block (MatNest-like for both
             # nested and monolithic sparsities; pyop2/types/mat.py:572-666).
+            self._parent = None
+            self._state = Mat.ASSEMBLED
             self._blocks = [[Mat(sparsity[i, j], self._datatype,
                                  "_".join([self._name, str(i), str(j)]))
                              for j in range(sparsity.shape[1])]
                             for i in range(sparsity.shape[0])]
+            if not sparsity.nested:
+                # blocks of a monolithic matrix share its assembly state
+                # (the reference's MatBlock, pyop2/types/mat.py:868-960)
+                for b in self:
+                    b._parent = self
             self._values = None
             self._err = None
-            self.assembly_state = Mat.ASSEMBLED
             self._version = 0
             return
+        self._parent = None
+        self._state = Mat.ASSEMBLED
         self._blocks = [[self]]
         rdim, cdim = sparsity.dims[0][0]
         self._values = torch.zeros(max(sparsity.nblocks * rdim * cdim, 1), dtype=torch.float64,
                                    device=device.device())
         self._err = torch.zeros(1, dtype=torch.int32, device=device.device())
-        self.assembly_state = Mat.ASSEMBLED
         self._version = 0
 
     @utils.validate_in(('access', _modes, ex.ModeValueError))
@@ -518,6 +525,17 @@ class Mat(DataCarrier):
         return self._blocks
 
     # ---- assembly state machine (pyop2/types/mat.py:488-501, 820-835)
+    @property
+    def assembly_state(self):
+        return self._parent.assembly_state if self._parent is not None else self._state
+
+    @assembly_state.setter
+    def assembly_state(self, value):
+        if self._parent is not None:
+            self._parent.assembly_state = value
+        else:
+            self._state = value
+
     def change_assembly_state(self, new_state):
         if new_state == Mat.ASSEMBLED or self.assembly_state == Mat.ASSEMBLED:
             self.assembly_state = new_state
@@ -526,7 +544,10 @@ class Mat(DataCarrier):
             self.assembly_state = new_state
 
     def _flush_assembly(self):
-        self._check_err()
+        if self._parent is not None:
+            self._parent._flush_assembly()
+        else:
+            self._check_err()
 
     def _check_err(self):
         if self._mixed:
@@ -543,17 +564,24 @@ class Mat(DataCarrier):
                 raise ex.MapValueError("Mat %s: map value out of range" % self._name)
 
     def assemble(self):
-        if self._mixed:
+        if self._parent is not None:
+            raise RuntimeError("Should never call assemble on MatBlock")
+        if self._mixed and self._sparsity.nested:
             for b in self:
                 b.assemble()
         self._check_err()
         self.change_assembly_state(Mat.ASSEMBLED)
 
+    def _assemble_owner(self):
+        """Assemble this matrix, or its monolithic parent."""
+        (self._parent or self).assemble()
+
     def zero(self):
-        self.assemble()
+        self._assemble_owner()
         if self._mixed:
             for b in self:
-                b.zero()
+                b._values.zero_()
+                b.increment_dat_version()
         else:
             self._values.zero_()
         self.increment_dat_version()
@@ -670,7 +698,7 @@ class Mat(DataCarrier):
     @property
     def values(self):
         """Dense copy of the matrix (refused above 1e6 entries, as the reference does)."""
-        self.assemble()
+        self._assemble_owner()
         if self.nrows * self.ncols > 1000000:
             raise ValueError("Printing dense matrix with more than 1 million entries not allowed.\n"
                              "Are you sure you wanted to do this?")
@@ -698,7 +726,7 @@ class Mat(DataCarrier):
                     y[i].tensor.copy_(acc)
                 y[i].mark_device_modified()
             return
-        self.assemble()
+        self._assemble_owner()
         b = self._bcsr()
         if transpose:
             y.tensor.zero_()

@@ -1035,3 +1035,96 @@ class TestParLoopAPI:
             with pytest.raises(RuntimeError):
                 op2.ParLoop(op2.Kernel("static void k(int *x) {}", "k"), s1, d(op2.WRITE, m))
         assert not d._halo_frozen
+
+
+# ------------------------------------------- object caching (test_caching.py)
+class TestObjectCaching:
+
+    @pytest.fixture
+    def base_set(self):
+        return op2.Set(1)
+
+    @pytest.fixture
+    def base_set2(self):
+        return op2.Set(1)
+
+    @pytest.fixture
+    def base_map(self, base_set):
+        return op2.Map(base_set, base_set, 1, [0])
+
+    @pytest.fixture
+    def base_map2(self, base_set, base_set2):
+        return op2.Map(base_set, base_set2, 1, [0])
+
+    def test_set_and_map_identity(self, base_set, base_set2, base_map, base_map2):
+        assert base_set is not base_set2 and base_set != base_set2 and not base_set == base_set2
+        assert base_map is not base_map2 and base_map != base_map2 and not base_map == base_map2
+
+    def test_dataset_cache(self, base_set, base_set2):
+        assert base_set ** 2 is base_set ** 2
+        d1 = base_set ** 1
+        for other in (base_set ** 2, base_set2 ** 1):
+            assert d1 is not other and d1 != other and not d1 == other
+
+    @gpu
+    def test_sparsity_cache_hit(self, gpu_op2, base_set, base_map):
+        dsets = (base_set ** 1, base_set ** 1)
+        sp = op2.Sparsity(dsets, [(base_map, base_map, None)])
+        assert sp is op2.Sparsity(dsets, [(base_map, base_map, None)])
+        mixed_set = op2.MixedSet([base_set, base_set])
+        maps = op2.MixedMap([base_map, base_map])
+        blocks = {(i, j): [(rm, cm, None)] for i, rm in enumerate(maps) for j, cm in enumerate(maps)}
+        sp = op2.Sparsity((mixed_set ** 1, mixed_set ** 1), blocks)
+        mixed_set2 = op2.MixedSet([base_set, base_set])
+        maps2 = op2.MixedMap([base_map, base_map])
+        blocks2 = {(i, j): [(rm, cm, None)] for i, rm in enumerate(maps2) for j, cm in enumerate(maps2)}
+        sp2 = op2.Sparsity((mixed_set2 ** 1, mixed_set2 ** 1), blocks2)
+        assert sp is sp2 and sp == sp2 and not sp != sp2
+
+    @gpu
+    def test_sparsity_cache_miss(self, gpu_op2, base_set, base_set2, base_map, base_map2):
+        sp = op2.Sparsity((base_set ** 1, base_set ** 1), [(base_map, base_map, (op2.ALL,))])
+        mixed_set = op2.MixedSet([base_set, base_set])
+        maps2 = op2.MixedMap([base_map, base_map])
+        sp2 = op2.Sparsity((mixed_set ** 1, mixed_set ** 1),
+                           {(i, j): [(rm, cm, (op2.ALL,))] for i, rm in enumerate(maps2)
+                            for j, cm in enumerate(maps2)})
+        assert sp is not sp2 and sp != sp2
+        sp3 = op2.Sparsity((base_set ** 1, base_set2 ** 1), [(base_map, base_map2, (op2.ALL,))])
+        assert sp is not sp3 and sp != sp3
+
+
+@gpu
+class TestSparsityCache:
+
+    @pytest.fixture
+    def s2(cls):
+        return op2.Set(5)
+
+    @pytest.fixture
+    def ds2(cls, s2):
+        return op2.DataSet(s2, 1)
+
+    @pytest.fixture
+    def m1(cls, s2):
+        return op2.Map(op2.Set(5), s2, 1, [0, 1, 2, 3, 4])
+
+    @pytest.fixture
+    def m2(cls, m1, s2):
+        return op2.Map(m1.iterset, s2, 1, [1, 2, 3, 4, 0])
+
+    def test_differing_maps_not_cached(self, gpu_op2, m1, m2, ds2):
+        assert op2.Sparsity((ds2, ds2), [(m1, m1, None)]) is not \
+            op2.Sparsity((ds2, ds2), [(m2, m2, None)])
+        assert op2.Sparsity((ds2, ds2), [(m1, m2, None)]) is not \
+            op2.Sparsity((ds2, ds2), [(m2, m1, None)])
+        assert op2.Sparsity((ds2, ds2), [(m1, m1, None), (m2, m2, None)]) is not \
+            op2.Sparsity((ds2, ds2), [(m2, m2, None), (m2, m2, None)])
+
+    def test_same_maps_cached(self, gpu_op2, m1, m2, ds2):
+        assert op2.Sparsity((ds2, ds2), [(m1, m1, None)]) is \
+            op2.Sparsity((ds2, ds2), [(m1, m1, None)])
+        assert op2.Sparsity((ds2, ds2), [(m1, m1, None), (m2, m2, None)]) is \
+            op2.Sparsity((ds2, ds2), [(m1, m1, None), (m2, m2, None)])
+        assert op2.Sparsity((ds2, ds2), [(m1, m1, None), (m2, m2, None)]) is \
+            op2.Sparsity((ds2, ds2), [(m2, m2, None), (m1, m1, None)])
