@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define OP2G_ABI_VERSION 2
+#define OP2G_ABI_VERSION 3
 
 /* ---------------------------------------------------------------- status */
 typedef int32_t op2g_status;
@@ -137,6 +137,10 @@ typedef struct op2g_arg_desc {
                          blocks of a mixed Mat in row-major block order (one element
                          matrix over all blocks, pyop2/codegen/builder.py:609-680)      */
     int32_t group_cols; /* MAT groups: number of block columns                         */
+    int32_t stride;   /* DAT: elements from one entity's values to the next (0 = dim).  A
+                         view of one component of a dim-S Dat (DatView,
+                         pyop2/types/dat.py:668-760) has dim 1, stride S, and its device
+                         pointer at the component                                       */
 } op2g_arg_desc;
 
 typedef struct op2g_loop_desc {

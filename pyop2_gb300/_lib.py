@@ -18,7 +18,7 @@ ERR_INVALID, ERR_COMPILE, ERR_CUDA, ERR_BOUNDS, ERR_NEW_NONZERO, ERR_CAPACITY, \
 DEVERR_MAP_BOUNDS, DEVERR_NEW_NONZERO, DEVERR_CAPACITY = 1, 2, 4
 
 F64, F32, I32, U32, I64, U64, I16, U16, I8, U8 = range(10)
-ABI_VERSION = 2
+ABI_VERSION = 3
 ARG_DAT, ARG_GLOBAL, ARG_MAT, ARG_PASSTHROUGH = range(4)
 MAP_PLAIN, MAP_PERMUTED, MAP_COMPOSED = range(3)
 SCATTER_ATOMIC, SCATTER_WARP, SCATTER_PLAIN, SCATTER_SHARED = range(4)
@@ -41,7 +41,7 @@ class MapDesc(ctypes.Structure):
 class ArgDesc(ctypes.Structure):
     _fields_ = [("kind", _i32), ("access", _i32), ("dtype", _i32), ("dim", _i32),
                 ("map", _i32), ("cmap", _i32), ("rdim", _i32), ("cdim", _i32),
-                ("group", _i32), ("group_cols", _i32)]
+                ("group", _i32), ("group_cols", _i32), ("stride", _i32)]
 
 
 class LoopDesc(ctypes.Structure):

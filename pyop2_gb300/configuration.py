@@ -73,18 +73,20 @@ class Configuration(dict):
             self[k] = v
 
     def __setitem__(self, key, value):
-        if key not in self.DEFAULTS:
-            raise ConfigurationError("Unknown configuration option %r" % key)
-        typ = self.DEFAULTS[key][1]
-        if typ is bool:
-            value = _bool(value)
-        elif typ is int and not isinstance(value, int):
-            try:
-                value = int(value)
-            except (TypeError, ValueError):
-                raise ConfigurationError("Option %r needs an int" % key)
+        """Known keys are type-checked (pyop2/configuration.py:155-168: a value
+        of the wrong type raises ConfigurationError); other keys are stored."""
+        if key in self.DEFAULTS:
+            typ = self.DEFAULTS[key][1]
+            ok = isinstance(value, typ) if isinstance(typ, tuple) else (
+                isinstance(value, bool) if typ is bool else
+                isinstance(value, int) and not isinstance(value, bool) if typ is int else
+                isinstance(value, typ))
+            if not ok:
+                raise ConfigurationError("Values for configuration key %s must be of type %r, "
+                                         "not %r" % (key, typ, type(value)))
         if key == "scatter" and value not in ("atomic", "warp", "colour", "shared", "auto"):
             raise ConfigurationError("scatter must be atomic, warp, colour, shared or auto")
+        self._set.add(key)
         super().__setitem__(key, value)
 
 

@@ -113,6 +113,12 @@ struct Gen {
         layout();
     }
 
+    // Elements between consecutive entities' values of a Dat argument.
+    int gstride(size_t a) const {
+        const op2g_arg_desc &d = S.args[a].d;
+        return d.stride > 0 ? d.stride : d.dim;
+    }
+
     int dat_pack(size_t a) const {
         const op2g_arg_desc &d = S.args[a].d;
         return d.map >= 0 ? nf * S.maps[d.map].arity * d.dim : d.dim;
@@ -543,8 +549,8 @@ struct Gen {
                     O << I << "#pragma unroll\n";
                     O << I << "  for (int i = 0; i < " << nf * ar << "; ++i) {\n";
                     O << I << "    const bool v_ = active && ti" << a << "[i] >= 0;\n";
-                    O << I << "    const long long o_ = v_ ? (long long)ti" << a << "[i] * " << D
-                      << " : 0;\n";
+                    O << I << "    const long long o_ = v_ ? (long long)ti" << a << "[i] * "
+                      << gstride(a) << " : 0;\n";
                     O << I << "#pragma unroll\n";
                     O << I << "    for (int j = 0; j < " << D << "; ++j) op2g::warp_agg_inc(d_ + o_ + j, t"
                       << a << "[i * " << D << " + j], v_);\n";
@@ -567,7 +573,7 @@ struct Gen {
                       << ") { const int h_ = sl" << a << "[s_]; const int k_ = sk" << a
                       << "[h_]; sk" << a << "[h_] = -1;\n";
                     O << "        for (int j = 0; j < " << D << "; ++j) { op2g::atomic_inc(&d_[(long long)k_ * "
-                      << D << " + j], sv" << a << "[h_ * " << D << " + j]); sv" << a << "[h_ * " << D
+                      << gstride(a) << " + j], sv" << a << "[h_ * " << D << " + j]); sv" << a << "[h_ * " << D
                       << " + j] = (" << T << ")0; } } }\n";
                 }
             O << "    __syncthreads();\n";
@@ -675,7 +681,8 @@ struct Gen {
                 if (A.d.map < 0) {
                     // direct: pointer into the Dat (pyop2/codegen/builder.py:367-377)
                     kargs.push_back("op2g::ptr((" + std::string(T) + " *)p.ptr[" +
-                                    std::to_string(A.slot) + "] + n * " + std::to_string(D) + ")");
+                                    std::to_string(A.slot) + "] + n * " +
+                                    std::to_string(gstride(a)) + ")");
                     continue;
                 }
                 const int ar = S.maps[A.d.map].arity;
@@ -702,7 +709,7 @@ struct Gen {
                         const bool nc = S.loop.nc_reads && A.d.access == OP2G_READ;
                         O << J << "    for (int j = 0; j < " << D << "; ++j) " << tn << "[" << po
                           << "(" << f * ar << " + i) * " << D << " + j] = x_ >= 0 ? "
-                          << (nc ? "__ldg(&" : "") << "d_[(long long)x_ * " << D << " + j]"
+                          << (nc ? "__ldg(&" : "") << "d_[(long long)x_ * " << gstride(a) << " + j]"
                           << (nc ? ")" : "") << " : (" << T << ")0;\n";
                         O << J << "  }\n";
                     }
@@ -773,7 +780,7 @@ struct Gen {
                     }
                     O << J << "#pragma unroll\n";
                     O << J << "    for (int j = 0; j < " << D << "; ++j) {\n";
-                    std::string dst = "d_[(long long)x_ * " + std::to_string(D) + " + j]";
+                    std::string dst = "d_[(long long)x_ * " + std::to_string(gstride(a)) + " + j]";
                     std::string src = "t" + std::to_string(first[a]) + "[" +
                                       std::to_string(poff[a]) + " + (" + std::to_string(f * ar) +
                                       " + i) * " + std::to_string(D) + " + j]";
@@ -875,6 +882,8 @@ std::string validate_signature(const Signature &S) {
         switch (d.kind) {
             case OP2G_ARG_DAT:
                 if (d.dim <= 0) return an + "dim must be positive";
+                if (d.stride < 0 || (d.stride > 0 && d.stride < d.dim))
+                    return an + "stride must be 0 or at least dim";
                 if (d.map >= (int)S.maps.size()) return an + "map index out of range";
                 if (d.map >= 0 && (d.access == OP2G_INC || d.access == OP2G_MIN || d.access == OP2G_MAX) &&
                     !atomic_capable(d.dtype) && S.loop.scatter != OP2G_SCATTER_PLAIN)

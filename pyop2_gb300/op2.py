@@ -8,7 +8,7 @@ from pyop2_gb300.logger import debug, info, warning, error, critical, set_log_le
 from pyop2_gb300.types import (  # noqa: F401
     Set, ExtrudedSet, MixedSet, Subset, DataSet, MixedDataSet, GlobalDataSet,
     Map, MixedMap, PermutedMap, ComposedMap, Sparsity,
-    Global, Constant, Dat, MixedDat, Mat,
+    Global, Constant, Dat, DatView, MixedDat, Mat,
     READ, WRITE, RW, INC, MIN, MAX, ON_BOTTOM, ON_TOP, ON_INTERIOR_FACETS, ALL)
 from pyop2_gb300.local_kernel import CStringLocalKernel, Kernel  # noqa: F401
 from pyop2_gb300.datatypes import OpaqueType  # noqa: F401
@@ -23,7 +23,7 @@ __all__ = ['configuration', 'READ', 'WRITE', 'RW', 'INC', 'MIN', 'MAX',
            'MixedSet', 'Subset', 'DataSet', 'GlobalDataSet', 'MixedDataSet',
            'Dat', 'MixedDat', 'Mat', 'Global', 'Constant', 'Map', 'MixedMap',
            'Sparsity', 'parloop', 'Parloop', 'ParLoop', 'par_loop',
-           'PermutedMap', 'ComposedMap', 'MixedDat', 'PassthroughArg', 'OpaqueType']
+           'PermutedMap', 'ComposedMap', 'MixedDat', 'DatView', 'PassthroughArg', 'OpaqueType']
 
 _initialised = False
 set_log_level(configuration['log_level'])

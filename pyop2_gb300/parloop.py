@@ -25,7 +25,7 @@ from pyop2_gb300.datatypes import IntType, as_code
 from pyop2_gb300.exceptions import KernelTypeError, MapValueError, SetTypeError
 from pyop2_gb300.local_kernel import CStringLocalKernel, LocalKernel
 from pyop2_gb300.types.access import ALL, Access, IterationRegion
-from pyop2_gb300.types.dat import Dat
+from pyop2_gb300.types.dat import Dat, DatView
 from pyop2_gb300.types.glob import Constant, Global
 from pyop2_gb300.types.map import ComposedMap, Map, MixedMap, PermutedMap
 from pyop2_gb300.types.mat import Mat
@@ -347,7 +347,8 @@ class Parloop:
                 d = (_lib.ARG_PASSTHROUGH, int(Access.RW), as_code(a.dtype), 1, -1, -1, 0, 0)
             else:
                 raise ValueError("Unhandled argument type %r" % type(a))
-            argdescs.append(d + (group, gcols))
+            stride = getattr(a.data, "_view_stride", 0) if isinstance(a, DatLegacyArg) else 0
+            argdescs.append(d + (group, gcols, stride))
         return table, argdescs
 
     def _nc_reads(self):
@@ -356,7 +357,8 @@ class Parloop:
         read, written = set(), set()
         for a in self._components:
             if isinstance(a, DatLegacyArg):
-                (read if a.access is Access.READ else written).add(id(a.data))
+                owner = a.data._parent if isinstance(a.data, DatView) else a.data
+                (read if a.access is Access.READ else written).add(id(owner))
         return not (read & written)
 
     def _loop_desc(self, scatter, block_size, prefetch=None):

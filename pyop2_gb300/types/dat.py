@@ -388,6 +388,25 @@ class Dat(AbstractDat):
     def __repr__(self):
         return "Dat(%r, None, %r, %r)" % (self._dataset, self.dtype, self._name)
 
+    # ---- vector views (pyop2/types/dat.py:762-784 hand out a PETSc Vec; here
+    # the Vec is the flat device tensor of the owned values)
+    def vec_context(self, access):
+        """Context manager yielding the owned values as a flat CUDA tensor;
+        unless ``access`` is READ the Dat counts as modified on exit."""
+        return _VecContext(self, access)
+
+    @property
+    def vec(self):
+        return self.vec_context(Access.RW)
+
+    @property
+    def vec_wo(self):
+        return self.vec_context(Access.WRITE)
+
+    @property
+    def vec_ro(self):
+        return self.vec_context(Access.READ)
+
     # ---- halo freezing (pyop2/types/dat.py:634-665, 1154-1175).  A single
     # device has no halo exchanges to skip, but the bookkeeping is kept: a Dat
     # frozen for one access mode may only be used with that mode.
@@ -423,6 +442,161 @@ class Dat(AbstractDat):
 
     def local_to_global_end(self, insert_mode):
         pass
+
+
+class DatView(Dat):
+    """One component of a Dat (pyop2/types/dat.py:668-760): in a par_loop the
+    kernel sees only component ``index``, with dim 1; ``data`` and friends
+    are the matching column of the parent's arrays.  No storage of its own:
+    the device pointer is the parent's, advanced to the component, and the
+    wrapper strides by the parent's dim."""
+
+    def __init__(self, dat, index):
+        index = utils.as_tuple(index)
+        assert len(index) == len(dat.dim)
+        for i, d in zip(index, dat.dim):
+            if not (0 <= i < d):
+                raise ex.IndexValueError("Can't create DatView with index %s for Dat with "
+                                         "shape %s" % (index, dat.dim))
+        self.index = index
+        self._idx = (slice(None), *index)
+        self._parent = dat
+        self._dataset = dat.dataset
+        self.comm = dat.comm
+        self._dtype = dat.dtype
+        self._m = dat._m
+        self._shape = (dat.dataset.total_size,)
+        self._name = "view[%s](%s)" % (index, dat.name)
+        # flat position of the component inside one entity's values
+        self._view_offset = int(np.ravel_multi_index(index, dat.dim)) if dat.cdim > 1 else 0
+        self._view_stride = dat.cdim
+
+    @property
+    def cdim(self):
+        return 1
+
+    @property
+    def dim(self):
+        return (1,)
+
+    @property
+    def halo_valid(self):
+        return self._parent.halo_valid
+
+    @halo_valid.setter
+    def halo_valid(self, value):
+        self._parent.halo_valid = value
+
+    @property
+    def dat_version(self):
+        return self._parent.dat_version
+
+    def increment_dat_version(self):
+        self._parent.increment_dat_version()
+
+    @property
+    def _halo_frozen(self):
+        return self._parent._halo_frozen
+
+    @property
+    def _frozen_access_mode(self):
+        return self._parent._frozen_access_mode
+
+    @property
+    def _data(self):
+        return self._parent._data[self._idx]
+
+    @property
+    def data(self):
+        return self._parent.data[self._idx]
+
+    @property
+    def data_ro(self):
+        return self._parent.data_ro[self._idx]
+
+    @property
+    def data_wo(self):
+        return self._parent.data_wo[self._idx]
+
+    @property
+    def data_with_halos(self):
+        return self._parent.data_with_halos[self._idx]
+
+    @property
+    def data_ro_with_halos(self):
+        return self._parent.data_ro_with_halos[self._idx]
+
+    @property
+    def data_wo_with_halos(self):
+        return self._parent.data_wo_with_halos[self._idx]
+
+    @property
+    def nbytes(self):
+        return self.dtype.itemsize * self.dataset.total_size
+
+    @property
+    def tensor(self):
+        """Strided device view of the component."""
+        t = self._parent.tensor
+        return t.reshape(t.shape[0], -1)[:, self._view_offset]
+
+    def _device_ptr(self):
+        return self._m.dev().data_ptr() + self._view_offset * self.dtype.itemsize
+
+    def mark_device_modified(self):
+        self._parent.mark_device_modified()
+
+    def zero(self, subset=None):
+        if subset is not None:
+            self.data[subset.owned_indices] = 0
+            return
+        self.increment_dat_version()
+        self.tensor.zero_()
+        self._m.dev_modified()
+        self._parent.halo_valid = True
+
+    def __repr__(self):
+        return "DatView(%r, %r)" % (self._parent, self.index)
+
+    def __str__(self):
+        return "OP2 DatView: %s of %s" % (self.index, self._parent)
+
+
+class _VecContext:
+    """``with dat.vec as v:``: ``v`` is the flat device tensor of the owned
+    values (a MixedDat's components concatenated, copied back on exit)."""
+
+    def __init__(self, dat, access):
+        self._dat = dat
+        self._access = access
+
+    def __enter__(self):
+        import torch
+        d = self._dat
+        if isinstance(d, MixedDat):
+            self._parts = [c.tensor[:c.dataset.size].reshape(-1) for c in d]
+            self._v = torch.cat(self._parts)
+        else:
+            self._v = d.tensor[:d.dataset.size].reshape(-1)
+        self._before = self._v.clone() if self._access is not Access.READ else None
+        return self._v
+
+    def __exit__(self, *args):
+        if self._access is Access.READ:
+            return
+        d = self._dat
+        if isinstance(d, MixedDat):
+            o = 0
+            for c, part in zip(d, self._parts):
+                n = part.numel()
+                if not bool((self._v[o:o + n] == self._before[o:o + n]).all()):
+                    part.copy_(self._v[o:o + n])
+                    c.mark_device_modified()
+                    c.halo_valid = False
+                o += n
+        elif not bool((self._v == self._before).all()):
+            d.mark_device_modified()
+            d.halo_valid = False
 
 
 class _FrozenHalo:
@@ -679,6 +853,21 @@ class MixedDat(AbstractDat):
     @property
     def _halo_frozen(self):
         return all(d._halo_frozen for d in self._dats)
+
+    def vec_context(self, access):
+        return _VecContext(self, access)
+
+    @property
+    def vec(self):
+        return self.vec_context(Access.RW)
+
+    @property
+    def vec_wo(self):
+        return self.vec_context(Access.WRITE)
+
+    @property
+    def vec_ro(self):
+        return self.vec_context(Access.READ)
 
     def freeze_halo(self, access_mode):
         for d in self._dats:

@@ -2,6 +2,8 @@
 par_loop.  INC / MIN / MAX reductions happen on the device into the Global's
 own device copy, so successive loops accumulate as in the reference
 (pyop2/parloop.py:449-452)."""
+import operator
+
 import numpy as np
 
 from pyop2_gb300 import exceptions as ex
@@ -135,6 +137,63 @@ class Global(DataCarrier):
     def duplicate(self):
         return type(self)(self.dim, data=np.copy(self.data_ro), dtype=self.dtype, name=self.name,
                           comm=self.comm)
+
+    # ---- arithmetic on the (small) values, on the host
+    # (pyop2/types/glob.py:132-204)
+    def _op(self, other, op):
+        ret = type(self)(self.dim, dtype=self.dtype, name=self.name, comm=self.comm)
+        ret.data[:] = op(self.data_ro, other.data_ro if isinstance(other, Global) else other)
+        return ret
+
+    def _iop(self, other, op):
+        op(self.data[:], other.data_ro if isinstance(other, Global) else other)
+        return self
+
+    def __pos__(self):
+        return self.duplicate()
+
+    def __neg__(self):
+        return type(self)(self.dim, data=-np.copy(self.data_ro), dtype=self.dtype,
+                          name=self.name, comm=self.comm)
+
+    def __add__(self, other):
+        return self._op(other, operator.add)
+
+    def __radd__(self, other):
+        return self + other
+
+    def __sub__(self, other):
+        return self._op(other, operator.sub)
+
+    def __rsub__(self, other):
+        ret = -self
+        ret += other
+        return ret
+
+    def __mul__(self, other):
+        return self._op(other, operator.mul)
+
+    def __rmul__(self, other):
+        return self.__mul__(other)
+
+    def __truediv__(self, other):
+        return self._op(other, operator.truediv)
+
+    def __iadd__(self, other):
+        return self._iop(other, operator.iadd)
+
+    def __isub__(self, other):
+        return self._iop(other, operator.isub)
+
+    def __imul__(self, other):
+        return self._iop(other, operator.imul)
+
+    def __itruediv__(self, other):
+        return self._iop(other, operator.itruediv)
+
+    def inner(self, other):
+        assert issubclass(type(other), type(self))
+        return np.dot(self.data_ro, np.conj(other.data_ro))
 
     def __str__(self):
         return "OP2 Global Argument: %s with dim %s and value %s" % (self._name, self._dim,

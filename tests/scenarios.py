@@ -459,6 +459,33 @@ static void comp_vol(double A[1], double x[6][2], double y[1])
     return float(g.data[0])
 
 
+def sc_extrusion_fields(op2):
+    """test_extruded_nbytes, test_write_data_field, test_write_data_coords,
+    test_read_coord_neighbours_write_to_field (test/unit/test_extrusion.py:
+    358-426)."""
+    elements, node_set, elem_set, coords_map, field_map, dat_coords, dat_field = _ext(op2)
+    wedges = EXT_LAYERS - 1
+    if hasattr(dat_field, "nbytes"):
+        assert dat_field.nbytes == EXT_NELEMS * wedges * 8
+    dat_f = op2.Dat(op2.DataSet(elem_set, 1), -np.ones(EXT_NELEMS * wedges), np.float64, "f")
+    op2.par_loop(op2.Kernel("static void wo(double* x) { x[0] = 42.0; }\n", "wo"), elements,
+                 dat_f(op2.WRITE, field_map))
+    assert np.all(dat_f.data == 42)
+    dat_c = op2.Dat(op2.DataSet(node_set, 2), np.zeros(((EXT_NELEMS + 2) * EXT_LAYERS, 2)),
+                    np.float64, "c")
+    op2.par_loop(op2.Kernel("""static void wo_c(double x[6][2]) {
+       for (int i = 0; i < 6; ++i) { x[i][0] = 42.0; x[i][1] = 42.0; } }""", "wo_c"), elements,
+                 dat_c(op2.WRITE, coords_map))
+    assert np.all(dat_c.data == 42)
+    op2.par_loop(op2.Kernel("""static void wtf(double* y, double x[6][2]) {
+       double sum = 0.0;
+       for (int i=0; i<6; i++) sum += x[i][0] + x[i][1];
+       y[0] = sum; }""", "wtf"), elements, dat_f(op2.WRITE, field_map),
+                 dat_coords(op2.READ, coords_map))
+    assert np.all(dat_f.data >= 0)
+    return dat_f.data.copy()
+
+
 def sc_extrusion_direct_inc(op2):
     iterset = op2.Set(EXT_NELEMS)
     dat = op2.Dat(op2.DataSet(iterset, 1))

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib):
     L = lib.lib()
     for name in declared_functions():
         assert hasattr(L, name), name
-    assert L.op2g_abi_version() == 2
+    assert L.op2g_abi_version() == 3
     assert L.op2g_last_error() is not None
 
 
@@ -42,7 +42,7 @@ STRUCTS = {
     "op2g_map_desc": ("MapDesc", ["kind", "arity", "base", "ncomposed", "composed", "offset",
                                   "offset_quotient", "permutation"]),
     "op2g_arg_desc": ("ArgDesc", ["kind", "access", "dtype", "dim", "map", "cmap", "rdim", "cdim",
-                                  "group", "group_cols"]),
+                                  "group", "group_cols", "stride"]),
     "op2g_loop_desc": ("LoopDesc", ["extruded", "constant_layers", "extruded_periodic", "indexed",
                                     "iteration_region", "pass_layer_arg", "scatter",
                                     "block_size", "debug_checks", "batched", "prefetch",

@@ -170,8 +170,10 @@ def test_kernel_rejects_host_only_options():
 def test_configuration():
     from pyop2_gb300.configuration import configuration
     from pyop2_gb300.exceptions import ConfigurationError
+    configuration["no_such_key"] = 1           # other keys are stored (as the reference does)
+    assert configuration["no_such_key"] == 1
     with pytest.raises(ConfigurationError):
-        configuration["no_such_key"] = 1
+        configuration["debug"] = "yes"          # known keys are type-checked
     with pytest.raises(ConfigurationError):
         configuration["scatter"] = "sometimes"
     op2.init(debug=False, scatter="atomic")

@@ -1128,3 +1128,44 @@ class TestSparsityCache:
             op2.Sparsity((ds2, ds2), [(m1, m1, None), (m2, m2, None)])
         assert op2.Sparsity((ds2, ds2), [(m1, m1, None), (m2, m2, None)]) is \
             op2.Sparsity((ds2, ds2), [(m2, m2, None), (m1, m1, None)])
+
+
+# ------------------------------------ test_globals.py, test_configuration.py
+def test_global_operations():
+    g1 = op2.Global(1, data=2.)
+    g2 = op2.Global(1, data=5.)
+    assert (g1 + g2).data == 7.
+    assert (g2 - g1).data == 3.
+    assert (-g2).data == -5.
+    assert (g1 * g2).data == 10.
+    g1 *= g2
+    assert g1.data == 10.
+
+
+def test_global_dat_version():
+    g1 = op2.Global(1, data=1.)
+    g2 = op2.Global(1, data=2.)
+    assert g1.dat_version == 0 and g2.dat_version == 0
+    d1 = g1.data
+    assert g1.dat_version == 1 and g2.dat_version == 0
+    g2.data[:] += 1
+    assert g1.dat_version == 1 and g2.dat_version == 1
+    g1.zero()
+    assert g1.dat_version == 2 and g2.dat_version == 1
+    g2.data = d1
+    assert g1.dat_version == 2 and g2.dat_version == 2
+
+
+def test_add_configuration_value():
+    from pyop2_gb300.configuration import Configuration
+    c = Configuration()
+    c.reconfigure(foo='bar')
+    assert c['foo'] == 'bar'
+
+
+@pytest.mark.parametrize(('key', 'val'), [('debug', 'illegal'), ('log_level', 1.5)])
+def test_configuration_illegal_types(key, val):
+    from pyop2_gb300.configuration import Configuration
+    c = Configuration()
+    with pytest.raises(exceptions.ConfigurationError):
+        c[key] = val

@@ -16,6 +16,7 @@ UNSIZED = [S.sc_2d_map, S.sc_itspace_sum_nodes_to_edges, S.sc_vm_read_1d, S.sc_v
            S.sc_vm_inc_1d, S.sc_vm_read_2d, S.sc_vm_write_2d, S.sc_vm_inc_2d, S.sc_direct,
            S.sc_permuted_map, S.sc_subset_direct, S.sc_subset_indirect,
            S.sc_extrusion_volume, S.sc_extrusion_direct_inc, S.sc_extrusion_layer_arg,
+           S.sc_extrusion_fields,
            S.sc_extrusion_write_coords, S.sc_mass_matrix, S.sc_rhs, S.sc_set_matrix,
            S.sc_vector_mass_matrix, S.sc_sparsity_nnz, S.sc_sparsity_blockwise]
 
