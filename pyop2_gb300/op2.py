@@ -14,7 +14,14 @@ from pyop2_gb300.local_kernel import CStringLocalKernel, Kernel  # noqa: F401
 from pyop2_gb300.datatypes import OpaqueType  # noqa: F401
 from pyop2_gb300.parloop import (Parloop, ParLoop, LegacyParloop, parloop, par_loop,  # noqa: F401
                                  GlobalLegacyArg, DatLegacyArg, MatLegacyArg, PassthroughArg,
-                                 MixedDatLegacyArg, MixedMatLegacyArg)
+                                 MixedDatLegacyArg, MixedMatLegacyArg,
+                                 GlobalParloopArg, DatParloopArg, MixedDatParloopArg,
+                                 MatParloopArg, MixedMatParloopArg, PassthroughParloopArg)
+from pyop2_gb300.global_kernel import (GlobalKernelArg, DatKernelArg,  # noqa: F401
+                                       MixedDatKernelArg, MatKernelArg, MixedMatKernelArg,
+                                       MapKernelArg, PermutedMapKernelArg,
+                                       ComposedMapKernelArg, PassthroughKernelArg,
+                                       GlobalKernel)
 
 __all__ = ['configuration', 'READ', 'WRITE', 'RW', 'INC', 'MIN', 'MAX',
            'ON_BOTTOM', 'ON_TOP', 'ON_INTERIOR_FACETS', 'ALL',

@@ -47,6 +47,15 @@ class GlobalLegacyArg(LegacyArg):
         return self.data.dtype
 
     @property
+    def global_kernel_arg(self):
+        from pyop2_gb300.global_kernel import GlobalKernelArg
+        return GlobalKernelArg(self.data.dim)
+
+    @property
+    def parloop_arg(self):
+        return GlobalParloopArg(self.data)
+
+    @property
     def maps(self):
         return ()
 
@@ -60,6 +69,17 @@ class DatLegacyArg(LegacyArg):
     @property
     def dtype(self):
         return self.data.dtype
+
+    @property
+    def global_kernel_arg(self):
+        from pyop2_gb300.global_kernel import DatKernelArg
+        m = self.map_._global_kernel_arg if self.map_ is not None else None
+        index = self.data.index if isinstance(self.data, DatView) else None
+        return DatKernelArg(self.data.dataset.dim, m, index=index)
+
+    @property
+    def parloop_arg(self):
+        return DatParloopArg(self.data, self.map_)
 
     @property
     def maps(self):
@@ -77,6 +97,16 @@ class MatLegacyArg(LegacyArg):
     @property
     def dtype(self):
         return self.data.dtype
+
+    @property
+    def global_kernel_arg(self):
+        from pyop2_gb300.global_kernel import MatKernelArg
+        return MatKernelArg(self.data.dims, tuple(m._global_kernel_arg for m in self.maps),
+                            unroll=self.needs_unrolling)
+
+    @property
+    def parloop_arg(self):
+        return MatParloopArg(self.data, self.maps, self.lgmaps)
 
 
 @dataclass
@@ -97,6 +127,15 @@ class MixedDatLegacyArg(LegacyArg):
 
     def components(self):
         return [DatLegacyArg(d, m, self.access) for d, m in zip(self.data, self.map_)]
+
+    @property
+    def global_kernel_arg(self):
+        from pyop2_gb300.global_kernel import MixedDatKernelArg
+        return MixedDatKernelArg(tuple(c.global_kernel_arg for c in self.components()))
+
+    @property
+    def parloop_arg(self):
+        return MixedDatParloopArg(self.data, self.map_)
 
 
 @dataclass
@@ -120,6 +159,16 @@ class MixedMatLegacyArg(LegacyArg):
         return [MatLegacyArg(self.data[i, j], (rm.split[i], cm.split[j]), self.access)
                 for i in range(nr) for j in range(nc)]
 
+    @property
+    def global_kernel_arg(self):
+        from pyop2_gb300.global_kernel import MixedMatKernelArg
+        return MixedMatKernelArg(tuple(c.global_kernel_arg for c in self.components()),
+                                 shape=self.data.sparsity.shape)
+
+    @property
+    def parloop_arg(self):
+        return MixedMatParloopArg(self.data, tuple(self.maps), self.lgmaps)
+
 
 @dataclass
 class PassthroughArg(LegacyArg):
@@ -131,6 +180,92 @@ class PassthroughArg(LegacyArg):
     @property
     def maps(self):
         return ()
+
+    @property
+    def global_kernel_arg(self):
+        from pyop2_gb300.global_kernel import PassthroughKernelArg
+        return PassthroughKernelArg()
+
+    @property
+    def parloop_arg(self):
+        return PassthroughParloopArg(self.data)
+
+
+# ------------------------------------------- non-legacy loop arguments
+# (pyop2/parloop.py:30-164): data (+ maps) without the access, which the
+# local kernel's ``accesses`` supply.
+class ParloopArg:
+    pass
+
+
+@dataclass
+class GlobalParloopArg(ParloopArg):
+    data: Global
+
+    @property
+    def maps(self):
+        return ()
+
+
+@dataclass
+class DatParloopArg(ParloopArg):
+    data: Dat
+    map_: Optional[Map] = None
+
+    @property
+    def maps(self):
+        return (self.map_,) if self.map_ is not None else ()
+
+
+@dataclass
+class MixedDatParloopArg(ParloopArg):
+    data: Any
+    map_: Any
+
+    @property
+    def maps(self):
+        return (self.map_,)
+
+
+@dataclass
+class MatParloopArg(ParloopArg):
+    data: Mat
+    maps: Tuple[Map, Map]
+    lgmaps: Optional[Any] = None
+
+
+@dataclass
+class MixedMatParloopArg(ParloopArg):
+    data: Mat
+    maps: Tuple[Any, Any]
+    lgmaps: Any = None
+
+
+@dataclass
+class PassthroughParloopArg(ParloopArg):
+    data: int
+
+    @property
+    def maps(self):
+        return ()
+
+
+def _legacy_from(parg, access, dtype, garg):
+    """The legacy argument equivalent to a ParloopArg with its access."""
+    if isinstance(parg, GlobalParloopArg):
+        return GlobalLegacyArg(parg.data, access)
+    if isinstance(parg, DatParloopArg):
+        return DatLegacyArg(parg.data, parg.map_, access)
+    if isinstance(parg, MixedDatParloopArg):
+        return MixedDatLegacyArg(parg.data, parg.map_, access)
+    if isinstance(parg, MatParloopArg):
+        return MatLegacyArg(parg.data, tuple(parg.maps), access, parg.lgmaps,
+                            getattr(garg, "unroll", False))
+    if isinstance(parg, MixedMatParloopArg):
+        return MixedMatLegacyArg(parg.data, tuple(parg.maps), access, parg.lgmaps)
+    if isinstance(parg, PassthroughParloopArg):
+        return PassthroughArg(dtype if dtype is not None else np.uint8, parg.data)
+    raise ValueError("Unhandled argument type %r" % type(parg))
 
 
 # ------------------------------------------------------------- validation
@@ -281,6 +416,25 @@ class Parloop:
     """
 
     def __init__(self, local_knl, iterset, args, iteration_region=None, pass_layer_arg=False):
+        from pyop2_gb300.global_kernel import GlobalKernel, check_constants
+        self._global_kernel = None
+        self._parloop_args = None
+        if isinstance(local_knl, GlobalKernel):
+            # the non-legacy form Parloop(global_kernel, iterset, parloop_args)
+            # (pyop2/parloop.py:167-190)
+            g = local_knl
+            if len(g.arguments) != len(args):
+                raise ValueError("You are trying to pass in a different number of arguments "
+                                 "than the kernel is expecting")
+            check_constants(g, args)
+            dtypes = getattr(g.local_kernel, "dtypes", None) or (None,) * len(args)
+            self._global_kernel = g
+            self._parloop_args = list(args)
+            args = [_legacy_from(pa, acc, dt, ga) for pa, acc, dt, ga in
+                    zip(args, g.local_kernel.accesses, dtypes, g.arguments)]
+            iteration_region = g._iteration_region
+            pass_layer_arg = g._pass_layer_arg
+            local_knl = g.local_kernel
         if not isinstance(local_knl, LocalKernel):
             raise KernelTypeError
         if pass_layer_arg and not iterset._extruded:
@@ -298,6 +452,9 @@ class Parloop:
         self.iteration_region = IterationRegion(iteration_region or ALL)
         self.pass_layer_arg = bool(pass_layer_arg)
         self._built = None
+        self._flatten()
+
+    def _flatten(self):
         # Arguments as the wrapper sees them: mixed arguments become their
         # components, tagged with a group id (one kernel parameter per group)
         # and, for Mats, the number of block columns.
@@ -324,8 +481,32 @@ class Parloop:
         return tuple(a.access for a in self.args)
 
     @property
+    def global_kernel(self):
+        """The GlobalKernel this loop runs (built from legacy arguments when
+        the loop was constructed from them)."""
+        if self._global_kernel is None:
+            self.local_kernel.accesses = self.accesses
+            self._global_kernel = global_kernel_of(self.local_kernel, self.iterset, self.args,
+                                                   self.iteration_region, self.pass_layer_arg)
+        return self._global_kernel
+
+    def replace_data(self, index, new_argument):
+        """Run the loop on other data (pyop2/parloop.py:218-219): argument
+        ``index`` now refers to ``new_argument``.  The compiled wrapper is
+        kept when the signature is unchanged."""
+        old_key = self.cache_key()
+        a = self.args[index]
+        a.data = new_argument
+        if self._parloop_args is not None:
+            self._parloop_args[index].data = new_argument
+        self._flatten()
+        self._launch_cache = None
+        if self.cache_key() != old_key:
+            self._built = None
+
+    @property
     def arguments(self):
-        return self.args
+        return tuple(self._parloop_args) if self._parloop_args is not None else self.args
 
     # ---- signature
     def _signature(self):
@@ -678,6 +859,18 @@ def LegacyParloop(local_knl, iterset, *args, **kwargs):
     if isinstance(local_knl, CStringLocalKernel):
         local_knl.dtypes = tuple(a.dtype for a in args)
     return Parloop(local_knl, iterset, args, **kwargs)
+
+
+def global_kernel_of(local_knl, iterset, args, iteration_region=None, pass_layer_arg=False):
+    """The GlobalKernel describing a legacy loop (pyop2/parloop.py:719-737)."""
+    from pyop2_gb300.global_kernel import GlobalKernel
+    extruded = iterset._extruded
+    return GlobalKernel(local_knl, tuple(a.global_kernel_arg for a in args),
+                        extruded=extruded,
+                        extruded_periodic=iterset._extruded_periodic,
+                        constant_layers=bool(extruded and iterset.constant_layers),
+                        subset=isinstance(iterset, Subset),
+                        iteration_region=iteration_region, pass_layer_arg=pass_layer_arg)
 
 
 def ParLoop(*args, **kwargs):

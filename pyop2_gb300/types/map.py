@@ -59,6 +59,12 @@ class Map:
         return self._mirror.dev()
 
     @property
+    def _global_kernel_arg(self):
+        from pyop2_gb300.global_kernel import MapKernelArg
+        return MapKernelArg(self.arity, utils.tuplify(self.offset),
+                            utils.tuplify(self.offset_quotient))
+
+    @property
     def _cache_key(self):
         """What of this map determines generated code (pyop2/types/map.py:60-62)."""
         return (type(self).__name__, self.arity, utils.tuplify(self.offset),
@@ -134,6 +140,11 @@ class Map:
 class PermutedMap(Map):
     """``local[i] = global[map[permutation[i]]]`` (pyop2/types/map.py:171-215)."""
 
+    @property
+    def _global_kernel_arg(self):
+        from pyop2_gb300.global_kernel import PermutedMapKernelArg
+        return PermutedMapKernelArg(self.map_._global_kernel_arg, tuple(self.permutation))
+
     def __init__(self, map_, permutation):
         if not isinstance(map_, Map):
             raise TypeError("map_ must be a Map instance")
@@ -190,6 +201,11 @@ class PermutedMap(Map):
 class ComposedMap(Map):
     """``local[i] = global[maps_[0][maps_[1][...[n]]][i]]``; inner maps have
     arity 1 (pyop2/types/map.py:218-294)."""
+
+    @property
+    def _global_kernel_arg(self):
+        from pyop2_gb300.global_kernel import ComposedMapKernelArg
+        return ComposedMapKernelArg(*(m._global_kernel_arg for m in self.maps_))
 
     def __init__(self, *maps_, name=None):
         if not all(isinstance(m, Map) for m in maps_):
