@@ -15,16 +15,28 @@ _CODES = {
 }
 
 
+_CODE_OF = {}     # dtype (or type) -> code, filled on first use
+
+
 def as_code(dtype):
     """libop2g element-type code of a numpy dtype (an OpaqueType travels as
     bytes: the kernel gets an untyped pointer)."""
     if isinstance(dtype, OpaqueType):
         return _CODES["uint8"]
+    try:
+        return _CODE_OF[dtype]
+    except (KeyError, TypeError):
+        pass
     name = numpy.dtype(dtype).name
     try:
-        return _CODES[name]
+        code = _CODES[name]
     except KeyError:
         raise TypeError("pyop2_gb300 has no device element type for %s" % name)
+    try:
+        _CODE_OF[dtype] = code
+    except TypeError:
+        pass
+    return code
 
 
 def as_cstr(dtype):

@@ -12,6 +12,7 @@ INC/MIN/MAX conflicts through maps are resolved by hardware atomics (default),
 warp-aggregated atomics, or a greedy colouring with one launch per colour
 (``configuration['scatter']``; ``'auto'`` lets the autotuner choose).
 """
+import collections
 import ctypes
 from dataclasses import dataclass
 from typing import Any, Optional, Tuple
@@ -452,6 +453,7 @@ class Parloop:
         self.iteration_region = IterationRegion(iteration_region or ALL)
         self.pass_layer_arg = bool(pass_layer_arg)
         self._built = None
+        self._plan = None
         self._flatten()
 
     def _flatten(self):
@@ -501,6 +503,7 @@ class Parloop:
             self._parloop_args[index].data = new_argument
         self._flatten()
         self._launch_cache = None
+        self._plan = None
         if self.cache_key() != old_key:
             self._built = None
 
@@ -620,27 +623,44 @@ class Parloop:
         _lib.call("op2g_kernel_prepare", k.handle)   # module loaded outside any capture
         self._built = (scatter, block_size, k, table, argdescs)
         self._launch_cache = None
+        self._plan = None
         return k
 
     # ---- execution
-    def _pointers(self, table, k):
-        """Device pointer slots (order documented in include/op2g.h) and the
-        error-word pointer."""
-        ptrs = []
+    def _pointer_plan(self, table):
+        """What the pointer slots come from, fixed for a built loop: per
+        component its kind and object; the maps' device arrays (uploaded once,
+        never moved) resolved now."""
+        plan = []
         err = None
         for a in self._components:
             if isinstance(a, (GlobalLegacyArg, DatLegacyArg)):
-                ptrs.append(a.data._device_ptr())
+                plan.append((0, a.data))
             elif isinstance(a, MatLegacyArg):
-                m = a.data
-                ptrs += [m._values.data_ptr(), m.sparsity.rowptr.data_ptr(),
-                         m.sparsity._colidx.data_ptr()]
+                plan.append((1, a.data))
                 if err is None:
-                    err = m._err
+                    err = a.data._err
             elif isinstance(a, PassthroughArg):
-                ptrs.append(int(a.data))
-        for obj in table.objs:
-            ptrs.append(obj._device_values().data_ptr() if obj is not None else 0)
+                plan.append((2, int(a.data)))
+        maps = [obj._device_values().data_ptr() if obj is not None else 0 for obj in table.objs]
+        mats = [(a.data, Mat.ADD_VALUES if a.access is Access.INC else Mat.INSERT_VALUES)
+                for a in self._components if isinstance(a, MatLegacyArg)]
+        return plan, maps, err, mats
+
+    def _pointers(self, table, k):
+        """Device pointer slots (order documented in include/op2g.h) and the
+        error-word pointer."""
+        plan, maps, err, _ = self._plan
+        ptrs = []
+        for kind, obj in plan:
+            if kind == 0:
+                ptrs.append(obj._device_ptr())     # uploads host-side changes
+            elif kind == 1:
+                ptrs += [obj._values.data_ptr(), obj.sparsity.rowptr.data_ptr(),
+                         obj.sparsity._colidx.data_ptr()]
+            else:
+                ptrs.append(obj)
+        ptrs += maps
         assert len(ptrs) == k.nptrs
         return ptrs, err
 
@@ -670,10 +690,10 @@ class Parloop:
             self.build()
         scatter, bs, k, table, argdescs = self._built
         it = self.iterset
-        for a in self._components:
-            if isinstance(a, MatLegacyArg):
-                a.data.change_assembly_state(Mat.ADD_VALUES if a.access is Access.INC
-                                             else Mat.INSERT_VALUES)
+        if self._plan is None:
+            self._plan = self._pointer_plan(table)
+        for m, state in self._plan[3]:
+            m.change_assembly_state(state)
         ptrs, err = self._pointers(table, k)
         dbg = configuration["debug"] and err is None
         cache = getattr(self, "_launch_cache", None)
@@ -749,7 +769,7 @@ class Parloop:
             finally:
                 D.start, D.end, D.indices = start, end, idx
         else:
-            _lib.call("op2g_kernel_launch", k.handle, ctypes.byref(D), st)
+            _lib.check(_launch(k.handle, ctypes.byref(D), st))
         self.mark_written()
         if self._dbg_err is not None:
             e = int(self._dbg_err.item())
@@ -763,6 +783,13 @@ class Parloop:
         if self._built is None:
             self.build()
         return self._built[2].source()
+
+
+def _launch(handle, desc, stream):
+    """op2g_kernel_launch, bound once."""
+    global _launch
+    _launch = _lib.lib().op2g_kernel_launch
+    return _launch(handle, desc, stream)
 
 
 # ------------------------------------------------------------- colouring
@@ -877,12 +904,74 @@ def ParLoop(*args, **kwargs):
     return LegacyParloop(*args, **kwargs)
 
 
+# Recently run loops, so that a par_loop call repeating an earlier one (same
+# kernel, iteration set, data objects, maps, access modes and options) skips
+# validation and signature building and reuses the launch descriptor (the
+# host cost of a call drops from ~45 to ~12 us, which is what a loop over a
+# few thousand cells costs on the device).  The entries hold their objects,
+# so the ids in a key cannot be reused while it lives; the cost is that the
+# data of the last 16 distinct loops stays alive.  Loops made internally for
+# temporaries (Dat arithmetic) go through run_once and are not kept.
+_RECENT = collections.OrderedDict()
+_RECENT_SIZE = 16
+_CONFIG_KEYS = ("scatter", "block_size", "prefetch", "grid", "debug", "autotune", "type_check")
+
+
+def _arg_key(a):
+    if isinstance(a, DatLegacyArg):
+        return (0, id(a.data), id(a.map_), a.access)
+    if isinstance(a, GlobalLegacyArg):
+        return (1, id(a.data), a.access)
+    if isinstance(a, MatLegacyArg):
+        return (2, id(a.data), id(a.maps[0]), id(a.maps[1]), a.access, a.needs_unrolling)
+    if isinstance(a, MixedDatLegacyArg):
+        return (3, id(a.data), id(a.map_), a.access)
+    if isinstance(a, MixedMatLegacyArg):
+        return (4, id(a.data), id(a.maps[0]), id(a.maps[1]), a.access)
+    if isinstance(a, PassthroughArg):
+        return (5, a.data, repr(a.dtype))
+    return None
+
+
 def parloop(knl, *args, **kwargs):
     """Construct and execute a par_loop (pyop2/parloop.py:748-760)."""
-    if isinstance(knl, LocalKernel):
-        LegacyParloop(knl, *args, **kwargs)()
-    else:
+    if not isinstance(knl, LocalKernel):
         raise KernelTypeError
+    key = None
+    if args:
+        akeys = tuple(_arg_key(a) for a in args[1:])
+        if None not in akeys:
+            try:
+                key = (id(knl), id(knl.code), id(args[0]), akeys, tuple(sorted(kwargs.items())),
+                       tuple(configuration[k] for k in _CONFIG_KEYS))
+                hash(key)
+            except TypeError:      # an unhashable keyword value: no reuse
+                key = None
+    pl = None
+    if key is not None:
+        hit = _RECENT.get(key)
+        if hit is not None and hit[1] is knl and hit[2] is args[0]:
+            pl = hit[0]
+            _RECENT.move_to_end(key)
+            for a in pl._components:      # halo freezing can change between calls
+                if isinstance(a, DatLegacyArg) and a.data._halo_frozen and \
+                        a.data._frozen_access_mode != a.access:
+                    raise RuntimeError("Dats with frozen halos must always be accessed with "
+                                       "the same access mode")
+    if pl is None:
+        pl = LegacyParloop(knl, *args, **kwargs)
+        if key is not None:
+            _RECENT[key] = (pl, knl, args[0])
+            if len(_RECENT) > _RECENT_SIZE:
+                _RECENT.popitem(last=False)
+    pl()
+
+
+def run_once(knl, *args, **kwargs):
+    """Run a loop without keeping it for reuse."""
+    if not isinstance(knl, LocalKernel):
+        raise KernelTypeError
+    LegacyParloop(knl, *args, **kwargs)()
 
 
 def par_loop(*args, **kwargs):

@@ -273,7 +273,7 @@ class Dat(AbstractDat):
 
     def _op(self, other, op, opname):
         from pyop2_gb300.datatypes import as_cstr
-        from pyop2_gb300.parloop import par_loop
+        from pyop2_gb300.parloop import run_once as par_loop
         from pyop2_gb300.types.access import READ, WRITE
         o, scalar = self._other(other)
         t, to = as_cstr(self.dtype), as_cstr(o.dtype)
@@ -288,7 +288,7 @@ class Dat(AbstractDat):
 
     def _iop(self, other, op, opname):
         from pyop2_gb300.datatypes import as_cstr
-        from pyop2_gb300.parloop import par_loop
+        from pyop2_gb300.parloop import run_once as par_loop
         from pyop2_gb300.types.access import READ, RW
         o, scalar = self._other(other)
         t, to = as_cstr(self.dtype), as_cstr(o.dtype)
@@ -342,7 +342,7 @@ class Dat(AbstractDat):
 
     def __neg__(self):
         from pyop2_gb300.datatypes import as_cstr
-        from pyop2_gb300.parloop import par_loop
+        from pyop2_gb300.parloop import run_once as par_loop
         from pyop2_gb300.types.access import READ, WRITE
         t = as_cstr(self.dtype)
         k = self._kernel(("neg", self.cdim, t),
@@ -357,7 +357,7 @@ class Dat(AbstractDat):
         """Euclidean inner product over the owned entities (a Global INC
         reduction on the device)."""
         from pyop2_gb300.datatypes import as_cstr
-        from pyop2_gb300.parloop import par_loop
+        from pyop2_gb300.parloop import run_once as par_loop
         from pyop2_gb300.types.access import INC, READ
         from pyop2_gb300.types.glob import Global
         self._check_shape(other)

@@ -151,3 +151,37 @@ def test_profiling_regions(gpu_op2):
     assert summ["Parloop_cells_k"][0] == 3 and summ["Parloop_cells_k"][1] > 0
     assert summ["CreateSparsity"][0] == 1
     assert np.all(d.data_ro == 3)
+
+
+def test_repeated_par_loop_reuses_the_loop(gpu_op2):
+    """Calling par_loop again with the same kernel, set, data and modes reuses
+    the earlier loop; anything different builds a new one; results are those
+    of separate calls."""
+    from pyop2_gb300 import parloop as P
+    from pyop2_gb300.configuration import configuration
+    op2 = gpu_op2
+    cells, verts = op2.Set(50), op2.Set(20)
+    vals = (np.arange(150) % 20).reshape(50, 3)
+    m = op2.Map(cells, verts, 3, vals)
+    y = op2.Dat(verts, np.zeros(20))
+    k = op2.Kernel("static void k(double *y) { for (int i = 0; i < 3; ++i) y[i] += 1.0; }", "k")
+    P._RECENT.clear()
+    for _ in range(3):
+        op2.par_loop(k, cells, y(op2.INC, m))
+    assert len(P._RECENT) == 1
+    assert np.array_equal(y.data_ro, 3 * np.bincount(vals.reshape(-1), minlength=20))
+    y2 = op2.Dat(verts, np.zeros(20))
+    op2.par_loop(k, cells, y2(op2.INC, m))
+    assert len(P._RECENT) == 2
+    old = configuration["block_size"]
+    configuration["block_size"] = 128
+    try:
+        op2.par_loop(k, cells, y2(op2.INC, m))
+    finally:
+        configuration["block_size"] = old
+    assert len(P._RECENT) == 3
+    assert np.array_equal(y2.data_ro, 2 * np.bincount(vals.reshape(-1), minlength=20))
+    # halo freezing is checked on reuse too
+    with y.frozen_halo(op2.READ):
+        with pytest.raises(RuntimeError):
+            op2.par_loop(k, cells, y(op2.INC, m))
