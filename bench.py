@@ -575,6 +575,54 @@ def measure_prisms(op2, steps, warmup, n=256):
     return out
 
 
+def measure_small(op2, calls=500, with_cpu=True):
+    """The small 2D configuration (64^2 x 2 = 8,192 triangles, P1 action plus
+    an area Global): device-side it is a few microseconds, so this reports
+    the cost of a whole op2.par_loop call (validation, launch, bookkeeping)
+    and of a reused ParLoop, next to the oracle's sequential C wrapper on one
+    host core for the same loop."""
+    import torch
+    from pyop2_gb300 import workloads as W
+    p = W.build_p1_2d(op2)
+    for _ in range(20):
+        p["run"]()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        p["run"]()
+    torch.cuda.synchronize()
+    per_call = (time.perf_counter() - t0) / calls
+    pl = op2.ParLoop(p["kernel"], p["cells"], p["y"](op2.INC, p["c2v"]),
+                     p["X"](op2.READ, p["c2v"]), p["x"](op2.READ, p["c2v"]),
+                     p["area"](op2.INC))
+    pl.compute()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        pl.compute()
+    torch.cuda.synchronize()
+    per_compute = (time.perf_counter() - t0) / calls
+    C = p["cells"].size
+    out = {"workload": "p1_tri_laplace_action_64sq", "cells": C,
+           "par_loop_us_per_call": per_call * 1e6, "parloop_compute_us_per_call": per_compute * 1e6,
+           "par_loop_cells_per_s": C / per_call}
+    if with_cpu:
+        from oracle import op2 as O
+        o = W.build_p1_2d(O)
+        loop = O.ParLoop(o["kernel"], o["cells"], o["y"](O.INC, o["c2v"]),
+                         o["X"](O.READ, o["c2v"]), o["x"](O.READ, o["c2v"]),
+                         o["area"](O.INC), profile="timing")
+        best = None
+        for _ in range(20):
+            t0 = time.perf_counter()
+            loop.compute()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        out["cpu_1core_us_per_loop"] = best * 1e6
+        out["cpu_1core_cells_per_s"] = C / best
+    return out
+
+
 def measure_data_path(op2, p, steps, warmup):
     """Loops with (almost) no arithmetic on the benchmark mesh, to show the
     wrapper's memory path against HBM where FP64 is not the limit: a direct
@@ -740,6 +788,7 @@ def run_ours(args):
         strategies["random_permutation"] = measure_strategies(op2, pr, 5, 2)
         del pr
     data_path = measure_data_path(op2, p, 10, 3) if not args.skip_extras else None
+    small = measure_small(op2, with_cpu=not args.no_cpu_baseline) if not args.skip_extras else None
     sparsity = measure_sparsity_assembly(op2, p, 5, 3) if not args.skip_extras else None
     adjoint = measure_adjoint(op2, max(args.steps, 5), 3) if not args.skip_extras else None
     batch = measure_batch(op2, 5, 3) if not args.skip_extras else None
@@ -787,6 +836,7 @@ def run_ours(args):
         "batch": batch,
         "prisms": prisms,
         "data_path": data_path,
+        "small_2d": small,
         "gpu_launches": args.steps,
         "clocks": clocks,
         "wall_s_timed": wall,
