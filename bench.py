@@ -475,6 +475,30 @@ def _time_sparsity_build(dsets, pairs, reps=3):
     return best, sp
 
 
+def _time_spmv(op2, A, x, steps, warmup):
+    """Mean time of y = A x (ms, CUDA events over `steps` back-to-back
+    products) and the bandwidth it implies over the compulsory bytes: block
+    values, column indices, row pointers, x and y once each."""
+    import torch
+    y = op2.Dat(A.sparsity.dsets[0])
+    for _ in range(warmup):
+        A.mult(x, y)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        A.mult(x, y)
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    sp = A.sparsity
+    rdim, cdim = A.dims[0][0]
+    nrows, ncols = sp.dsets[0].size, sp.dsets[1].size
+    nbytes = (sp.nblocks * (rdim * cdim * 8 + 4) + (nrows + 1) * 8
+              + ncols * cdim * 8 + nrows * rdim * 8)
+    return ms, nbytes / (ms * 1e-3) / 1e9
+
+
 def measure_sparsity_assembly(op2, p, steps, warmup):
     """Configuration 2b on the benchmark mesh: GPU sparsity build (block CSR,
     bit-exact pattern), CSR assembly of the 4x4 element matrices and SpMV."""
@@ -486,23 +510,12 @@ def measure_sparsity_assembly(op2, p, steps, warmup):
     asm = op2.ParLoop(op2.Kernel(W.P1_3D_LAPLACE_MATRIX, "p1_laplace_3d_mat"), p["cells"],
                       A(op2.INC, (p["c2v"], p["c2v"])), p["X"](op2.READ, p["c2v"]))
     t_asm = _time_loop(asm, steps, warmup)
-    y = op2.Dat(p["verts"])
-    for _ in range(warmup):
-        A.mult(p["x"], y)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(steps):
-        A.mult(p["x"], y)
-    e1.record()
-    e1.synchronize()
-    t_spmv = e0.elapsed_time(e1) / steps
+    t_spmv, gbs = _time_spmv(op2, A, p["x"], max(steps, 5), max(warmup, 3))
     C = p["cells"].size
     nnz = sp.nblocks
     out = {"workload": "p1_tet_laplace_128cube_csr", "nnz": nnz, "rows": p["verts"].size,
            "sparsity_build_ms": t_sp, "assembly_ms": t_asm,
-           "assembly_cells_per_s": C / (t_asm * 1e-3), "spmv_ms": t_spmv,
-           "spmv_gbs": (nnz * 12 + p["verts"].size * 8 * 3) / (t_spmv * 1e-3) / 1e9}
+           "assembly_cells_per_s": C / (t_asm * 1e-3), "spmv_ms": t_spmv, "spmv_gbs": gbs}
     del A, sp
     return out
 
@@ -563,6 +576,8 @@ def measure_prisms(op2, steps, warmup, n=256):
     asm = op2.ParLoop(op2.Kernel(W.PRISM_ELASTICITY_MATRIX, "prism_elasticity_mat"), cells,
                       A(op2.INC, (c2n, c2n)), p["X"](op2.READ, c2n), p["L"](op2.READ, c2c))
     t_asm = _time_loop(asm, 2, 1)
+    xs = op2.Dat(nodes ** 3, np.random.default_rng(0).uniform(-1, 1, (p["nnodes"], 3)))
+    t_spmv, gbs = _time_spmv(op2, A, xs, 5, 3)
     C = p["ncell"]
     out = {"workload": "prism_elasticity_%dx%dx64_8rhs" % (n, n), "cells": C, "nodes": p["nnodes"],
            "rhs": NR, "action_ms": t_act, "adjoint_ms": t_adj,
@@ -570,7 +585,8 @@ def measure_prisms(op2, steps, warmup, n=256):
            "action_cell_rhs_per_s": C * NR / (t_act * 1e-3),
            "adjoint_over_action": t_adj / t_act,
            "baij_blocks": sp.nblocks, "sparsity_build_ms": t_sp,
-           "assembly_ms": t_asm, "values_gb": sp.nblocks * 9 * 8 / 1e9}
+           "assembly_ms": t_asm, "values_gb": sp.nblocks * 9 * 8 / 1e9,
+           "spmv_ms": t_spmv, "spmv_gbs": gbs}
     del A, sp
     return out
 

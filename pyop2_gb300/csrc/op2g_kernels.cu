@@ -653,36 +653,130 @@ __global__ void k_set_diag(op2g_bcsr m, const int *__restrict__ rows, long long 
     }
 }
 
-__global__ void k_spmv(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
-    const long long nr = m.nrows * m.rdim;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    const int bs = m.rdim * m.cdim;
-    for (long long row = blockIdx.x * (long long)blockDim.x + threadIdx.x; row < nr; row += stride) {
-        const long long br = row / m.rdim;
-        const int ri = (int)(row - br * m.rdim);
-        double acc = 0.0;
-        for (long long q = m.rowptr[br]; q < m.rowptr[br + 1]; ++q) {
-            const long long c0 = (long long)m.colidx[q] * m.cdim;
-            const double *v = m.values + q * bs + ri * m.cdim;
-            for (int cj = 0; cj < m.cdim; ++cj) acc += v[cj] * x[c0 + cj];
+// y = A x, one CTA of SPMV_T threads per SPMV_T / R consecutive block rows,
+// thread (block row, ri) owning dof row ri of its block row.  The CTA walks
+// the values of its block rows (contiguous in block-CSR) in tiles of whole
+// blocks.  Load phase: every thread issues up to SPMV_PER independent,
+// coalesced loads of values and column indices, then the gathers of x, and
+// stages value and x side by side in shared memory.  Sum phase: each thread
+// runs acc = fma(value, x, acc) over the entries of its own row in the tile,
+// in column order, so the result does not depend on the launch shape.
+// GB300 issues FP64 at 2 thread-instructions per clock per SM, so one FMA
+// per entry (no separate multiply and add, no shuffle reductions) keeps the
+// FP64 work of a 1x1 product below its HBM time; issuing many loads per
+// thread before using any of them is what reaches HBM bandwidth on rows of
+// ~15 entries.  RT/CT = block shape when known at compile time, 0 = taken
+// from the descriptor.
+constexpr int SPMV_T = 256, SPMV_PER = 8, SPMV_TILE = SPMV_T * SPMV_PER;
+
+template <int RT, int CT>
+__global__ void __launch_bounds__(SPMV_T, RT * CT == 1 ? 4 : 3)
+    k_spmv_tile(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
+    extern __shared__ double stage[];
+    const int R = RT ? RT : m.rdim, C = CT ? CT : m.cdim;
+    const int BS = R * C;
+    const int QT = SPMV_TILE / BS;  // blocks per tile
+    const int NB = SPMV_T / R;      // block rows per CTA
+    double *sv = stage, *sx = stage + QT * BS;
+    const int tid = threadIdx.x;
+    const int lb = tid / R, ri = tid - lb * R;
+    for (long long br0 = blockIdx.x * (long long)NB; br0 < m.nrows;
+         br0 += (long long)gridDim.x * NB) {
+        const long long brN = br0 + NB < m.nrows ? br0 + NB : m.nrows;
+        const long long br = br0 + lb;
+        const bool own = lb < NB && br < brN;
+        long long q0 = 0, q1 = 0;
+        if (own) {
+            q0 = __ldg(m.rowptr + br);
+            q1 = __ldg(m.rowptr + br + 1);
         }
-        y[row] = acc;
+        const long long qb = __ldg(m.rowptr + brN);
+        double acc = 0.0;
+        for (long long qa = __ldg(m.rowptr + br0); qa < qb; qa += QT) {
+            const long long qe = qa + QT < qb ? qa + QT : qb;
+            const int n = (int)((qe - qa) * BS);
+            const double *vals = m.values + qa * BS;
+            const int *cols = m.colidx + qa;
+            __syncthreads();  // the previous tile has been summed
+            // all loads of the tile in flight before the first use
+            double v[SPMV_PER], xv[SPMV_PER];
+            int xi[SPMV_PER];  // ncols * C < 2^31, checked by the launcher
+#pragma unroll
+            for (int k = 0; k < SPMV_PER; ++k) {
+                const int i = tid + k * SPMV_T;
+                if (i < n) {
+                    const int dq = i / BS, w = i - dq * BS;
+                    v[k] = __ldg(vals + i);
+                    xi[k] = __ldg(cols + dq) * C + (w - (w / C) * C);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < SPMV_PER; ++k)
+                if (tid + k * SPMV_T < n) xv[k] = __ldg(x + xi[k]);
+#pragma unroll
+            for (int k = 0; k < SPMV_PER; ++k) {
+                const int i = tid + k * SPMV_T;
+                if (i < n) {
+                    sv[i] = v[k];
+                    sx[i] = xv[k];
+                }
+            }
+            __syncthreads();
+            if (own) {
+                const long long s = q0 > qa ? q0 : qa, e = q1 < qe ? q1 : qe;
+                for (long long q = s; q < e; ++q) {
+                    const int o = (int)(q - qa) * BS + ri * C;
+                    for (int cj = 0; cj < C; ++cj) acc = fma(sv[o + cj], sx[o + cj], acc);
+                }
+            }
+        }
+        if (own) y[br * R + ri] = acc;
     }
 }
 
-__global__ void k_spmv_t(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
+// Any other block shape: a group of G lanes per dof row, lanes strided over
+// the row's blocks.
+template <int G>
+__global__ void k_spmv_rows(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
+    constexpr int PER_WARP = 32 / G;
+    const int lane = threadIdx.x & 31;
+    const int sub = lane % G;
     const long long nr = m.nrows * m.rdim;
-    const long long stride = (long long)gridDim.x * blockDim.x;
     const int bs = m.rdim * m.cdim;
-    for (long long row = blockIdx.x * (long long)blockDim.x + threadIdx.x; row < nr; row += stride) {
-        const long long br = row / m.rdim;
-        const int ri = (int)(row - br * m.rdim);
-        const double xv = x[row];
-        if (xv == 0.0) continue;
-        for (long long q = m.rowptr[br]; q < m.rowptr[br + 1]; ++q) {
-            const long long c0 = (long long)m.colidx[q] * m.cdim;
-            const double *v = m.values + q * bs + ri * m.cdim;
-            for (int cj = 0; cj < m.cdim; ++cj) atomicAdd(&y[c0 + cj], v[cj] * xv);
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long base = warp * PER_WARP; base < nr; base += nwarps * PER_WARP) {
+        const long long row = base + lane / G;
+        double acc = 0.0;
+        if (row < nr) {
+            const long long br = row / m.rdim;
+            const int ri = (int)(row - br * m.rdim);
+            for (long long q = m.rowptr[br] + sub; q < m.rowptr[br + 1]; q += G) {
+                const long long c0 = (long long)m.colidx[q] * m.cdim;
+                const double *v = m.values + q * bs + ri * m.cdim;
+                for (int cj = 0; cj < m.cdim; ++cj) acc += v[cj] * x[c0 + cj];
+            }
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (row < nr && sub == 0) y[row] = acc;
+    }
+}
+
+// y += A^T x (y zeroed by the caller): a warp per block row walks its values
+// with coalesced loads and adds each product into y with an atomic.
+__global__ void k_spmv_t(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const int bs = m.rdim * m.cdim;
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long br = warp; br < m.nrows; br += nwarps) {
+        const long long t1 = m.rowptr[br + 1] * bs;
+        for (long long t = m.rowptr[br] * bs + lane; t < t1; t += 32) {
+            const long long q = t / bs;
+            const int w = (int)(t - q * bs);
+            const int ri = w / m.cdim, cj = w - ri * m.cdim;
+            atomicAdd(&y[(long long)m.colidx[q] * m.cdim + cj], m.values[t] * x[br * m.rdim + ri]);
         }
     }
 }
@@ -730,10 +824,26 @@ op2g_status op2g_mat_spmv(const op2g_bcsr *m, const double *x, double *y, int32_
     if (s != OP2G_OK) return s;
     const long long nr = m->nrows * m->rdim;
     if (nr <= 0) return OP2G_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int r = m->rdim, c = m->cdim;
     if (transpose)
-        k_spmv_t<<<grid_for(nr, 256), 256, 0, (cudaStream_t)stream>>>(*m, x, y);
-    else
-        k_spmv<<<grid_for(nr, 256), 256, 0, (cudaStream_t)stream>>>(*m, x, y);
+        k_spmv_t<<<grid_for(m->nrows * 32, 256), 256, 0, st>>>(*m, x, y);
+    else if (r > SPMV_T || r * c > SPMV_TILE || m->ncols * c > INT_MAX)
+        k_spmv_rows<8><<<grid_for(nr * 8, 256), 256, 0, st>>>(*m, x, y);
+    else {
+        // tiles of whole blocks: (SPMV_TILE / bs) * bs values and x entries
+        const size_t smem = 2 * (size_t)(SPMV_TILE / (r * c)) * (r * c) * sizeof(double);
+        const long long ctas = (m->nrows + SPMV_T / r - 1) / (SPMV_T / r);
+        const unsigned g = grid_for(ctas * SPMV_T, SPMV_T);
+        if (r == 1 && c == 1)
+            k_spmv_tile<1, 1><<<g, SPMV_T, smem, st>>>(*m, x, y);
+        else if (r == 2 && c == 2)
+            k_spmv_tile<2, 2><<<g, SPMV_T, smem, st>>>(*m, x, y);
+        else if (r == 3 && c == 3)
+            k_spmv_tile<3, 3><<<g, SPMV_T, smem, st>>>(*m, x, y);
+        else
+            k_spmv_tile<0, 0><<<g, SPMV_T, smem, st>>>(*m, x, y);
+    }
     CK(cudaGetLastError());
     return OP2G_OK;
 }

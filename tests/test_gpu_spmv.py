@@ -1,0 +1,58 @@
+"""Mat.mult (y = A x and y = A^T x) on assembled block-CSR matrices of every
+block shape the kernels specialise (1x1, 2x2, 3x3) and of shapes they do not
+(2x3, 1x2, 4x4), against scipy's product of the same assembled matrix."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(1, 1), (2, 2), (3, 3), (2, 3), (1, 2), (4, 4)]
+
+
+def _assembled(op2, r, c, seed):
+    rng = np.random.default_rng(seed)
+    ncell, nrow, ncol, ar, ac = 600, 257, 193, 3, 4
+    cells = op2.Set(ncell)
+    rows = op2.Set(nrow)
+    cols = op2.Set(ncol)
+    # the last 20 rows are never reached: empty block rows
+    rmap = op2.Map(cells, rows, ar, rng.integers(0, nrow - 20, (ncell, ar)).astype(np.int32))
+    cmap = op2.Map(cells, cols, ac, rng.integers(0, ncol, (ncell, ac)).astype(np.int32))
+    sp = op2.Sparsity((rows ** r, cols ** c), [(rmap, cmap, None)])
+    A = op2.Mat(sp)
+    w = op2.Dat(cells, rng.uniform(0.5, 1.5, ncell))
+    code = """
+void elem(double A[%(R)d][%(C)d], const double *w) {
+  for (int i = 0; i < %(R)d; ++i)
+    for (int j = 0; j < %(C)d; ++j)
+      A[i][j] += w[0] * (1.0 + i) / (2.0 + j) - 0.25 * (i == j);
+}""" % {"R": ar * r, "C": ac * c}
+    op2.par_loop(op2.Kernel(code, "elem"), cells, A(op2.INC, (rmap, cmap)), w(op2.READ))
+    A.assemble()
+    return A, rows ** r, cols ** c, rng
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=["%dx%d" % s for s in SHAPES])
+def test_mult_matches_scipy(gpu_op2, shape):
+    op2 = gpu_op2
+    r, c = shape
+    A, drows, dcols, rng = _assembled(op2, r, c, seed=11 * r + c)
+    S = A.to_scipy().tocsr()
+    assert S.shape == (257 * r, 193 * c)
+    x = op2.Dat(dcols, rng.uniform(-1, 1, (193, c)) if c > 1 else rng.uniform(-1, 1, 193))
+    y = op2.Dat(drows)
+    A.mult(x, y)
+    ref = S @ x.data_ro.reshape(-1)
+    got = y.data_ro.reshape(-1)
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+    assert np.all(got[-20 * r:] == 0.0)
+    # the same product twice is bitwise identical
+    y2 = op2.Dat(drows)
+    A.mult(x, y2)
+    assert np.array_equal(y2.data_ro, y.data_ro)
+    # transpose
+    xt = op2.Dat(drows, rng.uniform(-1, 1, (257, r)) if r > 1 else rng.uniform(-1, 1, 257))
+    yt = op2.Dat(dcols)
+    A.mult(xt, yt, transpose=True)
+    reft = S.T @ xt.data_ro.reshape(-1)
+    assert np.abs(yt.data_ro.reshape(-1) - reft).max() <= 1e-12 * np.abs(reft).max()
