@@ -653,66 +653,55 @@ __global__ void k_set_diag(op2g_bcsr m, const int *__restrict__ rows, long long 
     }
 }
 
-// y = A x, one CTA of SPMV_T threads per SPMV_T / R consecutive block rows,
-// thread (block row, ri) owning dof row ri of its block row.  The CTA walks
-// the values of its block rows (contiguous in block-CSR) in tiles of whole
-// blocks.  Load phase: every thread issues up to SPMV_PER independent,
-// coalesced loads of values and column indices, then the gathers of x, and
-// stages value and x side by side in shared memory.  Sum phase: each thread
-// runs acc = fma(value, x, acc) over the entries of its own row in the tile,
-// in column order, so the result does not depend on the launch shape.
-// GB300 issues FP64 at 2 thread-instructions per clock per SM, so one FMA
-// per entry (no separate multiply and add, no shuffle reductions) keeps the
-// FP64 work of a 1x1 product below its HBM time; issuing many loads per
-// thread before using any of them is what reaches HBM bandwidth on rows of
-// ~15 entries.  RT/CT = block shape when known at compile time, 0 = taken
-// from the descriptor.
+// y = A x on block-CSR.  GB300 issues FP64 at 2 thread-instructions per
+// clock per SM, so even a 1x1 product has as much FP64 time (one FMA per
+// entry) as HBM time; both kernels below stream the matrix with coalesced
+// loads into shared memory and spend one FMA per entry, summing each row in
+// a fixed order so that repeated products are bitwise identical.
 constexpr int SPMV_T = 256, SPMV_PER = 8, SPMV_TILE = SPMV_T * SPMV_PER;
 
-template <int RT, int CT>
-__global__ void __launch_bounds__(SPMV_T, RT * CT == 1 ? 4 : 3)
-    k_spmv_tile(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
-    extern __shared__ double stage[];
-    const int R = RT ? RT : m.rdim, C = CT ? CT : m.cdim;
-    const int BS = R * C;
-    const int QT = SPMV_TILE / BS;  // blocks per tile
-    const int NB = SPMV_T / R;      // block rows per CTA
-    double *sv = stage, *sx = stage + QT * BS;
+// 1x1 blocks (CSR).  A CTA owns SPMV_T consecutive rows, one per thread, and
+// walks their entries (contiguous) in tiles of SPMV_TILE: every thread
+// issues SPMV_PER loads of values and column indices, then the gathers of
+// x, stages value and x side by side in shared memory, and after a barrier
+// runs acc = fma(value, x, acc) over its own row's entries in column order.
+// At ~15 entries per row a CTA's rows span two tiles; 32 KB of shared
+// memory and 64 registers leave 4 CTAs per SM to overlap one another's load
+// and sum phases (measured faster than the pipelined kernel below, whose
+// double buffer allows only 3).
+__global__ void __launch_bounds__(SPMV_T, 4)
+    k_spmv_csr(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
+    __shared__ double sv[SPMV_TILE], sx[SPMV_TILE];
     const int tid = threadIdx.x;
-    const int lb = tid / R, ri = tid - lb * R;
-    for (long long br0 = blockIdx.x * (long long)NB; br0 < m.nrows;
-         br0 += (long long)gridDim.x * NB) {
-        const long long brN = br0 + NB < m.nrows ? br0 + NB : m.nrows;
-        const long long br = br0 + lb;
-        const bool own = lb < NB && br < brN;
+    for (long long r0 = blockIdx.x * (long long)SPMV_T; r0 < m.nrows;
+         r0 += (long long)gridDim.x * SPMV_T) {
+        const long long rN = r0 + SPMV_T < m.nrows ? r0 + SPMV_T : m.nrows;
+        const long long row = r0 + tid;
+        const bool own = row < rN;
         long long q0 = 0, q1 = 0;
         if (own) {
-            q0 = __ldg(m.rowptr + br);
-            q1 = __ldg(m.rowptr + br + 1);
+            q0 = __ldg(m.rowptr + row);
+            q1 = __ldg(m.rowptr + row + 1);
         }
-        const long long qb = __ldg(m.rowptr + brN);
+        const long long qb = __ldg(m.rowptr + rN);
         double acc = 0.0;
-        for (long long qa = __ldg(m.rowptr + br0); qa < qb; qa += QT) {
-            const long long qe = qa + QT < qb ? qa + QT : qb;
-            const int n = (int)((qe - qa) * BS);
-            const double *vals = m.values + qa * BS;
-            const int *cols = m.colidx + qa;
+        for (long long qa = __ldg(m.rowptr + r0); qa < qb; qa += SPMV_TILE) {
+            const int n = (int)(qa + SPMV_TILE < qb ? SPMV_TILE : qb - qa);
             __syncthreads();  // the previous tile has been summed
             // all loads of the tile in flight before the first use
             double v[SPMV_PER], xv[SPMV_PER];
-            int xi[SPMV_PER];  // ncols * C < 2^31, checked by the launcher
+            int ci[SPMV_PER];
 #pragma unroll
             for (int k = 0; k < SPMV_PER; ++k) {
                 const int i = tid + k * SPMV_T;
                 if (i < n) {
-                    const int dq = i / BS, w = i - dq * BS;
-                    v[k] = __ldg(vals + i);
-                    xi[k] = __ldg(cols + dq) * C + (w - (w / C) * C);
+                    v[k] = __ldg(m.values + qa + i);
+                    ci[k] = __ldg(m.colidx + qa + i);
                 }
             }
 #pragma unroll
             for (int k = 0; k < SPMV_PER; ++k)
-                if (tid + k * SPMV_T < n) xv[k] = __ldg(x + xi[k]);
+                if (tid + k * SPMV_T < n) xv[k] = __ldg(x + ci[k]);
 #pragma unroll
             for (int k = 0; k < SPMV_PER; ++k) {
                 const int i = tid + k * SPMV_T;
@@ -723,14 +712,158 @@ __global__ void __launch_bounds__(SPMV_T, RT * CT == 1 ? 4 : 3)
             }
             __syncthreads();
             if (own) {
-                const long long s = q0 > qa ? q0 : qa, e = q1 < qe ? q1 : qe;
-                for (long long q = s; q < e; ++q) {
-                    const int o = (int)(q - qa) * BS + ri * C;
-                    for (int cj = 0; cj < C; ++cj) acc = fma(sv[o + cj], sx[o + cj], acc);
+                const long long s0 = q0 > qa ? q0 : qa, e0 = q1 < qa + n ? q1 : qa + n;
+                for (int o = (int)(s0 - qa); o < (int)(e0 - qa); ++o) acc = fma(sv[o], sx[o], acc);
+            }
+        }
+        if (own) y[row] = acc;
+    }
+}
+
+// Blocks of R x C > 1 entries: a 3x3 block row holds ~190 entries, so one
+// thread per dof row would leave most lanes of a tile idle; instead S lanes
+// share a dof row and the next tile's loads overlap the current sums.
+//
+// Work: a CTA takes slabs of NB consecutive block rows (grid-stride); NB is
+// chosen from the mean row length so that a slab's entries fill about 90 %
+// of one tile (SPMV_TILE entries, whole blocks), capped at one block row
+// per thread.  A slab longer than a tile is walked in several tiles.
+// Load: every thread issues up to SPMV_PER loads of values and column
+// indices for the NEXT tile before summing the current one; the x gathers
+// follow once the column indices are in; values and x are staged side by
+// side in shared memory (double-buffered, one barrier per tile).
+// Sum: S lanes (a power of two, S * NB * R <= SPMV_T) per dof row; lane s
+// runs acc = fma(value, x, acc) over entries s, s + S, ... of its row in
+// each tile of the slab (column order), and at the end of the slab the S
+// partial sums are combined by butterfly shuffles.  NB and S depend only
+// on the matrix.  RT/CT = block shape when known at compile time, 0 = from
+// the descriptor.
+template <int RT, int CT>
+__global__ void __launch_bounds__(SPMV_T, 3)
+    k_spmv_bsr(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
+    extern __shared__ double stage[];  // [2][2][QT * BS]: values | x, two buffers
+    const int R = RT ? RT : m.rdim, C = CT ? CT : m.cdim;
+    const int BS = R * C;
+    const int QT = SPMV_TILE / BS;  // blocks per tile
+    const int tid = threadIdx.x;
+    int NB = SPMV_T / R;
+    {
+        const long long nnzb = __ldg(m.rowptr + m.nrows);
+        if (nnzb > 0) {
+            const long long fit = (long long)QT * m.nrows * 9 / (nnzb * 10);
+            if (fit < NB) NB = fit < 1 ? 1 : (int)fit;
+        }
+    }
+    int S = 1;
+    while (S < 32 && 2 * S * NB * R <= SPMV_T) S <<= 1;
+    const int grp = tid / S, lane_s = tid - grp * S;
+    const bool has_row = grp < NB * R;
+    const int lb = grp / R, ri = grp - lb * R;
+
+    // tile cursor: slab [br0, brN) with entries [qs, qz) blocks; tile [qa, qe)
+    long long br0 = blockIdx.x * (long long)NB;
+    if (br0 >= m.nrows) return;
+    const long long step = (long long)gridDim.x * NB;
+    long long brN = br0 + NB < m.nrows ? br0 + NB : m.nrows;
+    long long qz = __ldg(m.rowptr + brN);
+    long long qa = __ldg(m.rowptr + br0);
+    long long qe = qa + QT < qz ? qa + QT : qz;
+
+    double v[SPMV_PER];
+    int ci[SPMV_PER];
+    auto issue = [&](long long qa_, long long qe_) {
+        const int n = (int)((qe_ - qa_) * BS);
+        const double *vals = m.values + qa_ * BS;
+        const int *cols = m.colidx + qa_;
+#pragma unroll
+        for (int k = 0; k < SPMV_PER; ++k) {
+            const int i = tid + k * SPMV_T;
+            if (i < n) {
+                v[k] = __ldg(vals + i);
+                ci[k] = __ldg(cols + i / BS);
+            }
+        }
+    };
+    issue(qa, qe);
+
+    // this thread's dof row in the current slab
+    long long q0 = 0, q1 = 0;
+    bool own = has_row && br0 + lb < brN;
+    if (own) {
+        q0 = __ldg(m.rowptr + br0 + lb);
+        q1 = __ldg(m.rowptr + br0 + lb + 1);
+    }
+    double acc = 0.0;
+    int buf = 0;
+    for (;;) {
+        // stage the tile whose loads are in flight
+        {
+            const int n = (int)((qe - qa) * BS);
+            double *sv = stage + buf * 2 * QT * BS, *sx = sv + QT * BS;
+            double xv[SPMV_PER];
+#pragma unroll
+            for (int k = 0; k < SPMV_PER; ++k) {
+                const int i = tid + k * SPMV_T;
+                if (i < n) {
+                    const int w = i - (i / BS) * BS;
+                    xv[k] = __ldg(x + ci[k] * C + (w - (w / C) * C));
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < SPMV_PER; ++k) {
+                const int i = tid + k * SPMV_T;
+                if (i < n) {
+                    sv[i] = v[k];
+                    sx[i] = xv[k];
                 }
             }
         }
-        if (own) y[br * R + ri] = acc;
+        __syncthreads();  // tile staged; the buffer staged next was summed before this barrier
+        // advance the cursor and put the next tile's loads in flight
+        const long long cur_qa = qa, cur_qe = qe;
+        const bool slab_end = qe >= qz;
+        long long nbr0 = br0;
+        bool more = true;
+        if (!slab_end) {
+            qa = qe;
+            qe = qa + QT < qz ? qa + QT : qz;
+        } else {
+            nbr0 = br0 + step;
+            more = nbr0 < m.nrows;
+            if (more) {
+                const long long nbrN = nbr0 + NB < m.nrows ? nbr0 + NB : m.nrows;
+                qz = __ldg(m.rowptr + nbrN);
+                qa = __ldg(m.rowptr + nbr0);
+                qe = qa + QT < qz ? qa + QT : qz;
+            }
+        }
+        if (more) issue(qa, qe);
+        // sum the staged tile
+        if (own) {
+            const double *sv = stage + buf * 2 * QT * BS, *sx = sv + QT * BS;
+            const long long s0 = q0 > cur_qa ? q0 : cur_qa, e0 = q1 < cur_qe ? q1 : cur_qe;
+            const int len = (int)(e0 - s0) * C;
+            const int base = (int)(s0 - cur_qa) * BS + ri * C;
+            for (int j = lane_s; j < len; j += S) {
+                const int dq = j / C;
+                const int o = base + dq * BS + (j - dq * C);
+                acc = fma(sv[o], sx[o], acc);
+            }
+        }
+        if (slab_end) {
+            for (int o = S >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (own && lane_s == 0) y[(br0 + lb) * R + ri] = acc;
+            acc = 0.0;
+            if (!more) break;
+            br0 = nbr0;
+            brN = br0 + NB < m.nrows ? br0 + NB : m.nrows;
+            own = has_row && br0 + lb < brN;
+            if (own) {
+                q0 = __ldg(m.rowptr + br0 + lb);
+                q1 = __ldg(m.rowptr + br0 + lb + 1);
+            }
+        }
+        buf ^= 1;
     }
 }
 
@@ -788,6 +921,23 @@ unsigned grid_for(long long n, int bs) {
     return (unsigned)(g < 1 ? 1 : g);
 }
 
+// Launch k_spmv_bsr with more than the default 48 KB of dynamic shared
+// memory (the attribute is set once per instantiation and size).
+template <int RT, int CT>
+cudaError_t spmv_launch(unsigned grid, size_t smem, cudaStream_t st, const op2g_bcsr &m,
+                        const double *x, double *y) {
+    static size_t granted = 0;
+    if (smem > granted) {
+        cudaError_t e = cudaFuncSetAttribute(k_spmv_bsr<RT, CT>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        granted = smem;
+    }
+    k_spmv_bsr<RT, CT><<<grid, SPMV_T, smem, st>>>(m, x, y);
+    return cudaGetLastError();
+}
+
 op2g_status check_bcsr(const op2g_bcsr *m) {
     if (!m || !m->rowptr || !m->values || m->rdim <= 0 || m->cdim <= 0 || m->nrows < 0)
         return op2g::fail(OP2G_ERR_INVALID, "bad block-CSR descriptor");
@@ -830,19 +980,21 @@ op2g_status op2g_mat_spmv(const op2g_bcsr *m, const double *x, double *y, int32_
         k_spmv_t<<<grid_for(m->nrows * 32, 256), 256, 0, st>>>(*m, x, y);
     else if (r > SPMV_T || r * c > SPMV_TILE || m->ncols * c > INT_MAX)
         k_spmv_rows<8><<<grid_for(nr * 8, 256), 256, 0, st>>>(*m, x, y);
+    else if (r == 1 && c == 1)
+        k_spmv_csr<<<grid_for(m->nrows, SPMV_T), SPMV_T, 0, st>>>(*m, x, y);
     else {
-        // tiles of whole blocks: (SPMV_TILE / bs) * bs values and x entries
-        const size_t smem = 2 * (size_t)(SPMV_TILE / (r * c)) * (r * c) * sizeof(double);
+        // two buffers of (SPMV_TILE / bs) * bs values and x entries
+        const size_t smem = 4 * (size_t)(SPMV_TILE / (r * c)) * (r * c) * sizeof(double);
         const long long ctas = (m->nrows + SPMV_T / r - 1) / (SPMV_T / r);
         const unsigned g = grid_for(ctas * SPMV_T, SPMV_T);
-        if (r == 1 && c == 1)
-            k_spmv_tile<1, 1><<<g, SPMV_T, smem, st>>>(*m, x, y);
-        else if (r == 2 && c == 2)
-            k_spmv_tile<2, 2><<<g, SPMV_T, smem, st>>>(*m, x, y);
+        cudaError_t e;
+        if (r == 2 && c == 2)
+            e = spmv_launch<2, 2>(g, smem, st, *m, x, y);
         else if (r == 3 && c == 3)
-            k_spmv_tile<3, 3><<<g, SPMV_T, smem, st>>>(*m, x, y);
+            e = spmv_launch<3, 3>(g, smem, st, *m, x, y);
         else
-            k_spmv_tile<0, 0><<<g, SPMV_T, smem, st>>>(*m, x, y);
+            e = spmv_launch<0, 0>(g, smem, st, *m, x, y);
+        CK(e);
     }
     CK(cudaGetLastError());
     return OP2G_OK;

@@ -569,7 +569,10 @@ class Mat(DataCarrier):
         if self._mixed and self._sparsity.nested:
             for b in self:
                 b.assemble()
-        self._check_err()
+        elif self.assembly_state != Mat.ASSEMBLED:
+            # only a write since the last assembly can have set the error
+            # word, so an assembled matrix is not synchronised with again
+            self._check_err()
         self.change_assembly_state(Mat.ASSEMBLED)
 
     def _assemble_owner(self):
