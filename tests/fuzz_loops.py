@@ -315,3 +315,253 @@ def run_extruded(op2, spec):
                  iteration_region=getattr(op2, spec["region"]),
                  pass_layer_arg=spec["layer_arg"])
     return _results(objs, spec)
+
+
+# ------------------------------------------------------------------ matrices
+def make_mat_spec(seed):
+    """A random sparsity and its assembly: 1-3 (row map, column map) pairs
+    over one iteration set (flat, or extruded under random iteration
+    regions), block shapes rdim x cdim in 1..3, square spaces (diagonal
+    entries added) or rectangular ones, map entries sometimes -1 (ignored by
+    the pattern and by insertion).  Element matrices are integer-valued, so
+    the assembled values and the product with an integer x are exact."""
+    rng = np.random.default_rng(20_000 + seed)
+    extruded = bool(rng.random() < 0.5)
+    square = bool(rng.random() < 0.5)
+    rdim = int(rng.integers(1, 4))
+    cdim = rdim if square else int(rng.integers(1, 4))
+    nit = int(rng.integers(0, 16 if extruded else 120))
+    nr = int(rng.integers(1, 12 if extruded else 60))
+    nc = nr if square else int(rng.integers(1, 12 if extruded else 60))
+    spec = {"seed": 20_000 + seed, "extruded": extruded, "square": square, "rdim": rdim,
+            "cdim": cdim, "nit": nit, "nr": nr, "nc": nc,
+            "block_sparse": bool(rng.random() < 0.5)}
+    if extruded:
+        kind = rng.choice(["constant", "variable", "periodic"])
+        if kind == "variable":
+            bottom = rng.integers(0, 3, nit)
+            layers = np.stack([bottom, bottom + rng.integers(2, LTOP - 1, nit)], axis=1)
+            spec["layers"] = np.minimum(layers, LTOP).astype(np.int32)
+        else:
+            spec["layers"] = int(rng.integers(2, LTOP + 1))
+        spec["periodic"] = kind == "periodic"
+
+    def a_map(n_to):
+        a = int(rng.integers(1, 5))
+        v = rng.integers(0, n_to, (nit, a))
+        if extruded:
+            v = v * LNODES + 1
+        elif rng.random() < 0.25 and v.size:
+            # negative entries (flat maps only: a layer offset would move
+            # them back into range)
+            v[rng.random(v.shape) < 0.2] = -1
+        m = {"arity": a, "values": v.astype(np.int32)}
+        if extruded:
+            m["offset"] = rng.integers(0, 2, a).astype(np.int32)
+            if spec["periodic"]:
+                m["offset_quotient"] = rng.integers(0, 2, a).astype(np.int32)
+        return m
+
+    rmaps = [a_map(nr) for _ in range(int(rng.integers(1, 3)))]
+    cmaps = rmaps if square and rng.random() < 0.5 else \
+        [a_map(nc) for _ in range(int(rng.integers(1, 3)))]
+    pairs = []
+    for _ in range(int(rng.integers(1, 4))):
+        ri, ci = int(rng.integers(0, len(rmaps))), int(rng.integers(0, len(cmaps)))
+        if extruded:
+            k = int(rng.integers(1, 3))
+            regions = sorted(set(str(r) for r in rng.choice(REGIONS, k)))
+        else:
+            regions = ["ALL"]
+        pairs.append((ri, ci, regions))
+    # Per-entity layers with a bottom above 0: the reference's sparsity
+    # offsets by the absolute layer modulo the entity's layer count
+    # (pyop2/sparsity.pyx:362-384) while its wrappers offset from the
+    # entity's bottom (pyop2/codegen/builder.py:100-103).  Both are restated
+    # as they are, so only ALL-region loops (whose couplings agree as sets)
+    # are assembled there; the pattern itself is compared for every region.
+    spec["assemble_all_only"] = bool(extruded and not isinstance(spec["layers"], int)
+                                     and np.any(spec["layers"][:, 0] > 0))
+    ncols = nc * (LNODES if extruded else 1)
+    spec.update(rmaps=rmaps, cmaps=cmaps, shared_maps=cmaps is rmaps, pairs=pairs,
+                w=rng.integers(-3, 4, nit), x=rng.integers(-3, 4, (ncols, cdim)))
+    return spec
+
+
+def _mat_kernel(nrow, ncol, name):
+    return ("static void %s(double A[%d][%d], const double *w)\n{\n"
+            "  for (int i = 0; i < %d; ++i)\n    for (int j = 0; j < %d; ++j)\n"
+            "      A[i][j] += (double)((i + 1) * 3 - (j + 2) * (i %% 3)) + w[0];\n}\n"
+            % (name, nrow, ncol, nrow, ncol))
+
+
+def run_mat(op2, spec):
+    """Build the sparsity, assemble every (pair, region) with an INC
+    par_loop, and return the pattern, the row counts, the values and
+    A x (the GPU package's Mat.mult; scipy on the oracle's matrix)."""
+    nit = spec["nit"]
+    if spec["extruded"]:
+        base = op2.Set(nit, "base")
+        it = op2.ExtrudedSet(base, spec["layers"], extruded_periodic=True) \
+            if spec["periodic"] else op2.ExtrudedSet(base, spec["layers"])
+        rset = op2.Set(spec["nr"] * LNODES, "rows")
+        cset = rset if spec["square"] else op2.Set(spec["nc"] * LNODES, "cols")
+        wset = base
+    else:
+        it = op2.Set(nit, "it")
+        rset = op2.Set(spec["nr"], "rows")
+        cset = rset if spec["square"] else op2.Set(spec["nc"], "cols")
+        wset = it
+    rds = rset ** spec["rdim"]
+    cds = rds if spec["square"] else cset ** spec["cdim"]
+
+    def mk(m, to, name):
+        kw = {}
+        if spec["extruded"]:
+            kw["offset"] = m["offset"]
+            if "offset_quotient" in m:
+                kw["offset_quotient"] = m["offset_quotient"]
+        return op2.Map(it, to, m["arity"], m["values"], name, **kw)
+
+    rmaps = [mk(m, rset, "r%d" % i) for i, m in enumerate(spec["rmaps"])]
+    cmaps = rmaps if spec["shared_maps"] else \
+        [mk(m, cset, "c%d" % i) for i, m in enumerate(spec["cmaps"])]
+    triples = [(rmaps[ri], cmaps[ci], tuple(getattr(op2, r) for r in regs))
+               for ri, ci, regs in spec["pairs"]]
+    sp = op2.Sparsity((rds, cds), triples, block_sparse=spec["block_sparse"])
+    A = op2.Mat(sp)
+    w = op2.Dat(wset, spec["w"].astype(np.float64))
+    for ri, ci, regs in spec["pairs"]:
+        rm, cm = rmaps[ri], cmaps[ci]
+        for r in regs:
+            if spec["assemble_all_only"] and r != "ALL":
+                continue
+            nf = 2 if r == "ON_INTERIOR_FACETS" else 1
+            name = "am%d_%d_%d_%d" % (nf * rm.arity * spec["rdim"], nf * cm.arity * spec["cdim"],
+                                      spec["rdim"], spec["cdim"])
+            k = op2.Kernel(_mat_kernel(nf * rm.arity * spec["rdim"],
+                                       nf * cm.arity * spec["cdim"], name), name)
+            kw = {"iteration_region": getattr(op2, r)} if spec["extruded"] else {}
+            op2.par_loop(k, it, A(op2.INC, (rm, cm)), w(op2.READ), **kw)
+    A.assemble()
+    if hasattr(sp, "csr"):
+        rowptr, colidx = sp.csr()
+        values = A.csr()[2]
+        x = op2.Dat(cds, spec["x"].astype(np.float64))
+        y = op2.Dat(rds)
+        A.mult(x, y)
+        yv = np.array(y.data_ro_with_halos).reshape(-1)
+        nnz = np.array(sp.nnz)
+    else:
+        rowptr, colidx, values = sp.rowptr, sp.colidx, A.values_bcsr
+        yv = A.to_scipy() @ spec["x"].astype(np.float64).reshape(-1)
+        nnz = np.array(sp.nnz)
+    return {"rowptr": np.asarray(rowptr, dtype=np.int64), "colidx": np.asarray(colidx),
+            "nnz": nnz.astype(np.int64),
+            "values": np.asarray(values, dtype=np.float64).reshape(-1), "y": yv}
+
+
+def _layer_range(spec, e, region, for_sparsity):
+    """Cell layers an extruded loop (or the sparsity) visits on entity e:
+    pyop2/sparsity.pyx:344-361 and pyop2/codegen/builder.py:768-788."""
+    lay = spec["layers"]
+    if isinstance(lay, int):
+        start, end = 0, lay - 1
+    else:
+        start, end = int(lay[e, 0]), int(lay[e, 1]) - 1
+    bottom, nl = start, end - start
+    if region == "ON_BOTTOM":
+        end = start + 1
+    elif region == "ON_TOP":
+        start = end - 1
+    elif region == "ON_INTERIOR_FACETS" and not spec["periodic"]:
+        end = end - 1
+    return range(start, end), bottom, nl
+
+
+def _entries(spec, m, e, region, layer, bottom, nl, for_sparsity):
+    """Indices of map m on entity e at `layer` (both facets for interior
+    facets): the sparsity offsets by the absolute layer modulo the layer
+    count (pyop2/sparsity.pyx:371-384), a wrapper from the entity's bottom
+    (pyop2/codegen/builder.py:100-122)."""
+    a = m["arity"]
+    nf = 2 if region == "ON_INTERIOR_FACETS" else 1
+    out = []
+    for i in range(nf * a):
+        k, irem = divmod(i, a)
+        v = int(m["values"][e, irem])
+        if spec["extruded"]:
+            q = int(m["offset_quotient"][irem]) if "offset_quotient" in m else 0
+            off = int(m["offset"][irem])
+            if for_sparsity:
+                v += off * ((layer + k + q) % nl - q % nl)
+            elif spec["periodic"]:
+                v += off * ((layer - bottom + k + q) % nl - q % nl)
+            else:
+                v += off * (layer - bottom + k)
+        out.append(v)
+    return out
+
+
+def _visits(spec, ri, ci, region, for_sparsity):
+    for e in range(spec["nit"]):
+        if not spec["extruded"]:
+            yield e, (_entries(spec, spec["rmaps"][ri], e, region, 0, 0, 1, for_sparsity),
+                      _entries(spec, spec["cmaps"][ci], e, region, 0, 0, 1, for_sparsity))
+            continue
+        layers, bottom, nl = _layer_range(spec, e, region, for_sparsity)
+        for layer in layers:
+            yield e, (_entries(spec, spec["rmaps"][ri], e, region, layer, bottom, nl,
+                               for_sparsity),
+                      _entries(spec, spec["cmaps"][ci], e, region, layer, bottom, nl,
+                               for_sparsity))
+
+
+def mat_model(spec):
+    """The pattern (sorted distinct columns per block row, the diagonal on a
+    square space, negative indices ignored), the row counts, the assembled
+    values and A x of a make_mat_spec spec, in plain Python."""
+    L = LNODES if spec["extruded"] else 1
+    nrows, ncols = spec["nr"] * L, spec["nc"] * L
+    rdim, cdim = spec["rdim"], spec["cdim"]
+    pattern = [set() for _ in range(nrows)]
+    for ri, ci, regions in spec["pairs"]:
+        for region in regions:
+            for _, (rows, cols) in _visits(spec, ri, ci, region, True):
+                for r in rows:
+                    if r >= 0:
+                        pattern[r].update(c for c in cols if c >= 0)
+    if spec["square"]:
+        for i in range(min(nrows, ncols)):
+            pattern[i].add(i)
+    rowptr = np.zeros(nrows + 1, dtype=np.int64)
+    rowptr[1:] = np.cumsum([len(p) for p in pattern])
+    colidx = np.array([c for p in pattern for c in sorted(p)], dtype=np.int32)
+    where = [{c: k for k, c in enumerate(sorted(p))} for p in pattern]
+    values = np.zeros((len(colidx), rdim, cdim))
+    for ri, ci, regions in spec["pairs"]:
+        for region in regions:
+            if spec["assemble_all_only"] and region != "ALL":
+                continue
+            for e, (rows, cols) in _visits(spec, ri, ci, region, False):
+                w = float(spec["w"][e])
+                for i in range(len(rows) * rdim):
+                    r = rows[i // rdim]
+                    if r < 0:
+                        continue
+                    for j in range(len(cols) * cdim):
+                        c = cols[j // cdim]
+                        if c < 0:
+                            continue
+                        v = (i + 1) * 3 - (j + 2) * (i % 3) + w
+                        values[rowptr[r] + where[r][c], i % rdim, j % cdim] += v
+    counts = np.diff(rowptr)
+    if not (spec["block_sparse"] and rdim == cdim):
+        counts = np.repeat(counts * cdim, rdim)
+    x = spec["x"].astype(np.float64).reshape(ncols, cdim)
+    y = np.zeros((nrows, rdim))
+    for r in range(nrows):
+        for k in range(rowptr[r], rowptr[r + 1]):
+            y[r] += values[k] @ x[colidx[k]]
+    return {"rowptr": rowptr, "colidx": colidx, "nnz": counts.astype(np.int64),
+            "values": values.reshape(-1), "y": y.reshape(-1)}
