@@ -111,8 +111,8 @@ class Sparsity:
                                     diagonal_block=diag, nest=False))
             self._blocks.append(row)
         if self._nested:
-            self._d_nnz = tuple(b._d_nnz for row in self._blocks for b in row)
-            self._o_nnz = tuple(b._o_nnz for row in self._blocks for b in row)
+            self._d_nnz = tuple(b.nnz for row in self._blocks for b in row)
+            self._o_nnz = tuple(b.onnz for row in self._blocks for b in row)
         else:
             rows = []
             for i, row in enumerate(self._blocks):
@@ -263,12 +263,22 @@ class Sparsity:
         self._rowptr = rowptr
         self._colidx = colidx
         self._nnz_blocks = int(nnz.value)
-        counts = torch.diff(rowptr).to(torch.int32).cpu().numpy().astype(IntType)
-        rdim, cdim = rset.cdim, cset.cdim
-        if not (self._block_sparse and rdim == cdim):
-            counts = np.repeat(counts * cdim, rdim).astype(IntType)
-        self._d_nnz = counts
-        self._o_nnz = np.zeros_like(counts)
+        # row counts are read back from the device when first asked for
+        self._d_nnz = self._o_nnz = None
+
+    def _row_counts(self):
+        """(nnz, onnz) per row: dof rows with dof columns unless the matrix
+        is BAIJ (block_sparse and rdim == cdim), where they count blocks
+        (pyop2/sparsity.pyx:168-173); onnz is zero on one process."""
+        if self._d_nnz is None:
+            rset, cset = self._dsets
+            counts = torch.diff(self._rowptr).to(torch.int32).cpu().numpy().astype(IntType)
+            rdim, cdim = rset.cdim, cset.cdim
+            if not (self._block_sparse and rdim == cdim):
+                counts = np.repeat(counts * cdim, rdim).astype(IntType)
+            self._d_nnz = counts
+            self._o_nnz = np.zeros_like(counts)
+        return self._d_nnz, self._o_nnz
 
     # ---- properties
     @property
@@ -306,19 +316,19 @@ class Sparsity:
 
     @property
     def nnz(self):
-        return self._d_nnz
+        return self._row_counts()[0]
 
     @property
     def onnz(self):
-        return self._o_nnz
+        return self._row_counts()[1]
 
     @property
     def nz(self):
-        return int(self._d_nnz.sum())
+        return int(self.nnz.sum())
 
     @property
     def onz(self):
-        return int(self._o_nnz.sum())
+        return int(self.onnz.sum())
 
     @property
     def rowptr(self):
