@@ -105,9 +105,13 @@ __device__ __forceinline__ int col_of(const SpDev &S, const PairDev &P, long lon
 }
 
 // Row -> virtual-cell incidence: counts (pass 0) or fills (pass 1).
+// With a single pair every incidence brings the same number of candidate
+// columns (tc), so the candidate counts follow from the incidence counts
+// and cand is left untouched (one atomic per incidence instead of two).
 __global__ void k_incidence(SpDev S, const PairDev *__restrict__ pairs, int p, int pass,
-                            long long *__restrict__ cnt, int *__restrict__ cand,
-                            int *__restrict__ fillpos, long long *__restrict__ tlist) {
+                            int single_pair, long long *__restrict__ cnt,
+                            int *__restrict__ cand, int *__restrict__ fillpos,
+                            long long *__restrict__ tlist) {
     const PairDev &P = pairs[p];
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < P.nvirt; v += stride) {
@@ -125,7 +129,7 @@ __global__ void k_incidence(SpDev S, const PairDev *__restrict__ pairs, int p, i
             }
             if (pass == 0) {
                 atomicAdd((unsigned long long *)&cnt[r], 1ull);
-                atomicAdd(&cand[r], P.tc);
+                if (!single_pair) atomicAdd(&cand[r], P.tc);
             } else {
                 const long long pos = cnt[r] + atomicAdd(&fillpos[r], 1);
                 tlist[pos] = ((long long)p << 56) | v;
@@ -134,11 +138,19 @@ __global__ void k_incidence(SpDev S, const PairDev *__restrict__ pairs, int p, i
     }
 }
 
-__global__ void k_max_cand(const int *__restrict__ cand, long long n, int diag, int *out) {
+// Candidate count of row i: cand[i], or its incidences times tc when tc > 0
+// (one pair); cnt holds the scanned incidence offsets by then.
+__device__ __forceinline__ long long cand_of(const int *cand, const long long *cnt, int tc,
+                                             long long i) {
+    return tc > 0 ? (cnt[i + 1] - cnt[i]) * tc : (long long)cand[i];
+}
+
+__global__ void k_max_cand(const int *__restrict__ cand, const long long *__restrict__ cnt,
+                           int tc, long long n, int diag, int *out) {
     int m = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x)
-        m = max(m, cand[i] + diag);
+        m = max(m, (int)cand_of(cand, cnt, tc, i) + diag);
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
@@ -173,6 +185,14 @@ __device__ __forceinline__ void row_insert(int c, int *tab, unsigned mask, int t
     atomicOr(err, OP2G_DEVERR_CAPACITY);  // table full: cannot happen (tsize >= 2 x candidates)
 }
 
+// SIMPLE: one (row map, column map) pair over a flat set with no composed
+// maps, so a transpose-list code is the entity itself and its candidate
+// columns are one row of the column map.  The warp then walks the incident
+// cells in warp-uniform rounds and, per column slot, lets only the first of
+// the lanes holding the same column insert it (__match_any_sync): on a mesh
+// a vertex's own column recurs in every incident cell, and most neighbours
+// in several, so this removes about half of the shared-memory atomics.
+template <bool SIMPLE>
 __global__ void k_rows(SpDev S, const PairDev *__restrict__ pairs,
                        const long long *__restrict__ tptr, const long long *__restrict__ tlist,
                        int tsize, int ucap, const long long *__restrict__ candptr,
@@ -193,7 +213,25 @@ __global__ void k_rows(SpDev S, const PairDev *__restrict__ pairs,
         if (lane == 0) hdr[0] = 0;
         __syncwarp();
         const long long e0 = tptr[r], e1 = tptr[r + 1];
-        for (long long e = e0 + lane; e < e1; e += 32) {
+        if (SIMPLE) {
+            const int *cmap = pairs[0].cmap;
+            const int ca = pairs[0].carity;
+            for (long long b = e0; b < e1; b += 32) {  // warp-uniform rounds
+                const long long e = b + lane;
+                const int *crow = e < e1 ? cmap + tlist[e] * ca : nullptr;
+                for (int j = 0; j < ca; ++j) {
+                    int c = crow ? __ldg(crow + j) : -1;
+                    if (c >= S.ncols) {
+                        atomicOr(S.err, OP2G_DEVERR_MAP_BOUNDS);
+                        c = -1;
+                    }
+                    const unsigned same = __match_any_sync(0xffffffffu, c);
+                    if (c >= 0 && (__ffs(same) - 1) == lane)
+                        row_insert(c, tab, mask, tsize, uniq, uslot, hdr, S.err);
+                }
+            }
+        }
+        for (long long e = e0 + lane; !SIMPLE && e < e1; e += 32) {
             const long long code = tlist[e];
             const PairDev &P = pairs[(int)(code >> 56)];
             long long rent, cent;
@@ -250,11 +288,12 @@ __global__ void k_rows(SpDev S, const PairDev *__restrict__ pairs,
 }
 
 // candptr[r] = cand[r] + (diagonal entry of row r), to be scanned.
-__global__ void k_cand_sizes(const int *__restrict__ cand, long long n, long long ncols, int diag,
+__global__ void k_cand_sizes(const int *__restrict__ cand, const long long *__restrict__ cnt,
+                             int tc, long long n, long long ncols, int diag,
                              long long *__restrict__ candptr) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += stride)
-        candptr[r] = cand[r] + ((diag && r < ncols) ? 1 : 0);
+        candptr[r] = cand_of(cand, cnt, tc, r) + ((diag && r < ncols) ? 1 : 0);
 }
 
 // One warp per row: copy the sorted distinct columns to the CSR column array.
@@ -436,9 +475,10 @@ int sms_of_current() {
     return n > 0 ? n : 1;
 }
 
-op2g_status sp_rows_launch(const SpDev &S, const PairDev *pd, const long long *tptr,
-                           const long long *tlist, int max_cand, const long long *candptr,
-                           int *tmp, long long *rowcount, cudaStream_t st) {
+op2g_status sp_rows_launch(const SpDev &S, const PairDev *pd, bool simple,
+                           const long long *tptr, const long long *tlist, int max_cand,
+                           const long long *candptr, int *tmp, long long *rowcount,
+                           cudaStream_t st) {
     if (S.nrows == 0) return OP2G_OK;
     int tsize = 32;
     while (tsize < 2 * max_cand) tsize <<= 1;
@@ -451,13 +491,21 @@ op2g_status sp_rows_launch(const SpDev &S, const PairDev *pd, const long long *t
     const size_t smem = per * wpb;
     if (smem > 227 * 1024)
         return op2g::fail(OP2G_ERR_CAPACITY, "a sparsity row has more than 18,000 candidate columns");
-    if (smem > 48 * 1024)
-        CK(cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (smem > 48 * 1024) {
+        CK(cudaFuncSetAttribute(k_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+        CK(cudaFuncSetAttribute(k_rows<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+    }
     long long blocks = (S.nrows + wpb - 1) / wpb;
     const long long capb = (long long)sms_of_current() * 32;
     if (blocks > capb) blocks = capb;
-    k_rows<<<(unsigned)blocks, 32 * wpb, smem, st>>>(S, pd, tptr, tlist, tsize, ucap, candptr, tmp,
-                                                     rowcount);
+    if (simple)
+        k_rows<true><<<(unsigned)blocks, 32 * wpb, smem, st>>>(S, pd, tptr, tlist, tsize, ucap,
+                                                               candptr, tmp, rowcount);
+    else
+        k_rows<false><<<(unsigned)blocks, 32 * wpb, smem, st>>>(S, pd, tptr, tlist, tsize, ucap,
+                                                                candptr, tmp, rowcount);
     CK(cudaGetLastError());
     return OP2G_OK;
 }
@@ -517,12 +565,15 @@ op2g_status op2g_sparsity_count(const op2g_sparsity_desc *d, void *ws, size_t ws
     if (!pairs.empty())
         CK(cudaMemcpyAsync(pd, pairs.data(), sizeof(PairDev) * pairs.size(), cudaMemcpyHostToDevice, st));
     const long long capb = (long long)sms_of_current() * 16;
+    const int single = pairs.size() == 1 ? 1 : 0;
+    const int tc1 = single ? pairs[0].tc : 0;  // candidates per incidence with one pair
     for (int pass = 0; pass < 2; ++pass) {
         for (size_t p = 0; p < pairs.size(); ++p) {
             long long nb = (pairs[p].nvirt + 255) / 256;
             if (nb == 0) continue;
             if (nb > capb) nb = capb;
-            k_incidence<<<(unsigned)nb, 256, 0, st>>>(S, pd, (int)p, pass, cnt, cand, fill, tlist);
+            k_incidence<<<(unsigned)nb, 256, 0, st>>>(S, pd, (int)p, pass, single, cnt, cand,
+                                                      fill, tlist);
             CK(cudaGetLastError());
         }
         if (pass == 0) {
@@ -533,7 +584,8 @@ op2g_status op2g_sparsity_count(const op2g_sparsity_desc *d, void *ws, size_t ws
     if (d->nrows > 0) {
         long long nb = (d->nrows + 255) / 256;
         if (nb > capb) nb = capb;
-        k_max_cand<<<(unsigned)nb, 256, 0, st>>>(cand, d->nrows, d->set_diag ? 1 : 0, &misc->max_cand);
+        k_max_cand<<<(unsigned)nb, 256, 0, st>>>(cand, cnt, tc1, d->nrows, d->set_diag ? 1 : 0,
+                                                 &misc->max_cand);
         CK(cudaGetLastError());
     }
     SpMisc hm;
@@ -548,7 +600,8 @@ op2g_status op2g_sparsity_count(const op2g_sparsity_desc *d, void *ws, size_t ws
         long long nb = (d->nrows + 255) / 256;
         if (nb > capb) nb = capb;
         if (nb < 1) nb = 1;
-        k_cand_sizes<<<(unsigned)nb, 256, 0, st>>>(cand, d->nrows, d->ncols, d->set_diag ? 1 : 0,
+        k_cand_sizes<<<(unsigned)nb, 256, 0, st>>>(cand, cnt, tc1, d->nrows, d->ncols,
+                                                   d->set_diag ? 1 : 0,
                                                    candptr);
         CK(cudaGetLastError());
         CK(cudaMemsetAsync(candptr + d->nrows, 0, sizeof(long long), st));
@@ -557,7 +610,10 @@ op2g_status op2g_sparsity_count(const op2g_sparsity_desc *d, void *ws, size_t ws
     }
     int cap = hm.max_cand > 1 ? hm.max_cand : 1;
     CK(cudaMemcpyAsync(&misc->cap, &cap, sizeof(int), cudaMemcpyHostToDevice, st));
-    s = sp_rows_launch(S, pd, cnt, tlist, cap, candptr, tmp, (long long *)rowptr, st);
+    // one pair over a flat set without composed maps: codes are entities
+    const bool simple = pairs.size() == 1 && !d->extruded && pairs[0].nrc == 0 &&
+                        pairs[0].ncc == 0;
+    s = sp_rows_launch(S, pd, simple, cnt, tlist, cap, candptr, tmp, (long long *)rowptr, st);
     if (s != OP2G_OK) return s;
     CK(cudaMemsetAsync(rowptr + d->nrows, 0, sizeof(long long), st));
     s = scan_exclusive((long long *)rowptr, n1, scan, st);
