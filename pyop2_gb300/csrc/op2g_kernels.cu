@@ -108,8 +108,10 @@ __device__ __forceinline__ int col_of(const SpDev &S, const PairDev &P, long lon
 // With a single pair every incidence brings the same number of candidate
 // columns (tc), so the candidate counts follow from the incidence counts
 // and cand is left untouched (one atomic per incidence instead of two).
+// narrow: the transpose list holds 32-bit entity numbers (one pair over a
+// flat set), otherwise 64-bit codes (pair << 56 | virtual cell).
 __global__ void k_incidence(SpDev S, const PairDev *__restrict__ pairs, int p, int pass,
-                            int single_pair, long long *__restrict__ cnt,
+                            int single_pair, int narrow, long long *__restrict__ cnt,
                             int *__restrict__ cand, int *__restrict__ fillpos,
                             long long *__restrict__ tlist) {
     const PairDev &P = pairs[p];
@@ -132,7 +134,10 @@ __global__ void k_incidence(SpDev S, const PairDev *__restrict__ pairs, int p, i
                 if (!single_pair) atomicAdd(&cand[r], P.tc);
             } else {
                 const long long pos = cnt[r] + atomicAdd(&fillpos[r], 1);
-                tlist[pos] = ((long long)p << 56) | v;
+                if (narrow)
+                    ((int *)tlist)[pos] = (int)v;
+                else
+                    tlist[pos] = ((long long)p << 56) | v;
             }
         }
     }
@@ -186,8 +191,8 @@ __device__ __forceinline__ void row_insert(int c, int *tab, unsigned mask, int t
 }
 
 // SIMPLE: one (row map, column map) pair over a flat set with no composed
-// maps, so a transpose-list code is the entity itself and its candidate
-// columns are one row of the column map.  The warp then walks the incident
+// maps, so the transpose list holds 32-bit entity numbers and an entry's
+// candidate columns are one row of the column map.  The warp then walks the incident
 // cells in warp-uniform rounds and, per column slot, lets only the first of
 // the lanes holding the same column insert it (__match_any_sync): on a mesh
 // a vertex's own column recurs in every incident cell, and most neighbours
@@ -218,7 +223,8 @@ __global__ void k_rows(SpDev S, const PairDev *__restrict__ pairs,
             const int ca = pairs[0].carity;
             for (long long b = e0; b < e1; b += 32) {  // warp-uniform rounds
                 const long long e = b + lane;
-                const int *crow = e < e1 ? cmap + tlist[e] * ca : nullptr;
+                const int *crow =
+                    e < e1 ? cmap + (long long)((const int *)tlist)[e] * ca : nullptr;
                 for (int j = 0; j < ca; ++j) {
                     int c = crow ? __ldg(crow + j) : -1;
                     if (c >= S.ncols) {
@@ -567,13 +573,16 @@ op2g_status op2g_sparsity_count(const op2g_sparsity_desc *d, void *ws, size_t ws
     const long long capb = (long long)sms_of_current() * 16;
     const int single = pairs.size() == 1 ? 1 : 0;
     const int tc1 = single ? pairs[0].tc : 0;  // candidates per incidence with one pair
+    // one pair over a flat set without composed maps: the transpose list
+    // holds entity numbers (32-bit: set sizes are int32)
+    const bool simple = single && !d->extruded && pairs[0].nrc == 0 && pairs[0].ncc == 0;
     for (int pass = 0; pass < 2; ++pass) {
         for (size_t p = 0; p < pairs.size(); ++p) {
             long long nb = (pairs[p].nvirt + 255) / 256;
             if (nb == 0) continue;
             if (nb > capb) nb = capb;
-            k_incidence<<<(unsigned)nb, 256, 0, st>>>(S, pd, (int)p, pass, single, cnt, cand,
-                                                      fill, tlist);
+            k_incidence<<<(unsigned)nb, 256, 0, st>>>(S, pd, (int)p, pass, single,
+                                                      simple ? 1 : 0, cnt, cand, fill, tlist);
             CK(cudaGetLastError());
         }
         if (pass == 0) {
@@ -610,9 +619,6 @@ op2g_status op2g_sparsity_count(const op2g_sparsity_desc *d, void *ws, size_t ws
     }
     int cap = hm.max_cand > 1 ? hm.max_cand : 1;
     CK(cudaMemcpyAsync(&misc->cap, &cap, sizeof(int), cudaMemcpyHostToDevice, st));
-    // one pair over a flat set without composed maps: codes are entities
-    const bool simple = pairs.size() == 1 && !d->extruded && pairs[0].nrc == 0 &&
-                        pairs[0].ncc == 0;
     s = sp_rows_launch(S, pd, simple, cnt, tlist, cap, candptr, tmp, (long long *)rowptr, st);
     if (s != OP2G_OK) return s;
     CK(cudaMemsetAsync(rowptr + d->nrows, 0, sizeof(long long), st));
