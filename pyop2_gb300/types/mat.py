@@ -9,6 +9,7 @@ would use BAIJ, AIJ otherwise: the stored values are the same, only
 ``nnz`` is reported per dof row for AIJ, as pyop2/sparsity.pyx:168-173 does).
 """
 import ctypes
+import warnings
 from collections.abc import Sequence
 
 import numpy as np
@@ -692,6 +693,39 @@ class Mat(DataCarrier):
         rdim, cdim = self.dims[0][0]
         v = self.tensor.cpu().numpy().reshape(-1, rdim, cdim)
         return rp, ci, v
+
+    def to_torch(self):
+        """The matrix as a torch sparse tensor on the device, for solvers:
+        CSR for 1x1 blocks, BSR (``blocksize = (rdim, cdim)``) otherwise.
+        Values and column indices are views of the Mat's own device arrays
+        (no copy: later assemblies show through); the row pointers are
+        converted to the column indices' int32.  A mixed Mat is exported as
+        its monolithic whole, assembled from its blocks (a copy)."""
+        self._assemble_owner()
+        if self._mixed:
+            s = self.to_scipy().tocsr()
+            dev = device.device()
+            with warnings.catch_warnings():
+                # torch flags its sparse compressed layouts as beta
+                warnings.simplefilter("ignore", UserWarning)
+                return torch.sparse_csr_tensor(
+                    torch.as_tensor(s.indptr.astype(np.int64), device=dev),
+                    torch.as_tensor(s.indices.astype(np.int64), device=dev),
+                    torch.as_tensor(s.data, device=dev), size=s.shape)
+        sp = self._sparsity
+        rdim, cdim = self.dims[0][0]
+        if sp.nblocks >= 2 ** 31:
+            raise ValueError("to_torch: more than 2^31 - 1 blocks")
+        crow = sp.rowptr.to(torch.int32)
+        col = sp.colidx
+        shape = (self.nrows, self.ncols)
+        with warnings.catch_warnings():
+            # torch flags its sparse compressed layouts as beta
+            warnings.simplefilter("ignore", UserWarning)
+            if rdim == 1 and cdim == 1:
+                return torch.sparse_csr_tensor(crow, col, self.tensor, size=shape)
+            return torch.sparse_bsr_tensor(crow, col, self.tensor.view(-1, rdim, cdim),
+                                           size=shape)
 
     def to_scipy(self):
         """scipy.sparse BSR (or CSR for 1x1 blocks) copy of the matrix."""

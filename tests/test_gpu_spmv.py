@@ -56,3 +56,31 @@ def test_mult_matches_scipy(gpu_op2, shape):
     A.mult(xt, yt, transpose=True)
     reft = S.T @ xt.data_ro.reshape(-1)
     assert np.abs(yt.data_ro.reshape(-1) - reft).max() <= 1e-12 * np.abs(reft).max()
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=["%dx%d" % s for s in SHAPES])
+def test_to_torch_export(gpu_op2, shape):
+    """torch sparse export (CSR for 1x1, BSR otherwise) equals the scipy
+    export entry for entry and shares the Mat's device values."""
+    import torch
+    op2 = gpu_op2
+    r, c = shape
+    A, drows, dcols, rng = _assembled(op2, r, c, seed=5 * r + c)
+    T = A.to_torch()
+    assert T.layout == (torch.sparse_csr if (r, c) == (1, 1) else torch.sparse_bsr)
+    assert T.shape == (257 * r, 193 * c) and T.is_cuda
+    assert np.array_equal(T.to_dense().cpu().numpy(), A.to_scipy().toarray())
+    assert T.values().data_ptr() == A.tensor.data_ptr()
+    if (r, c) == (1, 1):
+        x = op2.Dat(dcols, rng.uniform(-1, 1, 193))
+        y = op2.Dat(drows)
+        A.mult(x, y)
+        ty = (T @ x.tensor.view(-1, 1)).view(-1)
+        assert torch.max(torch.abs(ty - y.tensor)).item() <= 1e-12 * torch.max(torch.abs(y.tensor)).item()
+
+
+def test_to_torch_mixed(gpu_op2):
+    import scenarios as S
+    A, _ = S.sc_mixed_p1p0(gpu_op2, 8, False)
+    T = A.to_torch()
+    assert np.array_equal(T.to_dense().cpu().numpy(), A.to_scipy().toarray())
