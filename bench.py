@@ -543,21 +543,9 @@ def measure_prisms(op2, steps, warmup, n=256):
                       p["L"](op2.READ, c2c), du(op2.INC, c2n), dL(op2.WRITE, c2c))
     t_act = _time_loop(act, steps, warmup)
     t_adj = _time_loop(adj, steps, warmup)
-    # both in one graph
-    for lp in (act, adj):
-        lp.launch_desc()
-    torch.cuda.synchronize()
-    g = torch.cuda.CUDAGraph()
-    s = torch.cuda.Stream()
-    s.wait_stream(torch.cuda.current_stream())
-    from pyop2_gb300 import _lib, device
-    import ctypes
-    with torch.cuda.stream(s):
-        with torch.cuda.graph(g, stream=s):
-            for lp in (act, adj):
-                _lib.call("op2g_kernel_launch", lp._built[2].handle,
-                          ctypes.byref(lp.launch_desc()), device.stream_handle())
-    torch.cuda.current_stream().wait_stream(s)
+    # both in one CUDA graph
+    from pyop2_gb300.graph import LoopGraph
+    g = LoopGraph([act, adj])
     for _ in range(warmup):
         g.replay()
     torch.cuda.synchronize()
@@ -568,8 +556,6 @@ def measure_prisms(op2, steps, warmup, n=256):
     e1.record()
     e1.synchronize()
     t_graph = e0.elapsed_time(e1) / steps
-    for lp in (act, adj):
-        lp.mark_written()
     # BAIJ sparsity + assembly
     t_sp, sp = _time_sparsity_build((nodes ** 3, nodes ** 3), [(c2n, c2n, None)])
     A = op2.Mat(sp)

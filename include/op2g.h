@@ -222,6 +222,23 @@ op2g_status op2g_kernel_launch_batched(op2g_kernel *k, const void *params_dev,
                                        const int64_t *work_dev, int64_t nwork,
                                        int32_t grid, void *stream);
 
+/* CUDA graphs of op2g launches: record a step once, replay it with one call
+ * (the reference builds no graphs; here several par_loops, or one batched
+ * launch of many, run as one unit).  op2g_graph_begin returns a private
+ * stream in capture mode; launch on it with op2g_kernel_launch,
+ * op2g_kernel_launch_batched, op2g_mat_spmv, ... (call op2g_kernel_prepare
+ * for each kernel first: module loading is not capturable; nothing on the
+ * capture stream runs until the graph is launched).  op2g_graph_end always
+ * ends the capture and releases the stream; it instantiates the recorded
+ * graph into *out.  Device arrays the launches referenced are used, not
+ * copied, by every replay and must outlive the graph. */
+typedef struct op2g_graph op2g_graph;
+op2g_status op2g_graph_begin(void **capture_stream);
+op2g_status op2g_graph_end(void *capture_stream, op2g_graph **out);
+/* Replay on `stream` (asynchronous). */
+op2g_status op2g_graph_launch(op2g_graph *g, void *stream);
+void op2g_graph_destroy(op2g_graph *g);
+
 /* ------------------------------------------------------------- sparsity */
 /* One (row map, column map, iteration region) triple of a Sparsity
  * (pyop2/types/mat.py:118-176).  Map arrays are device int32

@@ -94,6 +94,10 @@ SIGNATURES = {
     "op2g_kernel_param_bytes": (_i32, [_p]),
     "op2g_kernel_pack_params": (_i32, [_p, ctypes.POINTER(LaunchDesc), _p]),
     "op2g_kernel_launch_batched": (_i32, [_p, _p, _p, _i64, _i32, _p]),
+    "op2g_graph_begin": (_i32, [ctypes.POINTER(_p)]),
+    "op2g_graph_end": (_i32, [_p, ctypes.POINTER(_p)]),
+    "op2g_graph_launch": (_i32, [_p, _p]),
+    "op2g_graph_destroy": (None, [_p]),
     "op2g_sparsity_workspace": (_i32, [ctypes.POINTER(SparsityDesc),
                                        ctypes.POINTER(ctypes.c_size_t)]),
     "op2g_sparsity_count": (_i32, [ctypes.POINTER(SparsityDesc), _p, ctypes.c_size_t, _p,

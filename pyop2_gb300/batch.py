@@ -77,34 +77,39 @@ class BatchedParLoop:
 
     def compute(self):
         """Run every loop once in one launch."""
-        for lp in self.loops:
-            lp.launch_desc()     # uploads any host-side changes
-        _lib.call("op2g_kernel_launch_batched", self.kernel.handle, self.params.data_ptr(),
-                  self.work.data_ptr(), self.nwork, 0, device.stream_handle())
-        for lp in self.loops:
-            lp.mark_written()
+        self._enqueue(device.stream_handle())
+        self.mark_written()
 
     def capture(self):
-        """Record compute() into a CUDA graph (replay() runs it)."""
-        for lp in self.loops:
-            lp.launch_desc()
-        torch.cuda.synchronize()
-        g = torch.cuda.CUDAGraph()
-        s = torch.cuda.Stream()
-        s.wait_stream(torch.cuda.current_stream())
-        with torch.cuda.stream(s):
-            with torch.cuda.graph(g, stream=s):
-                _lib.call("op2g_kernel_launch_batched", self.kernel.handle,
-                          self.params.data_ptr(), self.work.data_ptr(), self.nwork, 0,
-                          device.stream_handle())
-        torch.cuda.current_stream().wait_stream(s)
-        self._graph = g
-        return g
+        """Record the launch into a CUDA graph (pyop2_gb300.graph.LoopGraph;
+        replay() runs it)."""
+        from pyop2_gb300.graph import LoopGraph
+        self._graph = LoopGraph([self])
+        return self._graph
 
     def replay(self):
         if self._graph is None:
             self.capture()
         self._graph.replay()
+
+    # ---- graph capture
+    def _prepare_capture(self):
+        self._refresh()
+        _lib.call("op2g_kernel_prepare", self.kernel.handle)
+
+    def _capture_key(self):
+        return (self.params.data_ptr(), self.work.data_ptr(), self.nwork)
+
+    def _refresh(self):
+        for lp in self.loops:
+            lp.launch_desc()     # uploads any host-side changes
+
+    def _enqueue(self, st):
+        self._refresh()
+        _lib.call("op2g_kernel_launch_batched", self.kernel.handle, self.params.data_ptr(),
+                  self.work.data_ptr(), self.nwork, 0, st)
+
+    def mark_written(self):
         for lp in self.loops:
             lp.mark_written()
 
@@ -140,7 +145,7 @@ def autotune_batch(loops, chunks=(512, 2048, 8192), block_sizes=(128, 256), reps
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(reps):
-            b._graph.replay()
+            b._graph.launch()
         e1.record()
         e1.synchronize()
         t = e0.elapsed_time(e1) / reps

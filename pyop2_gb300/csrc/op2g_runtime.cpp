@@ -498,3 +498,70 @@ op2g_status op2g_kernel_launch_batched(op2g_kernel *k, const void *params_dev,
 }
 
 }  // extern "C"
+
+struct op2g_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+op2g_status op2g_graph_begin(void **capture_stream) {
+    if (!capture_stream) return fail(OP2G_ERR_INVALID, "NULL argument");
+    *capture_stream = nullptr;
+    cudaStream_t s = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreateWithFlags");
+    // thread-local: other threads may keep using CUDA while this one records
+    e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(s);
+        return cuda_fail(e, "cudaStreamBeginCapture");
+    }
+    *capture_stream = (void *)s;
+    return OP2G_OK;
+}
+
+op2g_status op2g_graph_end(void *capture_stream, op2g_graph **out) {
+    if (!capture_stream) return fail(OP2G_ERR_INVALID, "NULL capture stream");
+    if (out) *out = nullptr;
+    cudaStream_t s = (cudaStream_t)capture_stream;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    cudaStreamDestroy(s);
+    if (e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return cuda_fail(e, "cudaStreamEndCapture");
+    }
+    if (!out) {
+        cudaGraphDestroy(graph);
+        return fail(OP2G_ERR_INVALID, "NULL output");
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    op2g_graph *g = new op2g_graph;
+    g->graph = graph;
+    g->exec = exec;
+    *out = g;
+    return OP2G_OK;
+}
+
+op2g_status op2g_graph_launch(op2g_graph *g, void *stream) {
+    if (!g || !g->exec) return fail(OP2G_ERR_INVALID, "NULL graph");
+    cudaError_t e = cudaGraphLaunch(g->exec, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
+    return OP2G_OK;
+}
+
+void op2g_graph_destroy(op2g_graph *g) {
+    if (!g) return;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+}
+
+}  // extern "C"

@@ -754,9 +754,34 @@ class Parloop:
         return self._compute()
 
     def _compute(self):
+        self._enqueue(device.stream_handle())
+        self.mark_written()
+        if self._dbg_err is not None:
+            e = int(self._dbg_err.item())
+            if e & _lib.DEVERR_MAP_BOUNDS:
+                self._dbg_err.zero_()
+                raise MapValueError("par_loop %s: a map value is outside its target set"
+                                    % self.local_kernel.name)
+
+    # ---- graph capture (pyop2_gb300.graph.LoopGraph)
+    def _prepare_capture(self):
+        """Everything a launch does besides launching: build, upload, load the
+        module, colour (none of it may happen inside a stream capture)."""
+        self.launch_desc()
+        _lib.call("op2g_kernel_prepare", self._built[2].handle)
+        if self._built[0] == _lib.SCATTER_PLAIN:
+            colour_plan(self)
+
+    def _capture_key(self):
+        return tuple(self._launch_cache[0])
+
+    def _refresh(self):
+        self.launch_desc()
+
+    def _enqueue(self, st):
+        """Launch this loop on stream `st` (no state updates)."""
         D = self.launch_desc()
         scatter, bs, k, table, argdescs = self._built
-        st = device.stream_handle()
         if scatter == _lib.SCATTER_PLAIN:
             plan = colour_plan(self)
             start, end, idx = D.start, D.end, D.indices
@@ -770,13 +795,6 @@ class Parloop:
                 D.start, D.end, D.indices = start, end, idx
         else:
             _lib.check(_launch(k.handle, ctypes.byref(D), st))
-        self.mark_written()
-        if self._dbg_err is not None:
-            e = int(self._dbg_err.item())
-            if e & _lib.DEVERR_MAP_BOUNDS:
-                self._dbg_err.zero_()
-                raise MapValueError("par_loop %s: a map value is outside its target set"
-                                    % self.local_kernel.name)
 
     def generated_source(self):
         """CUDA source of the wrapper this loop runs."""

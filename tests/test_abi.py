@@ -88,3 +88,12 @@ def test_invalid_descriptor_is_rejected(lib):
                               None, 0, b"sm_103a", None, ctypes.byref(h))
     assert st == lib.ERR_INVALID
     assert b"block_size" in L.op2g_last_error()
+
+
+def test_graph_entry_points_reject_null(lib):
+    """The graph calls validate their arguments before touching CUDA."""
+    L = lib.lib()
+    assert L.op2g_graph_begin(None) == lib.ERR_INVALID
+    assert L.op2g_graph_end(None, None) == lib.ERR_INVALID
+    assert L.op2g_graph_launch(None, None) == lib.ERR_INVALID
+    L.op2g_graph_destroy(None)
