@@ -604,9 +604,24 @@ def measure_small(op2, calls=500, with_cpu=True):
         pl.compute()
     torch.cuda.synchronize()
     per_compute = (time.perf_counter() - t0) / calls
+    # the same loop recorded into a CUDA graph, once and as 10 consecutive
+    # steps (the form a time-stepping loop over a small mesh would take)
+    from pyop2_gb300.graph import LoopGraph
+    graph_us = {}
+    for nrep in (1, 10):
+        g = LoopGraph([pl] * nrep)
+        g.replay()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(calls // nrep):
+            g.replay()
+        torch.cuda.synchronize()
+        graph_us[nrep] = (time.perf_counter() - t0) / (calls // nrep * nrep) * 1e6
     C = p["cells"].size
     out = {"workload": "p1_tri_laplace_action_64sq", "cells": C,
            "par_loop_us_per_call": per_call * 1e6, "parloop_compute_us_per_call": per_compute * 1e6,
+           "graph_replay_us_per_loop": graph_us[1],
+           "graph_of_10_steps_us_per_loop": graph_us[10],
            "par_loop_cells_per_s": C / per_call}
     if with_cpu:
         from oracle import op2 as O
@@ -861,6 +876,8 @@ def run_only(args):
         out = measure_adjoint(op2, args.steps, args.warmup, n=args.size or 64)
     elif args.only == "batch":
         out = measure_batch(op2, args.steps, args.warmup)
+    elif args.only == "small":
+        out = measure_small(op2, with_cpu=False)
     else:
         out = measure_prisms(op2, args.steps, args.warmup, n=args.size or 256)
     print(json.dumps({"only": args.only, "result": out}), flush=True)
@@ -879,7 +896,7 @@ def main():
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the headline action (no adjoint / batch measurements)")
     ap.add_argument("--only", default=None,
-                    choices=["sparsity", "adjoint", "batch", "prisms"],
+                    choices=["sparsity", "adjoint", "batch", "prisms", "small"],
                     help="run one secondary measurement alone (profiling runs)")
     ap.add_argument("--size", type=int, default=None,
                     help="with --only: mesh size (cube edge / prism base edge)")

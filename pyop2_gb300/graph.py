@@ -24,14 +24,16 @@ class LoopGraph:
         if not loops:
             raise ValueError("LoopGraph needs at least one loop")
         self.loops = list(loops)
+        # a loop recorded several times is refreshed and marked once per replay
+        self._distinct = list({id(lp): lp for lp in self.loops}.values())
         self.handle = None
         self._record()
 
     def _record(self):
         self._destroy()
-        for lp in self.loops:
+        for lp in self._distinct:
             lp._prepare_capture()
-        self._keys = [lp._capture_key() for lp in self.loops]
+        self._keys = [lp._capture_key() for lp in self._distinct]
         s = ctypes.c_void_p()
         _lib.call("op2g_graph_begin", ctypes.byref(s))
         failure = None
@@ -59,12 +61,12 @@ class LoopGraph:
     def replay(self):
         """Upload host-side changes, run the graph, mark the written
         arguments (re-recording first if an argument moved)."""
-        for lp in self.loops:
+        for lp in self._distinct:
             lp._refresh()
-        if [lp._capture_key() for lp in self.loops] != self._keys:
+        if [lp._capture_key() for lp in self._distinct] != self._keys:
             self._record()
         self.launch()
-        for lp in self.loops:
+        for lp in self._distinct:
             lp.mark_written()
 
     def _destroy(self):
