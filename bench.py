@@ -640,6 +640,75 @@ def measure_small(op2, calls=500, with_cpu=True):
     return out
 
 
+def cpu_sections(reps=2):
+    """The secondary configurations on ONE host core, through the oracle (the
+    reference's CPU path restated in C and compiled with the reference's
+    flags), each on a bounded sample of its workload: rates in the units the
+    GPU sections report, to sit beside them."""
+    from oracle import op2 as O
+    from pyop2_gb300 import meshes
+    from pyop2_gb300 import workloads as W
+
+    def best(fn):
+        b = None
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            dt = time.perf_counter() - t0
+            b = dt if b is None else min(b, dt)
+        return b
+
+    def loop(*a, **kw):
+        return O.ParLoop(*a, profile="timing", **kw)
+
+    out = {}
+    # configuration 2b: sparsity build and CSR assembly, 48^3 x 6 tets
+    p = W.build_p1_3d(O, n=48, seed=0)
+    C = p["cells"].size
+    built = []
+    t_sp = best(lambda: built.append(O.Sparsity((p["verts"] ** 1, p["verts"] ** 1),
+                                                [(p["c2v"], p["c2v"], None)])))
+    sp = built[-1]
+    A = O.Mat(sp)
+    asm = loop(O.Kernel(W.P1_3D_LAPLACE_MATRIX, "p1_laplace_3d_mat"), p["cells"],
+               A(O.INC, (p["c2v"], p["c2v"])), p["X"](O.READ, p["c2v"]))
+    t_asm = best(asm.compute)
+    out["sparsity_assembly"] = {"sample": "48^3 x 6 = %d tets, %d nonzeros" % (C, len(sp.colidx)),
+                                "sparsity_nnz_per_s": len(sp.colidx) / t_sp,
+                                "assembly_cells_per_s": C / t_asm}
+    # configuration 4: residual and its VJP, 32^3 x 6 tets
+    q = W.build_nonlinear(O, n=32, seed=0)
+    V, C = q["verts"].total_size, q["cells"].size
+    c2v, X = q["c2v"], q["X"]
+    F, du = O.Dat(q["verts"], np.zeros(V)), O.Dat(q["verts"], np.zeros(V))
+    lam, u = O.Dat(q["verts"], q["lam"]), O.Dat(q["verts"], q["u"])
+    k, dk = O.Dat(q["cells"], q["kappa"]), O.Dat(q["cells"], np.zeros(C))
+    fwd = loop(O.Kernel(W.NL_RESIDUAL, "nl_residual"), q["cells"], F(O.INC, c2v),
+               X(O.READ, c2v), u(O.READ, c2v), k(O.READ))
+    bwd = loop(O.Kernel(W.NL_RESIDUAL_VJP, "nl_residual_vjp"), q["cells"], lam(O.READ, c2v),
+               X(O.READ, c2v), u(O.READ, c2v), k(O.READ), du(O.INC, c2v), dk(O.WRITE))
+    out["adjoint"] = {"sample": "32^3 x 6 = %d tets" % C,
+                      "forward_cells_per_s": C / best(fwd.compute),
+                      "adjoint_cells_per_s": C / best(bwd.compute)}
+    # configuration 3: the first 24 meshes of the batch, one loop each
+    sizes = meshes.batch_sizes(256, seed=0)[:24]
+    probs = W.build_p2_batch(O, sizes, seed=0)
+    loops = [loop(b["kernel"], b["cells"], *b["args"]) for b in probs]
+    ncells = sum(b["cells"].size for b in probs)
+    out["batch"] = {"sample": "the first 24 of the 256 meshes, %d cells" % ncells,
+                    "cells_per_s": ncells / best(lambda: [lp.compute() for lp in loops])}
+    # configuration 5: prism action with 8 RHS, 32^2 x 2 x 64 prisms
+    r = W.build_prisms(O, n=32, layers=65, seed=0)
+    ds = O.DataSet(r["nodes"], (r["nrhs"], 3))
+    ur, yr = O.Dat(ds, r["u"]), O.Dat(ds)
+    act = loop(O.Kernel(W.PRISM_ELASTICITY_ACTION, "prism_elasticity"), r["cells"],
+               yr(O.INC, r["c2n"]), r["X"](O.READ, r["c2n"]), ur(O.READ, r["c2n"]),
+               r["L"](O.READ, r["c2c"]))
+    out["prisms"] = {"sample": "32^2 x 2 x 64 = %d prisms x %d RHS" % (r["ncell"], r["nrhs"]),
+                     "action_cell_rhs_per_s": r["ncell"] * r["nrhs"] / best(act.compute)}
+    return out
+
+
 def measure_data_path(op2, p, steps, warmup):
     """Loops with (almost) no arithmetic on the benchmark mesh, to show the
     wrapper's memory path against HBM where FP64 is not the limit: a direct
@@ -810,6 +879,12 @@ def run_ours(args):
     adjoint = measure_adjoint(op2, max(args.steps, 5), 3) if not args.skip_extras else None
     batch = measure_batch(op2, 5, 3) if not args.skip_extras else None
     prisms = measure_prisms(op2, 5, 2) if not args.skip_extras else None
+    if not args.skip_extras and not args.no_cpu_baseline and world == 1:
+        # the same configurations on one host core, beside each GPU section
+        cs = cpu_sections()
+        for sec, key in ((sparsity, "sparsity_assembly"), (adjoint, "adjoint"),
+                         (batch, "batch"), (prisms, "prisms")):
+            sec["cpu_1core"] = cs[key]
     cpu = None
     if not args.no_cpu_baseline:
         coords = p["coords"]

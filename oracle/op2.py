@@ -388,6 +388,12 @@ class Sparsity:
         S = _Sp(rds.set.size, cds.set.size, 1 if set_diag else 0, 1 if extr else 0, const,
                 periodic, layers.ctypes.data if layers is not None else None, len(triples), pairs)
         lib = _build.liboracle()
+        # full prototypes: without them ctypes passes a Python int as a C int,
+        # truncating any address above 2^31
+        lib.oracle_sparsity_build.argtypes = [
+            ctypes.POINTER(_Sp), ctypes.c_void_p,
+            ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)), ctypes.POINTER(ctypes.c_int64)]
+        lib.oracle_free.argtypes = [ctypes.c_void_p]
         rowptr = np.zeros(S.nrows + 1, dtype=np.int64)
         col = ctypes.POINTER(ctypes.c_int32)()
         nnz = ctypes.c_int64()
