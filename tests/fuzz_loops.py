@@ -344,6 +344,13 @@ def make_mat_spec(seed):
             spec["layers"] = np.minimum(layers, LTOP).astype(np.int32)
         else:
             spec["layers"] = int(rng.integers(2, LTOP + 1))
+            if kind == "periodic":
+                # at least 2 cell layers: with one, the reference's wrappers
+                # (a remainder by one conditional subtraction,
+                # pyop2/codegen/builder.py:27-30) and its sparsity (a true
+                # modulo, pyop2/sparsity.pyx:376-384) place interior-facet
+                # entries with offset quotients differently
+                spec["layers"] = max(spec["layers"], 3)
         spec["periodic"] = kind == "periodic"
 
     def a_map(n_to):
