@@ -881,7 +881,12 @@ def run_ours(args):
     prisms = measure_prisms(op2, 5, 2) if not args.skip_extras else None
     if not args.skip_extras and not args.no_cpu_baseline and world == 1:
         # the same configurations on one host core, beside each GPU section
-        cs = cpu_sections()
+        # (a failure there is reported in the line, not fatal to it)
+        try:
+            cs = cpu_sections()
+        except Exception as e:
+            cs = {k: {"error": repr(e)[:200]} for k in
+                  ("sparsity_assembly", "adjoint", "batch", "prisms")}
         for sec, key in ((sparsity, "sparsity_assembly"), (adjoint, "adjoint"),
                          (batch, "batch"), (prisms, "prisms")):
             sec["cpu_1core"] = cs[key]
