@@ -2,8 +2,9 @@
 
 ``make_spec(seed)`` draws one loop: an iteration set with random
 core/owned/total sizes (or a Subset of one), up to three target sets, maps of
-arity 1-4 (one of them, sometimes, a bijection onto a set as large as the
-iteration set), and one to six arguments -- direct Dats (READ, WRITE, RW,
+arity 1-4 (sometimes also a PermutedMap of one of them, a ComposedMap through
+an intermediate set, and a bijection onto a set as large as the iteration
+set), and one to six arguments -- direct Dats (READ, WRITE, RW,
 INC), indirect Dats (READ, INC, MIN, MAX; WRITE and RW only through the
 bijection, where the result does not depend on the order of iteration) and
 Globals (READ, INC, MIN, MAX) -- of dimension 1-3 and dtype float64 or int32.
@@ -21,7 +22,8 @@ direct arguments pointing at the entity; pyop2/parloop.py:243-260: entities
 
 ``make_extruded_spec(seed)`` / ``run_extruded(op2, spec)`` draw and run the
 extruded counterpart: a column mesh (constant or per-entity layers, or
-periodic), an iteration region, maps with per-entry layer offsets (and
+periodic), iterated whole or through a Subset of its columns, an iteration
+region, maps with per-entry layer offsets (and
 offset quotients when periodic), the layer argument or not, and arguments
 whose results do not depend on the order of iteration (indirect READ, INC,
 MIN, MAX; direct READ and INC on the base set; Globals).  They are compared
@@ -52,6 +54,21 @@ def make_spec(seed):
         a = int(rng.integers(1, 5))
         maps.append({"target": t, "arity": a,
                      "values": rng.integers(0, targets[t], (total, a)).astype(np.int32)})
+    # index transforms: a PermutedMap of a plain map, and a ComposedMap
+    # (an arity-1 map into an intermediate set, then a plain map from it)
+    if rng.random() < 0.4:
+        b = int(rng.integers(0, len(maps)))
+        perm = rng.permutation(maps[b]["arity"]).astype(np.int32)
+        maps.append({"kind": "perm", "base": b, "perm": perm, "target": maps[b]["target"],
+                     "arity": maps[b]["arity"], "values": maps[b]["values"][:, perm]})
+    if rng.random() < 0.4:
+        ni = int(rng.integers(1, 40))
+        t = int(rng.integers(0, len(targets)))
+        a = int(rng.integers(1, 5))
+        outer = rng.integers(0, targets[t], (ni, a)).astype(np.int32)
+        inner = rng.integers(0, ni, (total, 1)).astype(np.int32)
+        maps.append({"kind": "composed", "ni": ni, "outer": outer, "inner": inner, "target": t,
+                     "arity": a, "values": outer[inner[:, 0]].reshape(total, a)})
     bij = None
     if total > 0 and rng.random() < 0.35:
         targets.append(total)
@@ -134,8 +151,19 @@ def run(op2, spec):
     core, owned, total = spec["sizes"]
     iterset = op2.Set((core, owned, total), "it")
     targets = [op2.Set(n, "t%d" % i) for i, n in enumerate(spec["targets"])]
-    maps = [op2.Map(iterset, targets[m["target"]], m["arity"], m["values"], "m%d" % i)
-            for i, m in enumerate(spec["maps"])]
+    maps = []
+    for i, m in enumerate(spec["maps"]):
+        kind = m.get("kind", "plain")
+        if kind == "perm":
+            maps.append(op2.PermutedMap(maps[m["base"]], m["perm"]))
+        elif kind == "composed":
+            mid = op2.Set(m["ni"], "mid%d" % i)
+            outer = op2.Map(mid, targets[m["target"]], m["arity"], m["outer"], "o%d" % i)
+            inner = op2.Map(iterset, mid, 1, m["inner"], "i%d" % i)
+            maps.append(op2.ComposedMap(outer, inner))
+        else:
+            maps.append(op2.Map(iterset, targets[m["target"]], m["arity"], m["values"],
+                                "m%d" % i))
     objs, largs = [], []
     for a in spec["args"]:
         dt = np.dtype(a["dtype"])
@@ -278,9 +306,12 @@ def make_extruded_spec(seed):
             init = init * 1000
         args.append({"kind": k, "dtype": dtype, "dim": dim, "access": acc, "map": mp,
                      "init": init})
+    subset = None
+    if nb > 0 and rng.random() < 0.25:
+        subset = np.sort(rng.choice(nb, int(rng.integers(0, nb + 1)), replace=False))
     spec = {"seed": 10_000 + seed, "nb": nb, "layers": layers, "periodic": kind == "periodic",
             "region": region, "nfacets": nf, "layer_arg": bool(rng.random() < 0.5),
-            "targets": targets, "maps": maps, "args": args}
+            "targets": targets, "maps": maps, "args": args, "subset": subset}
     spec["code"], spec["name"] = kernel_code(spec)
     return spec
 
@@ -311,7 +342,8 @@ def run_extruded(op2, spec):
         d = op2.Dat(s ** a["dim"], a["init"].astype(dt), dt)
         objs.append(d)
         largs.append(d(acc) if a["map"] is None else d(acc, maps[a["map"]]))
-    op2.par_loop(op2.Kernel(spec["code"], spec["name"]), ext, *largs,
+    it = ext if spec.get("subset") is None else op2.Subset(ext, spec["subset"])
+    op2.par_loop(op2.Kernel(spec["code"], spec["name"]), it, *largs,
                  iteration_region=getattr(op2, spec["region"]),
                  pass_layer_arg=spec["layer_arg"])
     return _results(objs, spec)

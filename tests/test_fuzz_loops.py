@@ -29,7 +29,8 @@ def test_oracle_matches_model(oracle_op2, seed):
 
 def test_specs_cover_every_access_and_shape():
     """The seeds above draw every access mode of every argument kind, both
-    dtypes, Subsets, empty iteration sets and the bijective map."""
+    dtypes, plain, permuted and composed maps, Subsets, empty iteration sets
+    and the bijective map."""
     seen = set()
     subset = empty = bij = False
     for seed in CPU_SEEDS:
@@ -42,8 +43,11 @@ def test_specs_cover_every_access_and_shape():
         for a in s["args"]:
             seen.add((a["kind"], a["access"]))
             seen.add(a["dtype"])
+            if a["map"] is not None:
+                seen.add(("map", s["maps"][a["map"]].get("kind", "plain")))
     want = {("direct", x) for x in F.DIRECT_ACCESS} | {("global", x) for x in F.GLOBAL_ACCESS} \
-        | {("indirect", x) for x in F.INDIRECT_ACCESS} | {"float64", "int32"}
+        | {("indirect", x) for x in F.INDIRECT_ACCESS} | {"float64", "int32"} \
+        | {("map", k) for k in ("plain", "perm", "composed")}
     assert want <= seen
     assert subset and empty and bij
 
@@ -66,8 +70,8 @@ def test_gpu_matches_oracle(gpu_op2, oracle_op2, strategy, seed):
 
 def test_extruded_specs_cover_regions_and_layouts(oracle_op2):
     """The seeds draw every iteration region, every layer layout (constant,
-    per-entity, periodic) and both settings of the layer argument; each
-    spec runs on the oracle."""
+    per-entity, periodic), Subsets of columns and both settings of the layer
+    argument; each spec runs on the oracle."""
     seen = set()
     for seed in GPU_SEEDS:
         s = F.make_extruded_spec(seed)
@@ -75,12 +79,14 @@ def test_extruded_specs_cover_regions_and_layouts(oracle_op2):
             ("constant" if isinstance(s["layers"], int) else "variable")
         seen.add((s["region"], lay))
         seen.add(("layer_arg", s["layer_arg"]))
+        seen.add(("subset", s["subset"] is not None))
         F.run_extruded(oracle_op2, s)
     regions = {r for r, lay in seen if r in F.REGIONS}
     layouts = {lay for r, lay in seen if r in F.REGIONS}
     assert regions == set(F.REGIONS)
     assert layouts == {"constant", "variable", "periodic"}
     assert ("layer_arg", True) in seen and ("layer_arg", False) in seen
+    assert ("subset", True) in seen
 
 
 @pytest.mark.gpu
