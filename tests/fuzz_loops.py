@@ -6,8 +6,10 @@ arity 1-4 (sometimes also a PermutedMap of one of them, a ComposedMap through
 an intermediate set, and a bijection onto a set as large as the iteration
 set), and one to six arguments -- direct Dats (READ, WRITE, RW,
 INC), indirect Dats (READ, INC, MIN, MAX; WRITE and RW only through the
-bijection, where the result does not depend on the order of iteration) and
-Globals (READ, INC, MIN, MAX) -- of dimension 1-3 and dtype float64 or int32.
+bijection, where the result does not depend on the order of iteration),
+Globals (READ, INC, MIN, MAX) and sometimes a MixedDat through a MixedMap
+(READ or INC, one concatenated pack) -- of dimension 1-3 and dtype float64
+or int32.
 The kernel is generated C: it sums its inputs with fixed integer weights and
 writes integer-valued results into every written argument, so every
 implementation must agree bit for bit whatever its order of summation.
@@ -99,6 +101,22 @@ def make_spec(seed):
             init = init * 1000
         args.append({"kind": kind, "dtype": dtype, "dim": dim, "access": acc, "map": mp,
                      "init": init})
+    if rng.random() < 0.3:
+        # a MixedDat argument through a MixedMap: 2-3 components, each on its
+        # own set through its own map, one concatenated pack
+        comps = []
+        for _ in range(int(rng.integers(2, 4))):
+            targets.append(int(rng.integers(1, 30)))
+            a = int(rng.integers(1, 4))
+            maps.append({"target": len(targets) - 1, "arity": a,
+                         "values": rng.integers(0, targets[-1], (total, a)).astype(np.int32)})
+            dim = int(rng.integers(1, 4))
+            comps.append({"map": len(maps) - 1, "dim": dim,
+                          "init": rng.integers(-4, 5, (targets[-1], dim))})
+        args.insert(int(rng.integers(0, len(args) + 1)),
+                    {"kind": "mixed", "dtype": "float64", "access": str(rng.choice(["READ", "INC"])),
+                     "map": None, "dim": None, "comps": comps,
+                     "init": np.concatenate([c["init"].reshape(-1) for c in comps])})
     spec = {"seed": seed, "sizes": (core, owned, total), "subset": subset, "targets": targets,
             "maps": maps, "args": args}
     spec["code"], spec["name"] = kernel_code(spec)
@@ -106,6 +124,8 @@ def make_spec(seed):
 
 
 def _width(spec, a):
+    if a["kind"] == "mixed":
+        return sum(spec["maps"][c["map"]]["arity"] * c["dim"] for c in a["comps"])
     if a["map"] is None:
         return a["dim"]
     return spec.get("nfacets", 1) * spec["maps"][a["map"]]["arity"] * a["dim"]
@@ -173,6 +193,13 @@ def run(op2, spec):
             objs.append(g)
             largs.append(g(acc))
             continue
+        if a["kind"] == "mixed":
+            dats = [op2.Dat(targets[spec["maps"][c["map"]]["target"]] ** c["dim"],
+                            c["init"].astype(dt), dt) for c in a["comps"]]
+            md = op2.MixedDat(dats)
+            objs.append(md)
+            largs.append(md(acc, op2.MixedMap([maps[c["map"]] for c in a["comps"]])))
+            continue
         s = iterset if a["map"] is None else targets[spec["maps"][a["map"]]["target"]]
         d = op2.Dat(s ** a["dim"], a["init"].astype(dt), dt)
         objs.append(d)
@@ -185,14 +212,23 @@ def run(op2, spec):
 def _results(objs, spec):
     # every entry, ghosts included (the reference's data_ro stops at the
     # owned entries; the oracle keeps no such distinction)
-    return [np.array(o.data_ro).reshape(-1) if a["kind"] == "global"
-            else np.array(getattr(o, "data_ro_with_halos", o.data_ro)).reshape(a["init"].shape)
-            for o, a in zip(objs, spec["args"])]
+    out = []
+    for o, a in zip(objs, spec["args"]):
+        if a["kind"] == "global":
+            out.append(np.array(o.data_ro).reshape(-1))
+        elif a["kind"] == "mixed":
+            out.append(np.concatenate([
+                np.array(getattr(d, "data_ro_with_halos", d.data_ro)).reshape(-1) for d in o]))
+        else:
+            out.append(np.array(getattr(o, "data_ro_with_halos", o.data_ro))
+                       .reshape(a["init"].shape))
+    return out
 
 
 def model(spec):
     core, owned, total = spec["sizes"]
-    data = [a["init"].astype(a["dtype"]).copy() for a in spec["args"]]
+    data = [[c["init"].astype(a["dtype"]).copy() for c in a["comps"]] if a["kind"] == "mixed"
+            else a["init"].astype(a["dtype"]).copy() for a in spec["args"]]
     ents = range(owned) if spec["subset"] is None else spec["subset"]
     for e in ents:
         e = int(e)
@@ -200,6 +236,9 @@ def model(spec):
         for a in spec["args"]:
             if a["kind"] == "global":
                 rows.append(None)
+            elif a["kind"] == "mixed":
+                rows.append([[int(v) for v in spec["maps"][c["map"]]["values"][e]]
+                             for c in a["comps"]])
             elif a["map"] is None:
                 rows.append([e])
             else:
@@ -208,6 +247,11 @@ def model(spec):
         for k, a in enumerate(spec["args"]):
             if a["kind"] == "global":
                 p = data[k].astype(np.float64).copy()
+            elif a["kind"] == "mixed":
+                p = np.concatenate([data[k][ci][r] for ci, rr in enumerate(rows[k])
+                                    for r in rr]).astype(np.float64)
+                if a["access"] == "INC":
+                    p[:] = 0
             else:
                 p = np.concatenate([data[k][r] for r in rows[k]]).astype(np.float64)
             if a["access"] == "INC" and a["map"] is not None:
@@ -233,6 +277,14 @@ def model(spec):
                     p[i] = max(p[i], cast(s - i + k))
             if acc == "READ":
                 continue
+            if a["kind"] == "mixed":        # INC, component by component
+                o = 0
+                for ci, rr in enumerate(rows[k]):
+                    d = a["comps"][ci]["dim"]
+                    for r in rr:
+                        data[k][ci][r] += p[o:o + d]
+                        o += d
+                continue
             if a["kind"] == "global":
                 if acc == "INC":
                     data[k] += (p - data[k].astype(np.float64)).astype(data[k].dtype)
@@ -250,7 +302,8 @@ def model(spec):
                     data[k][r] = np.maximum(data[k][r], chunk.astype(data[k].dtype))
                 else:
                     data[k][r] = chunk.astype(data[k].dtype)
-    return [x.reshape(-1) if a["kind"] == "global" else x.reshape(a["init"].shape)
+    return [np.concatenate([c.reshape(-1) for c in x]) if a["kind"] == "mixed"
+            else x.reshape(-1) if a["kind"] == "global" else x.reshape(a["init"].shape)
             for x, a in zip(data, spec["args"])]
 
 

@@ -1,6 +1,6 @@
 """Randomised differential tests of par_loop: random sets, maps and argument
-lists (every access mode, direct and indirect, Globals, dims 1-3, float64 and
-int32, core/owned/total splits, Subsets, and extruded column meshes under
+lists (every access mode, direct and indirect, Globals, MixedDats through
+MixedMaps, dims 1-3, float64 and int32, core/owned/total splits, Subsets, and extruded column meshes under
 every iteration region) with a generated kernel whose results are integers.
 The oracle must equal the access-semantics model bit for bit (CPU), and the
 GPU must equal the oracle bit for bit under every INC strategy."""
@@ -29,8 +29,8 @@ def test_oracle_matches_model(oracle_op2, seed):
 
 def test_specs_cover_every_access_and_shape():
     """The seeds above draw every access mode of every argument kind, both
-    dtypes, plain, permuted and composed maps, Subsets, empty iteration sets
-    and the bijective map."""
+    dtypes, plain, permuted and composed maps, MixedDat arguments, Subsets,
+    empty iteration sets and the bijective map."""
     seen = set()
     subset = empty = bij = False
     for seed in CPU_SEEDS:
@@ -47,7 +47,8 @@ def test_specs_cover_every_access_and_shape():
                 seen.add(("map", s["maps"][a["map"]].get("kind", "plain")))
     want = {("direct", x) for x in F.DIRECT_ACCESS} | {("global", x) for x in F.GLOBAL_ACCESS} \
         | {("indirect", x) for x in F.INDIRECT_ACCESS} | {"float64", "int32"} \
-        | {("map", k) for k in ("plain", "perm", "composed")}
+        | {("map", k) for k in ("plain", "perm", "composed")} \
+        | {("mixed", "READ"), ("mixed", "INC")}
     assert want <= seen
     assert subset and empty and bij
 
