@@ -556,7 +556,23 @@ def measure_prisms(op2, steps, warmup, n=256):
     e1.record()
     e1.synchronize()
     t_graph = e0.elapsed_time(e1) / steps
-    # BAIJ sparsity + assembly
+    C = p["ncell"]
+    out = {"workload": "prism_elasticity_%dx%dx64_8rhs" % (n, n), "cells": C, "nodes": p["nnodes"],
+           "rhs": NR, "action_ms": t_act, "adjoint_ms": t_adj,
+           "graph_action_adjoint_ms": t_graph,
+           "action_cell_rhs_per_s": C * NR / (t_act * 1e-3),
+           "adjoint_over_action": t_adj / t_act}
+    out.update(measure_prism_assembly(op2, p))
+    return out
+
+
+def measure_prism_assembly(op2, p=None, n=256):
+    """BAIJ 3x3 sparsity, assembly of the 18x18 prism elasticity matrices and
+    SpMV on the extruded prism mesh (built here unless given)."""
+    from pyop2_gb300 import workloads as W
+    if p is None:
+        p = W.build_prisms(op2, n=n, layers=65, seed=0)
+    nodes, cells, c2n, c2c = p["nodes"], p["cells"], p["c2n"], p["c2c"]
     t_sp, sp = _time_sparsity_build((nodes ** 3, nodes ** 3), [(c2n, c2n, None)])
     A = op2.Mat(sp)
     asm = op2.ParLoop(op2.Kernel(W.PRISM_ELASTICITY_MATRIX, "prism_elasticity_mat"), cells,
@@ -564,15 +580,9 @@ def measure_prisms(op2, steps, warmup, n=256):
     t_asm = _time_loop(asm, 2, 1)
     xs = op2.Dat(nodes ** 3, np.random.default_rng(0).uniform(-1, 1, (p["nnodes"], 3)))
     t_spmv, gbs = _time_spmv(op2, A, xs, 5, 3)
-    C = p["ncell"]
-    out = {"workload": "prism_elasticity_%dx%dx64_8rhs" % (n, n), "cells": C, "nodes": p["nnodes"],
-           "rhs": NR, "action_ms": t_act, "adjoint_ms": t_adj,
-           "graph_action_adjoint_ms": t_graph,
-           "action_cell_rhs_per_s": C * NR / (t_act * 1e-3),
-           "adjoint_over_action": t_adj / t_act,
-           "baij_blocks": sp.nblocks, "sparsity_build_ms": t_sp,
-           "assembly_ms": t_asm, "values_gb": sp.nblocks * 9 * 8 / 1e9,
-           "spmv_ms": t_spmv, "spmv_gbs": gbs}
+    out = {"baij_blocks": sp.nblocks, "sparsity_build_ms": t_sp,
+           "assembly_ms": t_asm, "assembly_cells_per_s": p["ncell"] / (t_asm * 1e-3),
+           "values_gb": sp.nblocks * 9 * 8 / 1e9, "spmv_ms": t_spmv, "spmv_gbs": gbs}
     del A, sp
     return out
 
@@ -958,6 +968,8 @@ def run_only(args):
         out = measure_batch(op2, args.steps, args.warmup)
     elif args.only == "small":
         out = measure_small(op2, with_cpu=False)
+    elif args.only == "prism_assembly":
+        out = measure_prism_assembly(op2, n=args.size or 256)
     else:
         out = measure_prisms(op2, args.steps, args.warmup, n=args.size or 256)
     print(json.dumps({"only": args.only, "result": out}), flush=True)
@@ -976,7 +988,8 @@ def main():
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the headline action (no adjoint / batch measurements)")
     ap.add_argument("--only", default=None,
-                    choices=["sparsity", "adjoint", "batch", "prisms", "small"],
+                    choices=["sparsity", "adjoint", "batch", "prisms", "small",
+                             "prism_assembly"],
                     help="run one secondary measurement alone (profiling runs)")
     ap.add_argument("--size", type=int, default=None,
                     help="with --only: mesh size (cube edge / prism base edge)")
