@@ -143,3 +143,30 @@ def test_gpu_mat_matches_oracle(gpu_op2, oracle_op2, seed):
     and SpMV (exact: integer values) against the oracle."""
     spec = F.make_mat_spec(seed)
     _equal_mat(F.run_mat(gpu_op2, spec), F.run_mat(oracle_op2, spec))
+
+
+LAUNCH_CONFIGS = [dict(block_size=128, prefetch=1, grid=0),
+                  dict(block_size=512, prefetch=0, grid=-1),
+                  dict(block_size=64, prefetch=1, grid=3)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfg", LAUNCH_CONFIGS, ids=["bs128-pf", "bs512-uncapped", "bs64-pf-grid3"])
+@pytest.mark.parametrize("seed", range(0, 48, 4))
+def test_gpu_matches_oracle_launch_configs(gpu_op2, oracle_op2, cfg, seed):
+    """Other CTA sizes, map-row prefetch and grid policies (uncapped, and 3
+    CTAs striding over everything) under the atomic and warp strategies."""
+    from pyop2_gb300.configuration import configuration
+    old = {k: configuration[k] for k in list(cfg) + ["scatter"]}
+    try:
+        for k, v in cfg.items():
+            configuration[k] = v
+        for sc in ("atomic", "warp"):
+            configuration["scatter"] = sc
+            spec = F.make_spec(seed)
+            _equal(F.run(gpu_op2, spec), F.run(oracle_op2, spec))
+            spec = F.make_extruded_spec(seed)
+            _equal(F.run_extruded(gpu_op2, spec), F.run_extruded(oracle_op2, spec))
+    finally:
+        for k, v in old.items():
+            configuration[k] = v
