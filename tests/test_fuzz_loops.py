@@ -170,3 +170,21 @@ def test_gpu_matches_oracle_launch_configs(gpu_op2, oracle_op2, cfg, seed):
     finally:
         for k, v in old.items():
             configuration[k] = v
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", range(1, 48, 6))
+def test_gpu_autotuned_matches_oracle(gpu_op2, oracle_op2, seed):
+    """configuration['scatter'] = 'auto': the autotuner runs every candidate
+    on the loop's own arguments and restores them; the result must still be
+    the oracle's, bit for bit."""
+    from pyop2_gb300.configuration import configuration
+    old = configuration["scatter"]
+    configuration["scatter"] = "auto"
+    try:
+        spec = F.make_spec(seed)
+        _equal(F.run(gpu_op2, spec), F.run(oracle_op2, spec))
+        spec = F.make_extruded_spec(seed)
+        _equal(F.run_extruded(gpu_op2, spec), F.run_extruded(oracle_op2, spec))
+    finally:
+        configuration["scatter"] = old
