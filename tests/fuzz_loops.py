@@ -39,82 +39,90 @@ BIJECTION_ACCESS = ["READ", "INC", "MIN", "MAX", "WRITE", "RW"]
 GLOBAL_ACCESS = ["READ", "INC", "MIN", "MAX"]
 
 
-def make_spec(seed):
-    rng = np.random.default_rng(seed)
-    total = int(rng.integers(0, 160))
-    owned = int(rng.integers(0, total + 1))
-    core = int(rng.integers(0, owned + 1))
+def make_spec(seed, data_seed=None):
+    """One random loop.  The signature (argument kinds, accesses, dims,
+    dtypes, map kinds and arities) is drawn from `seed`; sizes, map values
+    and data from `data_seed` (default: derived from `seed`), so that specs
+    sharing a seed and differing in data_seed are loops of one signature
+    over different meshes (a batch)."""
+    rs = np.random.default_rng(seed)
+    rd = np.random.default_rng(1_000_000 + (seed if data_seed is None else data_seed))
+    want_subset = rs.random() < 0.25
+    want_bij = rs.random() < 0.35
+    total = int(rd.integers(1 if want_bij else 0, 160))
+    owned = int(rd.integers(0, total + 1))
+    core = int(rd.integers(0, owned + 1))
     subset = None
-    if rng.random() < 0.25:
+    if want_subset:
         # a Subset iterates its own indices, all of them owned
         core = owned = total
-        subset = np.sort(rng.choice(total, int(rng.integers(0, total + 1)), replace=False))
-    targets = [int(rng.integers(1, 60)) for _ in range(int(rng.integers(1, 4)))]
+        subset = np.sort(rd.choice(total, int(rd.integers(0, total + 1)), replace=False))
+    targets = [int(rd.integers(1, 60)) for _ in range(int(rs.integers(1, 4)))]
     maps = []
-    for _ in range(int(rng.integers(1, 4))):
-        t = int(rng.integers(0, len(targets)))
-        a = int(rng.integers(1, 5))
+    for _ in range(int(rs.integers(1, 4))):
+        t = int(rs.integers(0, len(targets)))
+        a = int(rs.integers(1, 5))
         maps.append({"target": t, "arity": a,
-                     "values": rng.integers(0, targets[t], (total, a)).astype(np.int32)})
+                     "values": rd.integers(0, targets[t], (total, a)).astype(np.int32)})
     # index transforms: a PermutedMap of a plain map, and a ComposedMap
     # (an arity-1 map into an intermediate set, then a plain map from it)
-    if rng.random() < 0.4:
-        b = int(rng.integers(0, len(maps)))
-        perm = rng.permutation(maps[b]["arity"]).astype(np.int32)
+    if rs.random() < 0.4:
+        b = int(rs.integers(0, len(maps)))
+        perm = rs.permutation(maps[b]["arity"]).astype(np.int32)
         maps.append({"kind": "perm", "base": b, "perm": perm, "target": maps[b]["target"],
                      "arity": maps[b]["arity"], "values": maps[b]["values"][:, perm]})
-    if rng.random() < 0.4:
-        ni = int(rng.integers(1, 40))
-        t = int(rng.integers(0, len(targets)))
-        a = int(rng.integers(1, 5))
-        outer = rng.integers(0, targets[t], (ni, a)).astype(np.int32)
-        inner = rng.integers(0, ni, (total, 1)).astype(np.int32)
+    if rs.random() < 0.4:
+        ni = int(rd.integers(1, 40))
+        t = int(rs.integers(0, len(targets)))
+        a = int(rs.integers(1, 5))
+        outer = rd.integers(0, targets[t], (ni, a)).astype(np.int32)
+        inner = rd.integers(0, ni, (total, 1)).astype(np.int32)
         maps.append({"kind": "composed", "ni": ni, "outer": outer, "inner": inner, "target": t,
                      "arity": a, "values": outer[inner[:, 0]].reshape(total, a)})
     bij = None
-    if total > 0 and rng.random() < 0.35:
+    if want_bij:
         targets.append(total)
         bij = len(maps)
         maps.append({"target": len(targets) - 1, "arity": 1,
-                     "values": rng.permutation(total).astype(np.int32).reshape(total, 1)})
+                     "values": rd.permutation(total).astype(np.int32).reshape(total, 1)})
     args = []
-    for _ in range(int(rng.integers(1, 7))):
-        kind = rng.choice(["direct", "indirect", "global"], p=[0.3, 0.45, 0.25])
-        dtype = "float64" if rng.random() < 0.75 else "int32"
-        dim = int(rng.integers(1, 4))
+    for _ in range(int(rs.integers(1, 7))):
+        kind = rs.choice(["direct", "indirect", "global"], p=[0.3, 0.45, 0.25])
+        dtype = "float64" if rs.random() < 0.75 else "int32"
+        dim = int(rs.integers(1, 4))
         if kind == "direct":
-            acc = str(rng.choice(DIRECT_ACCESS))
+            acc = str(rs.choice(DIRECT_ACCESS))
             mp = None
         elif kind == "indirect":
-            mp = int(rng.integers(0, len(maps)))
-            acc = str(rng.choice(BIJECTION_ACCESS if mp == bij else INDIRECT_ACCESS))
+            mp = int(rs.integers(0, len(maps)))
+            acc = str(rs.choice(BIJECTION_ACCESS if mp == bij else INDIRECT_ACCESS))
         else:
-            acc = str(rng.choice(GLOBAL_ACCESS))
+            acc = str(rs.choice(GLOBAL_ACCESS))
             mp = None
         if kind == "global":
             shape = (dim,)
         else:
             size = total if mp is None else targets[maps[mp]["target"]]
             shape = (size, dim)
-        init = rng.integers(-4, 5, shape)
+        init = rd.integers(-4, 5, shape)
         if kind == "global" and acc in ("MIN", "MAX"):
             init = init * 1000
         args.append({"kind": kind, "dtype": dtype, "dim": dim, "access": acc, "map": mp,
                      "init": init})
-    if rng.random() < 0.3:
+    if rs.random() < 0.3:
         # a MixedDat argument through a MixedMap: 2-3 components, each on its
         # own set through its own map, one concatenated pack
         comps = []
-        for _ in range(int(rng.integers(2, 4))):
-            targets.append(int(rng.integers(1, 30)))
-            a = int(rng.integers(1, 4))
+        for _ in range(int(rs.integers(2, 4))):
+            targets.append(int(rd.integers(1, 30)))
+            a = int(rs.integers(1, 4))
             maps.append({"target": len(targets) - 1, "arity": a,
-                         "values": rng.integers(0, targets[-1], (total, a)).astype(np.int32)})
-            dim = int(rng.integers(1, 4))
+                         "values": rd.integers(0, targets[-1], (total, a)).astype(np.int32)})
+            dim = int(rs.integers(1, 4))
             comps.append({"map": len(maps) - 1, "dim": dim,
-                          "init": rng.integers(-4, 5, (targets[-1], dim))})
-        args.insert(int(rng.integers(0, len(args) + 1)),
-                    {"kind": "mixed", "dtype": "float64", "access": str(rng.choice(["READ", "INC"])),
+                          "init": rd.integers(-4, 5, (targets[-1], dim))})
+        args.insert(int(rs.integers(0, len(args) + 1)),
+                    {"kind": "mixed", "dtype": "float64", "access": str(rs.choice(["READ", "INC"])),
                      "map": None, "dim": None, "comps": comps,
                      "init": np.concatenate([c["init"].reshape(-1) for c in comps])})
     spec = {"seed": seed, "sizes": (core, owned, total), "subset": subset, "targets": targets,
@@ -168,6 +176,30 @@ def kernel_code(spec):
 
 
 def run(op2, spec):
+    knl, it, largs, objs = build_loop(op2, spec)
+    op2.par_loop(knl, it, *largs)
+    return _results(objs, spec)
+
+
+def run_batch(op2, specs, replay=False):
+    """Loops of one signature (make_spec(seed, d) for several d): one
+    BatchedParLoop on the GPU package (or, with replay, its graph replayed
+    once), one par_loop each on the oracle."""
+    built = [build_loop(op2, s) for s in specs]
+    if op2.__name__.startswith("pyop2_gb300"):
+        from pyop2_gb300.batch import BatchedParLoop
+        b = BatchedParLoop([op2.ParLoop(k, it, *la) for k, it, la, _ in built], chunk=16)
+        if replay:
+            b.replay()
+        else:
+            b.compute()
+    else:
+        for k, it, la, _ in built:
+            op2.par_loop(k, it, *la)
+    return [_results(objs, s) for (_, _, _, objs), s in zip(built, specs)]
+
+
+def build_loop(op2, spec):
     core, owned, total = spec["sizes"]
     iterset = op2.Set((core, owned, total), "it")
     targets = [op2.Set(n, "t%d" % i) for i, n in enumerate(spec["targets"])]
@@ -205,8 +237,7 @@ def run(op2, spec):
         objs.append(d)
         largs.append(d(acc) if a["map"] is None else d(acc, maps[a["map"]]))
     it = iterset if spec["subset"] is None else op2.Subset(iterset, spec["subset"])
-    op2.par_loop(op2.Kernel(spec["code"], spec["name"]), it, *largs)
-    return _results(objs, spec)
+    return op2.Kernel(spec["code"], spec["name"]), it, largs, objs
 
 
 def _results(objs, spec):

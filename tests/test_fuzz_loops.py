@@ -188,3 +188,17 @@ def test_gpu_autotuned_matches_oracle(gpu_op2, oracle_op2, seed):
         _equal(F.run_extruded(gpu_op2, spec), F.run_extruded(oracle_op2, spec))
     finally:
         configuration["scatter"] = old
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("replay", [False, True], ids=["launch", "graph"])
+@pytest.mark.parametrize("seed", range(0, 48, 3))
+def test_gpu_batch_matches_oracle(gpu_op2, oracle_op2, seed, replay):
+    """Three loops of one random signature over different random meshes in
+    one persistent batched launch (16-entity work items), launched directly
+    or replayed from its CUDA graph, against the oracle running each loop."""
+    specs = [F.make_spec(seed, 100 * seed + d) for d in range(3)]
+    got = F.run_batch(gpu_op2, specs, replay=replay)
+    want = F.run_batch(oracle_op2, specs)
+    for g, w in zip(got, want):
+        _equal(g, w)
