@@ -12,6 +12,8 @@ from pyop2_gb300.types import (  # noqa: F401
     READ, WRITE, RW, INC, MIN, MAX, ON_BOTTOM, ON_TOP, ON_INTERIOR_FACETS, ALL)
 from pyop2_gb300.local_kernel import CStringLocalKernel, Kernel  # noqa: F401
 from pyop2_gb300.datatypes import OpaqueType  # noqa: F401
+from pyop2_gb300 import mpi as MPI  # noqa: F401
+from pyop2_gb300.types.halo import Halo  # noqa: F401
 from pyop2_gb300.parloop import (Parloop, ParLoop, LegacyParloop, parloop, par_loop,  # noqa: F401
                                  GlobalLegacyArg, DatLegacyArg, MatLegacyArg, PassthroughArg,
                                  MixedDatLegacyArg, MixedMatLegacyArg,
@@ -30,7 +32,8 @@ __all__ = ['configuration', 'READ', 'WRITE', 'RW', 'INC', 'MIN', 'MAX',
            'MixedSet', 'Subset', 'DataSet', 'GlobalDataSet', 'MixedDataSet',
            'Dat', 'MixedDat', 'Mat', 'Global', 'Constant', 'Map', 'MixedMap',
            'Sparsity', 'parloop', 'Parloop', 'ParLoop', 'par_loop',
-           'PermutedMap', 'ComposedMap', 'MixedDat', 'DatView', 'PassthroughArg', 'OpaqueType']
+           'PermutedMap', 'ComposedMap', 'MixedDat', 'DatView', 'PassthroughArg', 'OpaqueType',
+           'MPI', 'Halo']
 
 _initialised = False
 set_log_level(configuration['log_level'])

@@ -178,3 +178,37 @@ def test_configuration():
         configuration["scatter"] = "sometimes"
     op2.init(debug=False, scatter="atomic")
     assert op2.initialised()
+
+
+def test_mpi_and_halo_stand_ins():
+    """op2.MPI and op2.Halo, as exported by the reference (pyop2/op2.py:61-68):
+    single-rank communicators whose collectives return their input, and the
+    abstract Halo base class."""
+    import pytest
+    from pyop2_gb300 import op2
+    w = op2.MPI.COMM_WORLD
+    assert (w.rank, w.size, w.Get_rank(), w.Get_size()) == (0, 1, 0, 1)
+    assert w.allreduce(3.5) == 3.5 and w.bcast({"a": 1}) == {"a": 1} and w.allgather(2) == [2]
+    assert op2.MPI.internal_comm(None) is w and op2.MPI.is_pyop2_comm(op2.MPI.COMM_SELF)
+    s = op2.Set(5, "s", comm=w)
+    assert s.comm is w
+    with pytest.raises(TypeError):
+        op2.Halo()
+
+    class MyHalo(op2.Halo):
+        comm = w
+        local_to_global_numbering = None
+
+        def global_to_local_begin(self, dat, insert_mode):
+            pass
+
+        def global_to_local_end(self, dat, insert_mode):
+            pass
+
+        def local_to_global_begin(self, dat, insert_mode):
+            pass
+
+        def local_to_global_end(self, dat, insert_mode):
+            pass
+
+    assert isinstance(MyHalo(), op2.Halo)
