@@ -901,7 +901,7 @@ def run_ours(args):
                          (batch, "batch"), (prisms, "prisms")):
             sec["cpu_1core"] = cs[key]
     cpu = None
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and world == 1 and rank == 0:
         coords = p["coords"]
         cells = p["cellmap"]
         x0 = p["x"].data_ro.copy()
