@@ -43,6 +43,10 @@ class Configuration(dict):
         "device": ("OP2G_DEVICE", int, 0),
         # NVTX ranges + CUDA-event timing of named regions (profiling.summary())
         "profiling": ("OP2G_PROFILING", bool, False),
+        # check a Map's values against its target set when they are uploaded
+        # (an index outside it would fault the GPU; with "debug" the launch
+        # checks every access instead)
+        "check_maps": ("OP2G_CHECK_MAPS", bool, True),
     }
 
     def __init__(self):

@@ -56,7 +56,45 @@ class Map:
         if self._mirror is None:
             self._values.setflags(write=False)
             self._mirror = Mirror(IntType, self._values.shape, self._values)
+            dev = self._mirror.dev()
+            from pyop2_gb300.configuration import configuration
+            if configuration["check_maps"] and not configuration["debug"]:
+                self._check_bounds(dev)
         return self._mirror.dev()
+
+    def _check_bounds(self, dev):
+        """Refuse values that would index outside the target set.  The
+        reference does not check (it would read or write past the array on
+        the CPU); on the GPU such an access faults the context, so the values
+        of the iterated entities are checked once, on the device, when they
+        are uploaded: every non-negative value (negative ones are skipped by
+        the wrappers), plus its layer offset times the largest layer term
+        an extruded loop forms (cell layers - 1 for every iteration region),
+        must be below ``toset.total_size``."""
+        import torch
+        n, a = self._iterset.size, self._arity
+        if n == 0 or a == 0:
+            return
+        v = dev[:self._values.nbytes].view(torch.int32).view(self._iterset.total_size, a)[:n]
+        v = v.to(torch.int64)
+        hi = v
+        it = self._iterset
+        if getattr(it, "_extruded", False) and self._offset is not None:
+            lay = np.asarray(it.layers_array, dtype=np.int64).reshape(-1, 2)
+            terms = lay[:, 1] - lay[:, 0] - 2          # cell layers - 1
+            if len(terms) == 1:
+                terms = np.full(n, terms[0])
+            else:
+                terms = terms[:n]
+            terms = np.maximum(terms, 0)
+            off = np.maximum(np.asarray(self._offset, dtype=np.int64), 0)
+            hi = v + torch.as_tensor(terms[:, None] * off[None, :], device=v.device)
+        hi = torch.where(v >= 0, hi, torch.zeros_like(hi))
+        m = int(hi.max().item())
+        if m >= self._toset.total_size:
+            raise ex.MapValueError("Map %s: entry %d (with its layer offset) is outside the "
+                                   "target set %s of size %d" % (self._name, m, self._toset.name,
+                                                                 self._toset.total_size))
 
     @property
     def _global_kernel_arg(self):

@@ -185,3 +185,29 @@ def test_repeated_par_loop_reuses_the_loop(gpu_op2):
     with y.frozen_halo(op2.READ):
         with pytest.raises(RuntimeError):
             op2.par_loop(k, cells, y(op2.INC, m))
+
+
+def test_out_of_range_map_is_refused_before_any_launch(gpu_op2):
+    """Without debug checks, a map value outside its target set (or pushed
+    outside it by an extruded layer offset) raises MapValueError when the
+    map is first uploaded, before any kernel could fault on it."""
+    from pyop2_gb300.exceptions import MapValueError
+    op2 = gpu_op2
+    s, t = op2.Set(4), op2.Set(3)
+    m = op2.Map(s, t, 1, np.array([0, 1, 3, 2]))          # 3 is out of range
+    d = op2.Dat(t, np.zeros(3))
+    k = op2.Kernel("static void k(double *x) { x[0] += 1; }", "k")
+    with pytest.raises(MapValueError):
+        op2.par_loop(k, s, d(op2.INC, m))
+    assert np.all(d.data_ro == 0.0)
+    # extruded: base values in range, the top layer's offset is not
+    base = op2.Set(2)
+    ext = op2.ExtrudedSet(base, 4)                         # 3 cell layers
+    nodes = op2.Set(6)
+    me = op2.Map(ext, nodes, 1, np.array([[0], [4]]), offset=[1])   # 4 + 2 = 6: outside
+    dn = op2.Dat(nodes, np.zeros(6))
+    with pytest.raises(MapValueError):
+        op2.par_loop(k, ext, dn(op2.INC, me))
+    ok = op2.Map(ext, nodes, 1, np.array([[0], [3]]), offset=[1])   # 3 + 2 = 5: inside
+    op2.par_loop(k, ext, dn(op2.INC, ok))
+    assert np.array_equal(dn.data_ro, np.ones(6))
