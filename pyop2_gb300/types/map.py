@@ -66,16 +66,16 @@ class Map:
         """Refuse values that would index outside the target set.  The
         reference does not check (it would read or write past the array on
         the CPU); on the GPU such an access faults the context, so the values
-        of the iterated entities are checked once, on the device, when they
+        of every entity are checked once, on the device, when they
         are uploaded: every non-negative value (negative ones are skipped by
         the wrappers), plus its layer offset times the largest layer term
         an extruded loop forms (cell layers - 1 for every iteration region),
         must be below ``toset.total_size``."""
         import torch
-        n, a = self._iterset.size, self._arity
+        n, a = self._iterset.total_size, self._arity     # ghost rows too: a Subset may use them
         if n == 0 or a == 0:
             return
-        v = dev[:self._values.nbytes].view(torch.int32).view(self._iterset.total_size, a)[:n]
+        v = dev[:self._values.nbytes].view(torch.int32).view(n, a)
         v = v.to(torch.int64)
         hi = v
         it = self._iterset
