@@ -598,11 +598,15 @@ struct Gen {
         }
         O << "}\n\n";
 
-        // ----- the entry points
+        // ----- the entry points.  Without shared-memory staging (whose
+        // tables are sized for BS threads) the wrapper may be launched with
+        // fewer threads per CTA than BS: a small iteration set is then
+        // spread over more SMs (each SM issues FP64 at 2 per clock).
+        const std::string bdim = any_shared ? std::to_string(BS) : std::string("blockDim.x");
         O << "extern \"C\" __global__ void __launch_bounds__(" << BS
           << ") op2g_wrap(const __grid_constant__ op2g_params_t p) {\n"
-          << "  op2g_run(p, p.start, p.end, (long long)blockIdx.x * " << BS
-          << ", (long long)gridDim.x * " << BS << ");\n}\n";
+          << "  op2g_run(p, p.start, p.end, (long long)blockIdx.x * " << bdim
+          << ", (long long)gridDim.x * " << bdim << ");\n}\n";
         O << "extern \"C\" __global__ void __launch_bounds__(" << BS
           << ") op2g_wrap_batched(const op2g_params_t *__restrict__ P, const long long "
              "*__restrict__ work, long long nwork) {\n"

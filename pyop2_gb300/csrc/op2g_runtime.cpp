@@ -455,8 +455,16 @@ op2g_status op2g_kernel_pack_params(const op2g_kernel *k, const op2g_launch_desc
 op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *stream) {
     if (!k || !d) return fail(OP2G_ERR_INVALID, "NULL argument");
     if (d->end < d->start || d->start < 0) return fail(OP2G_ERR_INVALID, "bad iteration range");
-    std::vector<int64_t> buf(k->param_bytes / 8);
-    op2g_status st = op2g_kernel_pack_params(k, d, buf.data());
+    // parameter record: on the stack for the usual sizes (no heap
+    // allocation per launch), on the heap for very long argument lists
+    int64_t small[512];
+    std::vector<int64_t> big;
+    int64_t *buf = small;
+    if ((size_t)k->param_bytes > sizeof small) {
+        big.resize(k->param_bytes / 8);
+        buf = big.data();
+    }
+    op2g_status st = op2g_kernel_pack_params(k, d, buf);
     if (st != OP2G_OK) return st;
     Loaded *L = nullptr;
     st = load_module(k->cubin, "op2g_wrap", "op2g_wrap_batched", k->sig.block_size, k->per_dev,
@@ -466,7 +474,17 @@ op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *
     const int64_t items = (d->end - d->start) * (k->sig.loop.extruded && k->sig.loop.constant_layers &&
                                                  column_parallel(k->sig) ? per : 1);
     if (items <= 0) return OP2G_OK;
-    const int bs = k->sig.block_size;
+    int bs = k->sig.block_size;
+    // A launch too small to give every SM a full CTA runs smaller CTAs (at
+    // least one warp each) so that it spreads over more SMs; wrappers with
+    // shared-memory staging need their compiled CTA size.
+    if (d->grid == 0 && k->sig.loop.scatter != OP2G_SCATTER_SHARED &&
+        items < (int64_t)L->sms * bs) {
+        int64_t per = (items + L->sms - 1) / L->sms;
+        per = (per + 31) / 32 * 32;
+        if (per < 32) per = 32;
+        if (per < bs) bs = (int)per;
+    }
     int64_t grid = d->grid > 0 ? d->grid : (items + bs - 1) / bs;
     // Default: up to 4 waves of resident CTAs.  Measured on GB300: one wave
     // leaves a tail of lone warps at the end of gather/scatter-bound loops
@@ -475,7 +493,7 @@ op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *
     if (d->grid == 0 && grid > cap) grid = cap;
     if (grid > INT32_MAX) grid = INT32_MAX;
     if (grid < 1) grid = 1;
-    void *params[] = {buf.data()};
+    void *params[] = {buf};
     return launch(L->f, (unsigned)grid, (unsigned)bs, params, stream);
 }
 
