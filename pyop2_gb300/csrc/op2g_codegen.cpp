@@ -607,6 +607,18 @@ struct Gen {
           << ") op2g_wrap(const __grid_constant__ op2g_params_t p) {\n"
           << "  op2g_run(p, p.start, p.end, (long long)blockIdx.x * " << bdim
           << ", (long long)gridDim.x * " << bdim << ");\n}\n";
+        if (!any_shared) {
+            // Balanced form for launches of a few CTAs per SM: CTA b takes the
+            // b-th of gridDim.x equal contiguous chunks of the entities, so a
+            // grid of k CTAs per SM gives every SM the same work.
+            O << "extern \"C\" __global__ void __launch_bounds__(" << BS
+              << ") op2g_wrap_chunked(const __grid_constant__ op2g_params_t p) {\n"
+              << "  const long long n_ = p.end - p.start;\n"
+              << "  const long long c_ = (n_ + gridDim.x - 1) / gridDim.x;\n"
+              << "  const long long s_ = p.start + (long long)blockIdx.x * c_;\n"
+              << "  const long long e_ = s_ + c_ < p.end ? s_ + c_ : p.end;\n"
+              << "  if (s_ < e_) op2g_run(p, s_, e_, 0, (long long)blockDim.x);\n}\n";
+        }
         O << "extern \"C\" __global__ void __launch_bounds__(" << BS
           << ") op2g_wrap_batched(const op2g_params_t *__restrict__ P, const long long "
              "*__restrict__ work, long long nwork) {\n"

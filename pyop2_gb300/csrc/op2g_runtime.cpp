@@ -209,7 +209,7 @@ op2g_status build_cubin(const std::string &src, const std::string &arch, const c
 
 struct Loaded {
     CUmodule mod = nullptr;
-    CUfunction f = nullptr, fb = nullptr;
+    CUfunction f = nullptr, fb = nullptr, fc = nullptr;  // plain, batched, chunked
     int regs = -1;
     int occ = 0;  // resident CTAs per SM
     int sms = 0;
@@ -240,6 +240,8 @@ op2g_status load_module(const std::string &cubin, const char *fname, const char 
         r = D.ModuleGetFunction(&L.fb, L.mod, fname_b);
         if (r != CUDA_SUCCESS) return cu_fail(r, "cuModuleGetFunction (batched)");
     }
+    // the balanced entry exists only in wrappers without shared-memory staging
+    if (D.ModuleGetFunction(&L.fc, L.mod, "op2g_wrap_chunked") != CUDA_SUCCESS) L.fc = nullptr;
     D.FuncGetAttribute(&L.regs, CU_FUNC_ATTRIBUTE_NUM_REGS, L.f);
     if (D.OccupancyMaxActiveBlocksPerMultiprocessor(&L.occ, L.f, bs, 0) != CUDA_SUCCESS) L.occ = 1;
     if (L.occ < 1) L.occ = 1;
@@ -475,15 +477,24 @@ op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *
                                                  column_parallel(k->sig) ? per : 1);
     if (items <= 0) return OP2G_OK;
     int bs = k->sig.block_size;
-    // A launch too small to give every SM a full CTA runs smaller CTAs (at
-    // least one warp each) so that it spreads over more SMs; wrappers with
-    // shared-memory staging need their compiled CTA size.
-    if (d->grid == 0 && k->sig.loop.scatter != OP2G_SCATTER_SHARED &&
-        items < (int64_t)L->sms * bs) {
-        int64_t per = (items + L->sms - 1) / L->sms;
-        per = (per + 31) / 32 * 32;
-        if (per < 32) per = 32;
-        if (per < bs) bs = (int)per;
+    void *params[] = {buf};
+    // A launch of fewer than 4 full CTAs per SM runs the balanced entry: k
+    // CTAs per SM (k = full CTAs per SM, rounded up), each taking an equal
+    // contiguous chunk of the entities with as many threads as the chunk has
+    // iterations (a multiple of 32, at most the compiled CTA size).  Small
+    // loops then spread over every SM instead of a few full CTAs (each SM
+    // issues FP64 at 2 per clock), and medium ones give every SM the same
+    // work.  Wrappers with shared-memory staging keep their CTA size.
+    const int64_t full = (int64_t)L->sms * bs;
+    if (d->grid == 0 && L->fc && items < 4 * full) {
+        const int64_t ents = d->end - d->start;
+        int64_t g = (int64_t)L->sms * ((items + full - 1) / full);
+        if (g > ents) g = ents;
+        const int64_t chunk = (ents + g - 1) / g;
+        int64_t t = chunk * (items / ents);          // iterations per CTA
+        t = (t + 31) / 32 * 32;
+        if (t < bs) bs = (int)t;
+        return launch(L->fc, (unsigned)g, (unsigned)bs, params, stream);
     }
     int64_t grid = d->grid > 0 ? d->grid : (items + bs - 1) / bs;
     // Default: up to 4 waves of resident CTAs.  Measured on GB300: one wave
@@ -493,7 +504,6 @@ op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *
     if (d->grid == 0 && grid > cap) grid = cap;
     if (grid > INT32_MAX) grid = INT32_MAX;
     if (grid < 1) grid = 1;
-    void *params[] = {buf};
     return launch(L->f, (unsigned)grid, (unsigned)bs, params, stream);
 }
 
