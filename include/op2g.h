@@ -203,7 +203,11 @@ typedef struct op2g_launch_desc {
                                   used only to size the grid (0 = 1)                     */
     int32_t grid;              /* CTAs.  0: one per block_size iterations, at most 4 x the
                                   CTAs the GPU holds at once (threads then stride over
-                                  the rest); -1: one per block_size iterations, no cap;
+                                  the rest); a launch of fewer than 4 full CTAs per SM
+                                  instead runs k CTAs per SM on equal contiguous chunks,
+                                  with fewer threads per CTA when a chunk is small
+                                  (wrappers without shared-memory staging);
+                                  -1: one per block_size iterations, no cap;
                                   > 0: exactly this many                               */
 } op2g_launch_desc;
 
