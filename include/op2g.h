@@ -213,6 +213,15 @@ typedef struct op2g_launch_desc {
 
 /* Launch the wrapper over [start, end) on `stream`.  Asynchronous. */
 op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *stream);
+/* The launch shape op2g_kernel_launch uses (pure function, no device use):
+ * `items` iterations over `entities` entities, a wrapper compiled for
+ * `block_size` threads holding `ctas_per_sm` CTAs on each of `sms` SMs,
+ * the descriptor's `grid` request, and whether the wrapper has the balanced
+ * entry (wrappers without shared-memory staging).  Outputs CTAs, threads
+ * per CTA and 1 when the balanced entry runs. */
+void op2g_launch_shape(int64_t items, int64_t entities, int32_t block_size, int32_t sms,
+                       int32_t ctas_per_sm, int32_t grid_request, int32_t chunked_available,
+                       int32_t *grid_out, int32_t *block_out, int32_t *chunked_out);
 
 /* Persistent batched launch of a kernel built with loop->batched = 1: one
  * launch runs nloops loops of the same signature.  `params` is a DEVICE array

@@ -91,6 +91,7 @@ SIGNATURES = {
     "op2g_kernel_num_ptrs": (_i32, [_p]),
     "op2g_kernel_num_regs": (_i32, [_p]),
     "op2g_kernel_launch": (_i32, [_p, ctypes.POINTER(LaunchDesc), _p]),
+    "op2g_launch_shape": (None, [_i64, _i64, _i32, _i32, _i32, _i32, _i32, _pi32, _pi32, _pi32]),
     "op2g_kernel_param_bytes": (_i32, [_p]),
     "op2g_kernel_pack_params": (_i32, [_p, ctypes.POINTER(LaunchDesc), _p]),
     "op2g_kernel_launch_batched": (_i32, [_p, _p, _p, _i64, _i32, _p]),

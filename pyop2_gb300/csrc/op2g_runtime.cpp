@@ -476,35 +476,51 @@ op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *
     const int64_t items = (d->end - d->start) * (k->sig.loop.extruded && k->sig.loop.constant_layers &&
                                                  column_parallel(k->sig) ? per : 1);
     if (items <= 0) return OP2G_OK;
-    int bs = k->sig.block_size;
+    int32_t grid = 0, bs = 0, chunked = 0;
+    op2g_launch_shape(items, d->end - d->start, k->sig.block_size, L->sms, L->occ, d->grid,
+                      L->fc != nullptr, &grid, &bs, &chunked);
     void *params[] = {buf};
+    return launch(chunked ? L->fc : L->f, (unsigned)grid, (unsigned)bs, params, stream);
+}
+
+void op2g_launch_shape(int64_t items, int64_t entities, int32_t block_size, int32_t sms,
+                       int32_t ctas_per_sm, int32_t grid_request, int32_t chunked_available,
+                       int32_t *grid_out, int32_t *block_out, int32_t *chunked_out) {
+    int64_t bs = block_size > 0 ? block_size : 32;
+    const int64_t nsm = sms > 0 ? sms : 1;
+    if (entities < 1) entities = 1;
+    if (items < 1) items = 1;
     // A launch of fewer than 4 full CTAs per SM runs the balanced entry: k
     // CTAs per SM (k = full CTAs per SM, rounded up), each taking an equal
     // contiguous chunk of the entities with as many threads as the chunk has
     // iterations (a multiple of 32, at most the compiled CTA size).  Small
     // loops then spread over every SM instead of a few full CTAs (each SM
     // issues FP64 at 2 per clock), and medium ones give every SM the same
-    // work.  Wrappers with shared-memory staging keep their CTA size.
-    const int64_t full = (int64_t)L->sms * bs;
-    if (d->grid == 0 && L->fc && items < 4 * full) {
-        const int64_t ents = d->end - d->start;
-        int64_t g = (int64_t)L->sms * ((items + full - 1) / full);
-        if (g > ents) g = ents;
-        const int64_t chunk = (ents + g - 1) / g;
-        int64_t t = chunk * (items / ents);          // iterations per CTA
+    // work.  Wrappers with shared-memory staging have no balanced entry.
+    const int64_t full = nsm * bs;
+    if (grid_request == 0 && chunked_available && items < 4 * full) {
+        int64_t g = nsm * ((items + full - 1) / full);
+        if (g > entities) g = entities;
+        const int64_t chunk = (entities + g - 1) / g;
+        int64_t t = chunk * (items / entities);      // iterations per CTA
         t = (t + 31) / 32 * 32;
-        if (t < bs) bs = (int)t;
-        return launch(L->fc, (unsigned)g, (unsigned)bs, params, stream);
+        if (t < bs) bs = t;
+        *grid_out = (int32_t)g;
+        *block_out = (int32_t)bs;
+        *chunked_out = 1;
+        return;
     }
-    int64_t grid = d->grid > 0 ? d->grid : (items + bs - 1) / bs;
+    int64_t grid = grid_request > 0 ? grid_request : (items + bs - 1) / bs;
     // Default: up to 4 waves of resident CTAs.  Measured on GB300: one wave
     // leaves a tail of lone warps at the end of gather/scatter-bound loops
     // (10-14 % slower), while far more CTAs than that slow streaming loops.
-    const int64_t cap = (int64_t)L->occ * L->sms * 4;
-    if (d->grid == 0 && grid > cap) grid = cap;
+    const int64_t cap = (int64_t)(ctas_per_sm > 0 ? ctas_per_sm : 1) * nsm * 4;
+    if (grid_request == 0 && grid > cap) grid = cap;
     if (grid > INT32_MAX) grid = INT32_MAX;
     if (grid < 1) grid = 1;
-    return launch(L->f, (unsigned)grid, (unsigned)bs, params, stream);
+    *grid_out = (int32_t)grid;
+    *block_out = (int32_t)bs;
+    *chunked_out = 0;
 }
 
 op2g_status op2g_kernel_launch_batched(op2g_kernel *k, const void *params_dev,

@@ -97,3 +97,43 @@ def test_graph_entry_points_reject_null(lib):
     assert L.op2g_graph_end(None, None) == lib.ERR_INVALID
     assert L.op2g_graph_launch(None, None) == lib.ERR_INVALID
     L.op2g_graph_destroy(None)
+
+
+def test_launch_shape_policy(lib):
+    """The launch shape op2g_kernel_launch picks (a pure host function):
+    threads cover every iteration, CTAs are whole warps no larger than the
+    compiled size, launches of fewer than 4 full CTAs per SM run the
+    balanced entry with k CTAs per SM (never for wrappers without it, never
+    against an explicit grid), larger ones are capped at 4 resident waves."""
+    import ctypes
+    import numpy as np
+    L = lib.lib()
+    g, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+
+    def shape(items, ents, bs, sms=152, occ=5, req=0, avail=1):
+        L.op2g_launch_shape(items, ents, bs, sms, occ, req, avail, ctypes.byref(g),
+                            ctypes.byref(b), ctypes.byref(c))
+        return g.value, b.value, c.value
+
+    assert shape(8192, 8192, 256) == (152, 64, 1)            # small: every SM, one warp pair
+    assert shape(8192, 8192, 256, avail=0) == (32, 256, 0)   # shared staging: compiled size
+    assert shape(8192, 8192, 256, req=3) == (3, 256, 0)      # explicit grid
+    big = 12_582_912
+    assert shape(big, big, 256) == (5 * 152 * 4, 256, 0)     # 4 resident waves
+    assert shape(big, big, 256, req=-1) == ((big + 255) // 256, 256, 0)
+    rng = np.random.default_rng(0)
+    for _ in range(2000):
+        bs = int(rng.choice([64, 128, 256, 512]))
+        ents = int(rng.integers(1, 400_000))
+        per = int(rng.choice([1, 1, 1, 4, 64]))
+        items = ents * per
+        sms = int(rng.integers(1, 200))
+        gg, bb, cc = shape(items, ents, bs, sms=sms, occ=int(rng.integers(1, 9)))
+        assert bb % 32 == 0 and 32 <= bb <= bs and gg >= 1
+        if cc:
+            assert items < 4 * sms * bs and gg <= ents
+            assert gg % sms == 0 or gg == ents                 # k CTAs on every SM
+            chunk = -(-ents // gg)
+            assert chunk * gg >= ents                          # every entity in a chunk
+        else:
+            assert items >= 4 * sms * bs
