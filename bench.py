@@ -502,7 +502,6 @@ def _time_spmv(op2, A, x, steps, warmup):
 def measure_sparsity_assembly(op2, p, steps, warmup):
     """Configuration 2b on the benchmark mesh: GPU sparsity build (block CSR,
     bit-exact pattern), CSR assembly of the 4x4 element matrices and SpMV."""
-    import torch
     from pyop2_gb300 import workloads as W
     t_sp, sp = _time_sparsity_build((p["verts"] ** 1, p["verts"] ** 1),
                                     [(p["c2v"], p["c2v"], None)])

@@ -43,7 +43,6 @@ def test_map_offsets_past_2_31(gpu_op2, release):
     """537 M cells x arity 4 = 2.148e9 map entries: INC of 1 per entry into
     1000 targets, each reached exactly 2,148,000 times; a READ through the
     same map gathers the targets' ids."""
-    import torch
     op2 = gpu_op2
     ncell, arity, nt = 537_000_000, 4, 1000
     assert ncell * arity > BIG
