@@ -8,8 +8,8 @@ set), and one to six arguments -- direct Dats (READ, WRITE, RW,
 INC), indirect Dats (READ, INC, MIN, MAX; WRITE and RW only through the
 bijection, where the result does not depend on the order of iteration),
 Globals (READ, INC, MIN, MAX) and sometimes a MixedDat through a MixedMap
-(READ or INC, one concatenated pack) -- of dimension 1-3 and dtype float64
-or int32.
+(READ or INC, one concatenated pack) -- of dimension 1-3 and dtype float64,
+float32, int32 or int64.
 The kernel is generated C: it sums its inputs with fixed integer weights and
 writes integer-valued results into every written argument, so every
 implementation must agree bit for bit whatever its order of summation.
@@ -32,6 +32,15 @@ MIN, MAX; direct READ and INC on the base set; Globals).  They are compared
 between implementations only.
 """
 import numpy as np
+
+CTYPES = {"float64": "double", "float32": "float", "int32": "int", "int64": "long long"}
+
+
+def _dtype_of(u):
+    # every value the kernels produce is an integer small enough to be exact
+    # in each of these types
+    return "float64" if u < 0.6 else "int32" if u < 0.75 else "float32" if u < 0.875 else "int64"
+
 
 DIRECT_ACCESS = ["READ", "WRITE", "RW", "INC"]
 INDIRECT_ACCESS = ["READ", "INC", "MIN", "MAX"]
@@ -88,7 +97,7 @@ def make_spec(seed, data_seed=None):
     args = []
     for _ in range(int(rs.integers(1, 7))):
         kind = rs.choice(["direct", "indirect", "global"], p=[0.3, 0.45, 0.25])
-        dtype = "float64" if rs.random() < 0.75 else "int32"
+        dtype = _dtype_of(rs.random())
         dim = int(rs.integers(1, 4))
         if kind == "direct":
             acc = str(rs.choice(DIRECT_ACCESS))
@@ -147,7 +156,7 @@ def kernel_code(spec):
     name = "fz%d" % spec["seed"]
     params, reads, writes = [], [], []
     for k, a in enumerate(spec["args"]):
-        t = "double" if a["dtype"] == "float64" else "int"
+        t = CTYPES[a["dtype"]]
         n = _width(spec, a)
         const = "const " if a["access"] == "READ" else ""
         params.append("%s%s *a%d" % (const, t, k))
@@ -294,7 +303,8 @@ def model(spec):
                 s += sum(float(i + 1 + k) * packs[k][i] for i in range(len(packs[k])))
         for k, a in enumerate(spec["args"]):
             acc, p = a["access"], packs[k]
-            cast = (lambda v: float(v)) if a["dtype"] == "float64" else (lambda v: float(int(v)))
+            cast = (lambda v: float(v)) if a["dtype"].startswith("float") else \
+                (lambda v: float(int(v)))
             for i in range(len(p)):
                 if acc == "INC":
                     p[i] = p[i] + cast(s + i + k)
@@ -372,7 +382,7 @@ def make_extruded_spec(seed):
     args = []
     for _ in range(int(rng.integers(1, 6))):
         k = rng.choice(["direct", "indirect", "global"], p=[0.25, 0.5, 0.25])
-        dtype = "float64" if rng.random() < 0.75 else "int32"
+        dtype = _dtype_of(rng.random())
         dim = int(rng.integers(1, 4))
         mp = None
         if k == "direct":

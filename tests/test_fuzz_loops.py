@@ -1,6 +1,6 @@
 """Randomised differential tests of par_loop: random sets, maps and argument
 lists (every access mode, direct and indirect, Globals, MixedDats through
-MixedMaps, dims 1-3, float64 and int32, core/owned/total splits, Subsets, and extruded column meshes under
+MixedMaps, dims 1-3, float64, float32, int32 and int64, core/owned/total splits, Subsets, and extruded column meshes under
 every iteration region) with a generated kernel whose results are integers.
 The oracle must equal the access-semantics model bit for bit (CPU), and the
 GPU must equal the oracle bit for bit under every INC strategy."""
@@ -46,7 +46,7 @@ def test_specs_cover_every_access_and_shape():
             if a["map"] is not None:
                 seen.add(("map", s["maps"][a["map"]].get("kind", "plain")))
     want = {("direct", x) for x in F.DIRECT_ACCESS} | {("global", x) for x in F.GLOBAL_ACCESS} \
-        | {("indirect", x) for x in F.INDIRECT_ACCESS} | {"float64", "int32"} \
+        | {("indirect", x) for x in F.INDIRECT_ACCESS} | set(F.CTYPES) \
         | {("map", k) for k in ("plain", "perm", "composed")} \
         | {("mixed", "READ"), ("mixed", "INC")}
     assert want <= seen
