@@ -612,6 +612,10 @@ def _layer_range(spec, e, region, for_sparsity):
     return range(start, end), bottom, nl
 
 
+def _rem(a, b):
+    return a if a < b else a - b
+
+
 def _entries(spec, m, e, region, layer, bottom, nl, for_sparsity):
     """Indices of map m on entity e at `layer` (both facets for interior
     facets): the sparsity offsets by the absolute layer modulo the layer
@@ -623,13 +627,15 @@ def _entries(spec, m, e, region, layer, bottom, nl, for_sparsity):
     for i in range(nf * a):
         k, irem = divmod(i, a)
         v = int(m["values"][e, irem])
-        if spec["extruded"]:
+        if spec.get("extruded", True):
             q = int(m["offset_quotient"][irem]) if "offset_quotient" in m else 0
             off = int(m["offset"][irem])
             if for_sparsity:
                 v += off * ((layer + k + q) % nl - q % nl)
             elif spec["periodic"]:
-                v += off * ((layer - bottom + k + q) % nl - q % nl)
+                # the wrappers' remainder is one conditional subtraction
+                # (pyop2/codegen/builder.py:27-30)
+                v += off * (_rem(layer - bottom + k + q, nl) - _rem(q, nl))
             else:
                 v += off * (layer - bottom + k)
         out.append(v)
@@ -698,3 +704,73 @@ def mat_model(spec):
             y[r] += values[k] @ x[colidx[k]]
     return {"rowptr": rowptr, "colidx": colidx, "nnz": counts.astype(np.int64),
             "values": values.reshape(-1), "y": y.reshape(-1)}
+
+
+def model_extruded(spec):
+    """The access semantics of a make_extruded_spec loop in plain Python:
+    columns (or the Subset's columns) in order, the layers the iteration
+    region visits (pyop2/codegen/builder.py:768-788), map entries offset
+    from the column's bottom (both facets for interior facets), direct
+    arguments indexed by the column, the layer argument added as 3 * layer."""
+    data = [a["init"].astype(a["dtype"]).copy() for a in spec["args"]]
+    ents = range(spec["nb"]) if spec.get("subset") is None else spec["subset"]
+    for e in ents:
+        e = int(e)
+        layers, bottom, nl = _layer_range(spec, e, spec["region"], False)
+        for layer in layers:
+            rows = []
+            for a in spec["args"]:
+                if a["kind"] == "global":
+                    rows.append(None)
+                elif a["map"] is None:
+                    rows.append([e])
+                else:
+                    rows.append(_entries(spec, spec["maps"][a["map"]], e, spec["region"],
+                                         layer, bottom, nl, False))
+            packs = []
+            for k, a in enumerate(spec["args"]):
+                if a["kind"] == "global":
+                    p = data[k].astype(np.float64).copy()
+                else:
+                    p = np.concatenate([data[k][r] for r in rows[k]]).astype(np.float64)
+                if a["access"] == "INC" and a["map"] is not None:
+                    p[:] = 0
+                packs.append(p)
+            s = 0.0
+            for k, a in enumerate(spec["args"]):
+                if a["access"] in ("READ", "RW"):
+                    s += sum(float(i + 1 + k) * packs[k][i] for i in range(len(packs[k])))
+            if spec["layer_arg"]:
+                s += 3.0 * layer
+            for k, a in enumerate(spec["args"]):
+                acc, p = a["access"], packs[k]
+                if acc == "READ":
+                    continue
+                cast = (lambda v: float(v)) if a["dtype"].startswith("float") else \
+                    (lambda v: float(int(v)))
+                for i in range(len(p)):
+                    if acc == "INC":
+                        p[i] = p[i] + cast(s + i + k)
+                    elif acc == "MIN":
+                        p[i] = min(p[i], cast(s + i - k))
+                    elif acc == "MAX":
+                        p[i] = max(p[i], cast(s - i + k))
+                if a["kind"] == "global":
+                    if acc == "INC":
+                        data[k] += (p - data[k].astype(np.float64)).astype(data[k].dtype)
+                    else:
+                        data[k][:] = p.astype(data[k].dtype)
+                    continue
+                d = a["dim"]
+                for j, r in enumerate(rows[k]):
+                    chunk = p[j * d:(j + 1) * d].astype(data[k].dtype)
+                    if acc == "INC" and a["map"] is not None:
+                        data[k][r] += chunk
+                    elif acc == "INC":             # direct: the pack is the entity
+                        data[k][r] = chunk
+                    elif acc == "MIN":
+                        data[k][r] = np.minimum(data[k][r], chunk)
+                    else:
+                        data[k][r] = np.maximum(data[k][r], chunk)
+    return [x.reshape(-1) if a["kind"] == "global" else x.reshape(a["init"].shape)
+            for x, a in zip(data, spec["args"])]

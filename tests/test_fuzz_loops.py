@@ -90,6 +90,14 @@ def test_extruded_specs_cover_regions_and_layouts(oracle_op2):
     assert ("subset", True) in seen
 
 
+@pytest.mark.parametrize("seed", CPU_SEEDS)
+def test_oracle_extruded_matches_model(oracle_op2, seed):
+    """The oracle's extruded loops against the plain-Python statement of
+    their layers, offsets and accesses."""
+    spec = F.make_extruded_spec(seed)
+    _equal(F.run_extruded(oracle_op2, spec), F.model_extruded(spec))
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("seed", GPU_SEEDS)
 def test_gpu_matches_oracle_extruded(gpu_op2, oracle_op2, strategy, seed):
