@@ -6,6 +6,26 @@ it, and asserts the values those tests assert (their expected results are
 the golden vectors; the reference test each one follows is cited).  Some
 scenarios return arrays so a test can also compare implementations
 directly.
+
+Reference tests by name (test/unit/...) and the scenario restating each:
+
+    test_indirect_loop.py  test_onecolor_wo -> sc_indirect_wo,
+        test_onecolor_rw -> sc_indirect_rw, test_indirect_inc / _max / _min
+        -> sc_indirect_inc / _max / _min, test_global_read / _inc ->
+        sc_global_read / _inc, test_2d_dat -> sc_2d_dat, test_2d_map ->
+        sc_2d_map, test_mixed_non_mixed_dat(_itspace) ->
+        sc_mixed_non_mixed_dat, test_permuted_map / _both -> sc_permuted_map /
+        sc_permuted_map_both, test_composed_map_two_maps /
+        _three_maps -> sc_composed_two_maps / sc_composed_three_maps
+    test_iteration_space_dats.py  test_sum_nodes_to_edges ->
+        sc_itspace_sum_nodes_to_edges; test_{read,write,inc}_{1d,2d}_itspace_map
+        -> sc_vm_{read,write,inc}_{1d,2d} (the same loops through arity-1 maps)
+    test_vector_map.py  test_{read,write,inc}_{1d,2d}_vector_map ->
+        sc_vm_{read,write,inc}_{1d,2d}
+    test_extrusion.py  test_direct_loop_inc -> sc_extrusion_direct_inc,
+        test_extruded_layer_arg -> sc_extrusion_layer_arg,
+        test_indirect_coords_inc -> sc_extrusion_write_coords, the volume and
+        field tests -> sc_extrusion_volume, sc_extrusion_fields
 """
 import numpy as np
 from numpy.testing import assert_allclose
@@ -337,6 +357,28 @@ def sc_permuted_map(op2):
     vals = np.array([[1, 2, 3, 0]])
     expect = np.empty(4, dtype=np.int32)
     expect[vals[..., perm]] = np.arange(4)[vals]
+    assert np.all(d1.data == np.arange(4)) and np.all(d2.data == expect)
+
+
+def sc_permuted_map_both(op2):
+    """Both arguments through different permutations of one map
+    (test/unit/test_indirect_loop.py:296-313)."""
+    fromset, toset = op2.Set(1), op2.Set(4)
+    d1 = op2.Dat(op2.DataSet(toset, 1), dtype=np.int32)
+    d2 = op2.Dat(op2.DataSet(toset, 1), dtype=np.int32)
+    d1.data[:] = np.arange(4, dtype=np.int32)
+    k = op2.Kernel("""
+    void copy(int *to, const int * restrict from) {
+        for (int i = 0; i < 4; i++) { to[i] = from[i]; }
+    }""", "copy")
+    m1 = op2.Map(fromset, toset, 4, values=[0, 2, 1, 3])
+    p2, p3 = [3, 2, 1, 0], [0, 2, 3, 1]
+    m2 = op2.PermutedMap(m1, p2)
+    m3 = op2.PermutedMap(m1, p3)
+    op2.par_loop(k, fromset, d2(op2.WRITE, m2), d1(op2.READ, m3))
+    vals = np.array([[0, 2, 1, 3]])
+    expect = np.empty(4, dtype=np.int32)
+    expect[vals[..., p2]] = np.arange(4, dtype=np.int32)[vals[..., p3]]
     assert np.all(d1.data == np.arange(4)) and np.all(d2.data == expect)
 
 

@@ -132,6 +132,9 @@ def test_access_modes(s):
 
 
 def test_parloop_validation_before_any_device_work(s):
+    """test_mismatching_iterset, test_mismatching_indset and
+    test_uninitialized_map (test/unit/test_indirect_loop.py:109-129): refused
+    on the host, before anything is uploaded or compiled."""
     indset = op2.Set(5)
     x = op2.Dat(indset, np.arange(5.0))
     with pytest.raises(exceptions.MapValueError):          # map iterset mismatch

@@ -14,7 +14,7 @@ ALL_SIMPLE = [S.sc_indirect_wo, S.sc_indirect_rw, S.sc_indirect_inc, S.sc_indire
 SIZED = [S.sc_gr_direct_typed, S.sc_gr_read_and_inc, S.sc_gr_minmax, S.sc_gr_mixed_types]
 UNSIZED = [S.sc_2d_map, S.sc_itspace_sum_nodes_to_edges, S.sc_vm_read_1d, S.sc_vm_write_1d,
            S.sc_vm_inc_1d, S.sc_vm_read_2d, S.sc_vm_write_2d, S.sc_vm_inc_2d, S.sc_direct,
-           S.sc_permuted_map, S.sc_subset_direct, S.sc_subset_indirect,
+           S.sc_permuted_map, S.sc_permuted_map_both, S.sc_subset_direct, S.sc_subset_indirect,
            S.sc_extrusion_volume, S.sc_extrusion_direct_inc, S.sc_extrusion_layer_arg,
            S.sc_extrusion_fields,
            S.sc_extrusion_write_coords, S.sc_mass_matrix, S.sc_rhs, S.sc_set_matrix,
