@@ -1,9 +1,11 @@
 """Randomised differential tests of par_loop: random sets, maps and argument
 lists (every access mode, direct and indirect, Globals, MixedDats through
-MixedMaps, dims 1-3, float64, float32, int32 and int64, core/owned/total splits, Subsets, and extruded column meshes under
-every iteration region) with a generated kernel whose results are integers.
-The oracle must equal the access-semantics model bit for bit (CPU), and the
-GPU must equal the oracle bit for bit under every INC strategy."""
+MixedMaps, dims 1-3, float64, float32, int32 and int64, core/owned/total
+splits, Subsets, and extruded column meshes under every iteration region)
+with a generated kernel whose results are integers.  The oracle must equal
+the access-semantics models bit for bit (CPU: flat, extruded and matrix
+loops), and the GPU must equal the oracle bit for bit under every INC
+strategy."""
 import numpy as np
 import pytest
 
