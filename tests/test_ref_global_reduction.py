@@ -1,5 +1,17 @@
 """test/unit/test_global_reduction.py on the GPU: READ/INC/MIN/MAX Globals of
-every element type through direct loops, repeated and reused loops."""
+every element type through direct loops, repeated and reused loops.
+
+Reference tests restated here, several per function:
+test_direct_typed -- test_direct_{min,max}_{uint32,int32,float,double};
+test_1d_read -- test_1d_read, test_1d_read_no_init; test_2d_read;
+test_1d_inc -- test_1d_inc, test_1d_inc_no_data;
+test_1d_min_max -- test_1d_{min,max}_dat_is_{min,max},
+test_1d_{min,max}_global_is_{min,max}; test_2d_inc_min_max -- test_2d_inc,
+test_2d_{min,max}_dat_is_{min,max}, test_2d_{min,max}_global_is_{min,max};
+test_multi_inc -- test_1d_multi_inc_same_global(_reset),
+test_1d_multi_inc_diff_global; test_globals_with_different_types;
+test_inc_repeated_and_reused_loop -- test_inc_repeated_loop,
+test_inc_reused_loop."""
 import numpy as np
 import pytest
 from numpy.testing import assert_allclose

@@ -32,6 +32,7 @@ class TestSubSet:
 
     @pytest.mark.parametrize("by_call", [False, True])
     def test_direct_complementary_subsets(self, gpu_op2, iterset, by_call):
+        """by_call=True is test_direct_complementary_subsets_with_indexing."""
         op2 = gpu_op2
         even, odd = np.arange(0, NEL, 2, dtype=np.int32), np.arange(1, NEL, 2, dtype=np.int32)
         mk = iterset if by_call else (lambda idx: op2.Subset(iterset, idx))
@@ -43,6 +44,7 @@ class TestSubSet:
 
     @pytest.mark.parametrize("by_call", [False, True])
     def test_direct_loop_sub_subset(self, gpu_op2, iterset, by_call):
+        """by_call=True is test_direct_loop_sub_subset_with_indexing."""
         op2 = gpu_op2
         k = op2.Kernel(INC, "inc")
         ss = iterset(np.arange(0, NEL, 2, dtype=np.int32)) if by_call else \
