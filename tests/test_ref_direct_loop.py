@@ -1,6 +1,11 @@
 """test/unit/test_direct_loop.py on the GPU: direct loops, Global reductions
 through direct loops, host writes between loops, C++ kernels, passthrough
-handles."""
+handles.
+
+Consolidated tests and the reference tests they restate: test_global_max_min
+-- test_global_{max,min}_dat_is_{max,min}, test_global_{max,min}_g_is_{max,min};
+test_zero_dats -- test_zero_1d_dat, test_zero_2d_dat; test_passthrough_handle
+-- test_passthrough_mat (a device array in place of the PETSc Mat)."""
 import numpy as np
 import pytest
 
