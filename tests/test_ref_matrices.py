@@ -1,6 +1,17 @@
 """test/unit/test_matrices.py on the GPU: sparsity construction rules, Mat
 diagonal and row operations, WRITE assembly, nbytes, and the assembly state
-machine of nested and monolithic mixed matrices."""
+machine of nested and monolithic mixed matrices.
+
+Reference tests restated under other names: test_mat_always_has_diagonal_space
+-> test_sparsity_has_diagonal_space; test_mat_repeated_set_diagonal ->
+test_mat_set_diagonal (set twice); test_zero_matrix and test_solve ->
+test_zero_matrix_and_solve; test_zero_rows_subset and test_zero_last_row ->
+test_zero_rows.  test_assemble_mat, test_assemble_rhs and test_set_matrix
+are scenarios.sc_mass_matrix, sc_rhs and sc_set_matrix (run on the GPU and the
+oracle); test_matrices_sparsity_blockwise_specification is
+sc_sparsity_blockwise.  The FFC-generated variants (test_assemble_ffc,
+test_rhs_ffc, test_rhs_ffc_itspace) assert the same values with other kernel
+texts and are not restated."""
 import numpy as np
 import pytest
 from numpy.testing import assert_allclose
