@@ -332,18 +332,21 @@ op2g_status op2g_colour(int64_t ncells, int32_t nmaps, const int32_t *const *map
 
 /* Colouring without allocation (no counterpart in the reference).
  * For callers that cannot allocate device memory -- a host whose device
- * memory is owned by another allocator or a fixed pool, or code running while
- * a CUDA graph is captured -- this is op2g_colour with its scratch in a fixed
- * device array of the library (OP2G_COLOUR_NOALLOC_SCRATCH_BYTES, held by
- * every GPU that loads the library until the process exits) instead of a
- * caller workspace.  Inputs and outputs are the caller's, as for op2g_colour.
- * It calls no cudaMalloc/cudaFree (nor any allocating library routine), and
- * on success allocates no host memory either.  Problems
- * whose op2g_colour_workspace size exceeds the array fail with
+ * memory is owned by another allocator or a pool sized up front, or a runtime
+ * that forbids cudaMalloc after start-up -- this is op2g_colour with its
+ * scratch in a fixed device array of the library
+ * (OP2G_COLOUR_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the
+ * library until the process exits) instead of a caller workspace.  Inputs
+ * and outputs are the caller's, as for op2g_colour.  It calls no
+ * cudaMalloc/cudaFree (nor any allocating library routine) and allocates no
+ * host memory.  Like op2g_colour it reads a count back and synchronises
+ * `stream` in every colouring round.
+ * Problems whose op2g_colour_workspace size exceeds the array fail with
  * OP2G_ERR_CAPACITY.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress), so make that first call before any stream
- * capture.  All calls share the one array: calls that overlap on the GPU
- * (different streams, or threads) race and must be serialised by the caller. */
+ * address (cudaGetSymbolAddress, once per device, under a lock).  All calls
+ * share the one array and each call clears what it needs: calls that overlap
+ * on the GPU (different streams, or threads) race and must be serialised by
+ * the caller. */
 #define OP2G_COLOUR_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
 #define OP2G_NOALLOC_MAX_DEVICES 64
 op2g_status op2g_colour_noalloc(int64_t ncells, int32_t nmaps, const int32_t *const *maps,

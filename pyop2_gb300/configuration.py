@@ -47,6 +47,10 @@ class Configuration(dict):
         # (an index outside it would fault the GPU; with "debug" the launch
         # checks every access instead)
         "check_maps": ("OP2G_CHECK_MAPS", bool, True),
+        # bytes of Dat / Mat / Global data that op2.par_loop's table of
+        # recently run loops may keep alive; a loop whose own data exceed it is
+        # not kept (deleting its data then frees the device memory)
+        "recent_loops_bytes": ("OP2G_RECENT_LOOPS_BYTES", int, 1 << 30),
     }
 
     def __init__(self):

@@ -1188,42 +1188,36 @@ __global__ void k_transpose_base(const long long *__restrict__ h, long long nch,
 
 constexpr long long COL_CHUNK = 4096;
 
-}  // namespace
-
-extern "C" {
-
-op2g_status op2g_colour_workspace(int64_t ncells, int32_t nmaps, const int64_t *target_size,
-                                  size_t *bytes) {
-    if (nmaps <= 0 || nmaps > 8 || !target_size || ncells < 0)
-        return op2g::fail(OP2G_ERR_INVALID, "colouring takes 1..8 maps");
+// Workspace layout of one colouring (the same for the caller's workspace and
+// for the fixed array of op2g_colour_noalloc).  The histogram holds at least
+// 257 entries: the colour count is read from its first 256 whatever ncells is.
+size_t colour_layout(int64_t ncells, int32_t nmaps, const int64_t *target_size) {
     size_t off = 0;
     for (int k = 0; k < nmaps; ++k) {
         off = align256(off + sizeof(unsigned long long) * (size_t)target_size[k]);       // tmax
         off = align256(off + sizeof(unsigned long long) * CW * (size_t)target_size[k]);  // tmask
     }
     const long long nch = (ncells + COL_CHUNK - 1) / COL_CHUNK;
-    const long long nh = nch * 256 + 1;
-    off = align256(off + sizeof(long long) * nh);                 // histogram
-    off = align256(off + sizeof(long long) * nh);                 // transposed bases
+    const long long nh = (nch > 0 ? nch : 1) * 256 + 1;
+    off = align256(off + sizeof(long long) * nh);                  // histogram
+    off = align256(off + sizeof(long long) * nh);                  // transposed bases
     off = align256(off + sizeof(long long) * scan_tmp_elems(nh));  // scan temp
     off = align256(off + 64);                                      // counters
-    if (bytes) *bytes = off;
-    return OP2G_OK;
+    return off;
 }
 
-op2g_status op2g_colour(int64_t ncells, int32_t nmaps, const int32_t *const *maps,
-                        const int32_t *arity, const int64_t *target_size, int32_t max_colours,
-                        void *ws, size_t ws_bytes, int32_t *colour, int32_t *order,
-                        int64_t *colour_ptr, int32_t *ncolours, void *stream) {
-    size_t need = 0;
-    op2g_status s = op2g_colour_workspace(ncells, nmaps, target_size, &need);
-    if (s != OP2G_OK) return s;
-    if (!ws || ws_bytes < need) return op2g::fail(OP2G_ERR_INVALID, "workspace too small");
+// One colouring with its scratch at `ws` (colour_layout bytes, contents
+// arbitrary: everything that must start at zero is cleared here).  Each
+// Jones-Plassmann round reads its remaining count back to the host and
+// synchronises `stream`; host-side arrays are on the stack.
+op2g_status colour_run(int64_t ncells, int32_t nmaps, const int32_t *const *maps,
+                       const int32_t *arity, const int64_t *target_size, int32_t max_colours,
+                       void *ws, int32_t *colour, int32_t *order, int64_t *colour_ptr,
+                       int32_t *ncolours, cudaStream_t st) {
     if (max_colours <= 0 || max_colours > 64 * CW)
         return op2g::fail(OP2G_ERR_INVALID, "max_colours must be in 1..256");
-    if (!maps || !arity || !colour || !order || !colour_ptr)
+    if (!maps || !arity || !colour_ptr || (ncells > 0 && (!colour || !order)))
         return op2g::fail(OP2G_ERR_INVALID, "NULL argument");
-    cudaStream_t st = (cudaStream_t)stream;
     ColDev C;
     memset(&C, 0, sizeof C);
     C.nmaps = nmaps;
@@ -1241,7 +1235,7 @@ op2g_status op2g_colour(int64_t ncells, int32_t nmaps, const int32_t *const *map
         CK(cudaMemsetAsync(C.tmask[k], 0, sizeof(unsigned long long) * CW * target_size[k], st));
     }
     const long long nch = (ncells + COL_CHUNK - 1) / COL_CHUNK;
-    const long long nh = nch * 256 + 1;
+    const long long nh = (nch > 0 ? nch : 1) * 256 + 1;
     long long *hist = (long long *)(w + off);
     off = align256(off + sizeof(long long) * nh);
     long long *base = (long long *)(w + off);
@@ -1250,7 +1244,7 @@ op2g_status op2g_colour(int64_t ncells, int32_t nmaps, const int32_t *const *map
     off = align256(off + sizeof(long long) * scan_tmp_elems(nh));
     unsigned long long *remaining = (unsigned long long *)(w + off);
     int *err = (int *)(remaining + 1);
-    CK(cudaMemsetAsync(colour, 0xff, sizeof(int) * ncells, st));
+    if (ncells > 0) CK(cudaMemsetAsync(colour, 0xff, sizeof(int) * ncells, st));
     CK(cudaMemsetAsync(err, 0, sizeof(int), st));
     const unsigned grid = grid_for(ncells, 256);
     unsigned long long left = (unsigned long long)ncells;
@@ -1271,50 +1265,76 @@ op2g_status op2g_colour(int64_t ncells, int32_t nmaps, const int32_t *const *map
             return op2g::fail(OP2G_ERR_CAPACITY, "colouring needs more than max_colours colours");
     }
     // Number of colours = 1 + max colour; per-colour counts; stable order.
-    std::vector<long long> hc;
+    long long hc[256];
+    long long cp[64 * CW + 1];
+    CK(cudaMemsetAsync(hist, 0, sizeof(long long) * 257, st));
+    if (ncells > 0) k_col_hist<<<grid, 256, 0, st>>>(colour, ncells, hist);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(hc, hist, sizeof hc, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
     int ncol = 0;
-    {
-        CK(cudaMemsetAsync(hist, 0, sizeof(long long) * 257, st));
-        if (ncells > 0) k_col_hist<<<grid, 256, 0, st>>>(colour, ncells, hist);
-        CK(cudaGetLastError());
-        hc.resize(256);
-        CK(cudaMemcpyAsync(hc.data(), hist, sizeof(long long) * 256, cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        for (int k = 0; k < 256; ++k)
-            if (hc[k]) ncol = k + 1;
-    }
+    for (int k = 0; k < 256; ++k)
+        if (hc[k]) ncol = k + 1;
     if (ncolours) *ncolours = ncol;
-    std::vector<long long> cp(max_colours + 1, 0);
-    for (int k = 0; k < ncol; ++k) cp[k + 1] = cp[k] + hc[k];
-    for (int k = ncol; k < max_colours; ++k) cp[k + 1] = cp[k];
-    CK(cudaMemcpyAsync(colour_ptr, cp.data(), sizeof(long long) * (max_colours + 1),
+    cp[0] = 0;
+    for (int k = 0; k < max_colours; ++k) cp[k + 1] = cp[k] + (k < ncol ? hc[k] : 0);
+    CK(cudaMemcpyAsync(colour_ptr, cp, sizeof(long long) * (max_colours + 1),
                        cudaMemcpyHostToDevice, st));
     if (ncells > 0 && ncol > 0) {
         const long long nhist = nch * ncol;
         CK(cudaMemsetAsync(hist, 0, sizeof(long long) * (nhist + 1), st));
         k_col_chunk_hist<<<(unsigned)nch, 256, 0, st>>>(colour, ncells, COL_CHUNK, ncol, hist);
         CK(cudaGetLastError());
-        s = scan_exclusive(hist, nhist + 1, scan, st);
+        op2g_status s = scan_exclusive(hist, nhist + 1, scan, st);
         if (s != OP2G_OK) return s;
         k_transpose_base<<<(unsigned)((nhist + 255) / 256), 256, 0, st>>>(hist, nch, ncol, base);
         k_col_scatter<<<(unsigned)nch, 32, sizeof(long long) * ncol, st>>>(colour, ncells, COL_CHUNK,
                                                                           base, ncol, order);
         CK(cudaGetLastError());
     }
+    // the stack arrays hc / cp are read by the copies above: wait for them
     CK(cudaStreamSynchronize(st));
     return OP2G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+op2g_status op2g_colour_workspace(int64_t ncells, int32_t nmaps, const int64_t *target_size,
+                                  size_t *bytes) {
+    if (nmaps <= 0 || nmaps > 8 || !target_size || ncells < 0)
+        return op2g::fail(OP2G_ERR_INVALID, "colouring takes 1..8 maps");
+    for (int k = 0; k < nmaps; ++k)
+        if (target_size[k] < 0) return op2g::fail(OP2G_ERR_INVALID, "negative target size");
+    const size_t off = colour_layout(ncells, nmaps, target_size);
+    if (bytes) *bytes = off;
+    return OP2G_OK;
+}
+
+op2g_status op2g_colour(int64_t ncells, int32_t nmaps, const int32_t *const *maps,
+                        const int32_t *arity, const int64_t *target_size, int32_t max_colours,
+                        void *ws, size_t ws_bytes, int32_t *colour, int32_t *order,
+                        int64_t *colour_ptr, int32_t *ncolours, void *stream) {
+    size_t need = 0;
+    op2g_status s = op2g_colour_workspace(ncells, nmaps, target_size, &need);
+    if (s != OP2G_OK) return s;
+    if (!ws || ws_bytes < need) return op2g::fail(OP2G_ERR_INVALID, "workspace too small");
+    return colour_run(ncells, nmaps, maps, arity, target_size, max_colours, ws, colour, order,
+                      colour_ptr, ncolours, (cudaStream_t)stream);
 }
 
 }  // extern "C"
 
 // ------------------------------------------------- colouring without allocation
 // For callers that cannot allocate device memory: a host embedding the
-// library in a process whose allocator belongs to someone else (a
-// framework's caching allocator, a memory pool sized up front), code running
-// while a CUDA graph is being captured, or a runtime that forbids
-// cudaMalloc after start-up.  op2g_colour_noalloc is op2g_colour with its
-// scratch taken from a fixed device array of this file instead of a
-// caller-provided workspace; the caller still passes every input and output.
+// library in a process whose device memory belongs to another allocator (a
+// framework's caching allocator, a memory pool sized up front), or a runtime
+// that forbids cudaMalloc after start-up.  op2g_colour_noalloc runs the same
+// colouring (colour_run) with its scratch in a fixed device array of this
+// file instead of a caller-provided workspace; the caller still passes every
+// input and output.  Like op2g_colour it synchronises the stream every
+// Jones-Plassmann round.
 namespace {
 
 // Every GPU that loads the library holds this array until the process exits.
@@ -1359,92 +1379,11 @@ extern "C" op2g_status op2g_colour_noalloc(int64_t ncells, int32_t nmaps,
                               " bytes of scratch, above the fixed " +
                               std::to_string((long long)OP2G_COLOUR_NOALLOC_SCRATCH_BYTES) +
                               " (use op2g_colour with a workspace)");
-    if (max_colours <= 0 || max_colours > 64 * CW)
-        return op2g::fail(OP2G_ERR_INVALID, "max_colours must be in 1..256");
-    if (!maps || !arity || !colour || !order || !colour_ptr)
-        return op2g::fail(OP2G_ERR_INVALID, "NULL argument");
     void *ws = nullptr;
     s = colour_scratch(&ws);
     if (s != OP2G_OK) return s;
-    cudaStream_t st = (cudaStream_t)stream;
-    // Same layout and steps as op2g_colour; everything that must start at
-    // zero is cleared here because the array keeps the previous call's data.
-    ColDev C;
-    memset(&C, 0, sizeof C);
-    C.nmaps = nmaps;
-    char *w = (char *)ws;
-    size_t off = 0;
-    for (int k = 0; k < nmaps; ++k) {
-        if (!maps[k] || arity[k] <= 0) return op2g::fail(OP2G_ERR_INVALID, "bad colouring map");
-        C.maps[k] = maps[k];
-        C.arity[k] = arity[k];
-        C.tsz[k] = target_size[k];
-        C.tmax[k] = (unsigned long long *)(w + off);
-        off = align256(off + sizeof(unsigned long long) * (size_t)target_size[k]);
-        C.tmask[k] = (unsigned long long *)(w + off);
-        off = align256(off + sizeof(unsigned long long) * CW * (size_t)target_size[k]);
-        CK(cudaMemsetAsync(C.tmask[k], 0, sizeof(unsigned long long) * CW * target_size[k], st));
-    }
-    const long long nch = (ncells + COL_CHUNK - 1) / COL_CHUNK;
-    const long long nh = nch * 256 + 1;
-    long long *hist = (long long *)(w + off);
-    off = align256(off + sizeof(long long) * nh);
-    long long *base = (long long *)(w + off);
-    off = align256(off + sizeof(long long) * nh);
-    long long *scan = (long long *)(w + off);
-    off = align256(off + sizeof(long long) * scan_tmp_elems(nh));
-    unsigned long long *remaining = (unsigned long long *)(w + off);
-    int *err = (int *)(remaining + 1);
-    CK(cudaMemsetAsync(colour, 0xff, sizeof(int) * ncells, st));
-    CK(cudaMemsetAsync(err, 0, sizeof(int), st));
-    const unsigned grid = grid_for(ncells, 256);
-    unsigned long long left = (unsigned long long)ncells;
-    int rounds = 0;
-    while (left > 0) {
-        if (++rounds > 100000) return op2g::fail(OP2G_ERR_TIMEOUT, "colouring did not converge");
-        for (int k = 0; k < nmaps; ++k)
-            CK(cudaMemsetAsync(C.tmax[k], 0, sizeof(unsigned long long) * target_size[k], st));
-        CK(cudaMemsetAsync(remaining, 0, sizeof(unsigned long long), st));
-        k_jp_prio<<<grid, 256, 0, st>>>(C, ncells, colour);
-        k_jp_select<<<grid, 256, 0, st>>>(C, ncells, colour, max_colours, remaining, err);
-        CK(cudaGetLastError());
-        int herr = 0;
-        CK(cudaMemcpyAsync(&left, remaining, sizeof left, cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        if (herr & OP2G_DEVERR_CAPACITY)
-            return op2g::fail(OP2G_ERR_CAPACITY, "colouring needs more than max_colours colours");
-    }
-    long long hc[256];
-    long long cp[257];
-    CK(cudaMemsetAsync(hist, 0, sizeof(long long) * 257, st));
-    if (ncells > 0) k_col_hist<<<grid, 256, 0, st>>>(colour, ncells, hist);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(hc, hist, sizeof hc, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    int ncol = 0;
-    for (int k = 0; k < 256; ++k)
-        if (hc[k]) ncol = k + 1;
-    if (ncolours) *ncolours = ncol;
-    cp[0] = 0;
-    for (int k = 0; k < max_colours; ++k) cp[k + 1] = cp[k] + (k < ncol ? hc[k] : 0);
-    CK(cudaMemcpyAsync(colour_ptr, cp, sizeof(long long) * (max_colours + 1),
-                       cudaMemcpyHostToDevice, st));
-    if (ncells > 0 && ncol > 0) {
-        const long long nhist = nch * ncol;
-        CK(cudaMemsetAsync(hist, 0, sizeof(long long) * (nhist + 1), st));
-        k_col_chunk_hist<<<(unsigned)nch, 256, 0, st>>>(colour, ncells, COL_CHUNK, ncol, hist);
-        CK(cudaGetLastError());
-        s = scan_exclusive(hist, nhist + 1, scan, st);
-        if (s != OP2G_OK) return s;
-        k_transpose_base<<<(unsigned)((nhist + 255) / 256), 256, 0, st>>>(hist, nch, ncol, base);
-        k_col_scatter<<<(unsigned)nch, 32, sizeof(long long) * ncol, st>>>(colour, ncells, COL_CHUNK,
-                                                                          base, ncol, order);
-        CK(cudaGetLastError());
-    }
-    // the host arrays hc/cp are read by the copies above: wait for them
-    CK(cudaStreamSynchronize(st));
-    return OP2G_OK;
+    return colour_run(ncells, nmaps, maps, arity, target_size, max_colours, ws, colour, order,
+                      colour_ptr, ncolours, (cudaStream_t)stream);
 }
 
 // ---------------------------------------------------------------- probe

@@ -845,7 +845,8 @@ class ColourPlan:
 
 
 def colour_plan(loop, max_colours=256):
-    """Colouring of ``loop.iterset`` (cached on the set per map tuple)."""
+    """Colouring of ``loop.iterset`` (cached on the set per tuple of written
+    maps)."""
     it = loop.iterset
     if isinstance(it, Subset):
         raise NotImplementedError("coloured execution of subsets")
@@ -861,10 +862,12 @@ def colour_plan(loop, max_colours=256):
     seen = set()
     for m in maps:
         b = m.map_ if isinstance(m, PermutedMap) else m
-        if id(b) not in seen:
-            seen.add(id(b))
+        if b._serial not in seen:
+            seen.add(b._serial)
             base.append(b)
-    key = ("colour", tuple(id(b) for b in base))
+    # keyed by the maps' serial numbers (never reused, unlike id()); the
+    # values of a map are fixed once on the device, so the plan stays valid
+    key = ("colour", tuple(b._serial for b in base))
     if key in it._cache:
         return it._cache[key]
     n = it.size
@@ -927,12 +930,41 @@ def ParLoop(*args, **kwargs):
 # validation and signature building and reuses the launch descriptor (the
 # host cost of a call drops from ~45 to ~12 us, which is what a loop over a
 # few thousand cells costs on the device).  The entries hold their objects,
-# so the ids in a key cannot be reused while it lives; the cost is that the
-# data of the last 16 distinct loops stays alive.  Loops made internally for
-# temporaries (Dat arithmetic) go through run_once and are not kept.
-_RECENT = collections.OrderedDict()
+# so the ids in a key cannot be reused while it lives; the cost is that their
+# data stay alive.  That is bounded: at most 16 entries, whose Dat / Mat /
+# Global data together take at most configuration["recent_loops_bytes"]
+# (least recently used entries go first; a loop whose own data exceed the
+# bound is not kept).  Loops made internally for temporaries (Dat
+# arithmetic) go through run_once and are not kept.
+_RECENT = collections.OrderedDict()     # key -> (loop, kernel, iterset, bytes)
 _RECENT_SIZE = 16
+_RECENT_BYTES = [0]
 _CONFIG_KEYS = ("scatter", "block_size", "prefetch", "grid", "debug", "autotune", "type_check")
+
+
+def _data_bytes(args):
+    """Bytes of the distinct Dat / Mat / Global objects a loop references."""
+    seen, total = set(), 0
+    for a in args:
+        objs = a.data if isinstance(a, (MixedDatLegacyArg,)) else (
+            getattr(a, "data", None),)
+        for o in objs:
+            if o is None or isinstance(o, int) or id(o) in seen:
+                continue
+            seen.add(id(o))
+            total += int(getattr(o, "nbytes", 0) or 0)
+    return total
+
+
+def _recent_drop_oldest():
+    _, hit = _RECENT.popitem(last=False)
+    _RECENT_BYTES[0] -= hit[3]
+
+
+def recent_loops_clear():
+    """Forget every remembered loop (their data are no longer kept alive)."""
+    _RECENT.clear()
+    _RECENT_BYTES[0] = 0
 
 
 def _arg_key(a):
@@ -979,9 +1011,17 @@ def parloop(knl, *args, **kwargs):
     if pl is None:
         pl = LegacyParloop(knl, *args, **kwargs)
         if key is not None:
-            _RECENT[key] = (pl, knl, args[0])
-            if len(_RECENT) > _RECENT_SIZE:
-                _RECENT.popitem(last=False)
+            nb = _data_bytes(args[1:])
+            limit = int(configuration["recent_loops_bytes"])
+            if nb <= limit:
+                old = _RECENT.pop(key, None)
+                if old is not None:
+                    _RECENT_BYTES[0] -= old[3]
+                while _RECENT and (len(_RECENT) >= _RECENT_SIZE or
+                                   _RECENT_BYTES[0] + nb > limit):
+                    _recent_drop_oldest()
+                _RECENT[key] = (pl, knl, args[0], nb)
+                _RECENT_BYTES[0] += nb
     pl()
 
 

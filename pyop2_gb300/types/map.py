@@ -24,6 +24,9 @@ class Map:
     """
 
     dtype = IntType
+    # Serial numbers: unlike id(), never reused within a process, so caches
+    # keyed by them (colouring plans) cannot hand one map's result to another.
+    _serials = itertools.count()
 
     @utils.validate_type(('iterset', Set, ex.SetTypeError), ('toset', Set, ex.SetTypeError),
                          ('arity', numbers.Integral, ex.ArityTypeError),
@@ -48,6 +51,14 @@ class Map:
             self._offset_quotient = utils.verify_reshape(offset_quotient, IntType, (arity,))
         self._cache = {}
         self._mirror = None
+
+    @property
+    def _serial(self):
+        """This map's serial number, drawn at first use (every Map kind)."""
+        s = self.__dict__.get("_serial_no")
+        if s is None:
+            s = self.__dict__["_serial_no"] = next(Map._serials)
+        return s
 
     # ---- device
     def _device_values(self):

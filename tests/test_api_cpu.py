@@ -215,3 +215,21 @@ def test_mpi_and_halo_stand_ins():
             pass
 
     assert isinstance(MyHalo(), op2.Halo)
+
+
+def test_map_serials_are_never_reused():
+    """Colouring plans are cached per map serial: a map created after another
+    was freed (which may reuse its id()) still gets a new serial."""
+    import gc
+    from pyop2_gb300 import op2
+    s, t = op2.Set(4), op2.Set(3)
+    seen = set()
+    for _ in range(50):
+        m = op2.Map(s, t, 1, [0, 1, 2, 0])
+        assert m._serial not in seen
+        seen.add(m._serial)
+        assert m._serial == m._serial
+        del m
+        gc.collect()
+    pm = op2.PermutedMap(op2.Map(s, t, 1, [0, 1, 2, 0]), [0])
+    assert pm._serial not in seen

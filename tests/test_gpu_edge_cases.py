@@ -165,7 +165,7 @@ def test_repeated_par_loop_reuses_the_loop(gpu_op2):
     m = op2.Map(cells, verts, 3, vals)
     y = op2.Dat(verts, np.zeros(20))
     k = op2.Kernel("static void k(double *y) { for (int i = 0; i < 3; ++i) y[i] += 1.0; }", "k")
-    P._RECENT.clear()
+    P.recent_loops_clear()
     for _ in range(3):
         op2.par_loop(k, cells, y(op2.INC, m))
     assert len(P._RECENT) == 1
@@ -185,6 +185,52 @@ def test_repeated_par_loop_reuses_the_loop(gpu_op2):
     with y.frozen_halo(op2.READ):
         with pytest.raises(RuntimeError):
             op2.par_loop(k, cells, y(op2.INC, m))
+
+
+def test_recent_loop_table_is_bounded_by_bytes(gpu_op2):
+    """The table of recently run loops keeps at most
+    configuration["recent_loops_bytes"] of data alive: a loop over larger data
+    is not kept, so deleting its Dats frees their device memory; small loops
+    are still reused."""
+    import gc
+    import weakref
+    import torch
+    from pyop2_gb300 import parloop as P
+    from pyop2_gb300.configuration import configuration
+    op2 = gpu_op2
+    P.recent_loops_clear()
+    old = configuration["recent_loops_bytes"]
+    configuration["recent_loops_bytes"] = 4 << 20
+    try:
+        k = op2.Kernel("static void k(double *y) { y[0] += 1.0; }", "k")
+        small = op2.Set(100)
+        ys = op2.Dat(small, np.zeros(100))
+        for _ in range(3):
+            op2.par_loop(k, small, ys(op2.INC))
+        assert len(P._RECENT) == 1
+        big = op2.Set(2 << 20)                 # 16 MB of float64
+        yb = op2.Dat(big, np.zeros(2 << 20))
+        op2.par_loop(k, big, yb(op2.INC))
+        assert float(yb.data_ro[-1]) == 1.0
+        assert len(P._RECENT) == 1            # the big loop was not kept
+        ref = weakref.ref(yb)
+        torch.cuda.synchronize()
+        before = torch.cuda.memory_allocated()
+        del yb
+        gc.collect()
+        assert ref() is None
+        assert torch.cuda.memory_allocated() <= before - (16 << 20)
+        # loops under the bound evict the least recently used ones
+        dats = [op2.Dat(op2.Set(1 << 17)) for _ in range(5)]     # 1 MB each
+        for d in dats:
+            op2.par_loop(k, d.dataset.set, d(op2.INC))
+        assert P._RECENT_BYTES[0] <= 4 << 20
+        assert len(P._RECENT) <= 4
+        op2.par_loop(k, small, ys(op2.INC))
+        assert np.all(ys.data_ro == 4.0)
+    finally:
+        configuration["recent_loops_bytes"] = old
+        P.recent_loops_clear()
 
 
 def test_out_of_range_map_is_refused_before_any_launch(gpu_op2):
