@@ -1,80 +1,144 @@
 """The reference's non-legacy loop interface (pyop2/global_kernel.py:19-340):
-kernel-argument descriptors and GlobalKernel, the signature a Parloop is
-built from.  Here a GlobalKernel is only a description: the generated CUDA
-wrapper is compiled (and cached) from the concrete arguments when the
-Parloop first runs."""
+kernel-argument descriptors and GlobalKernel, the description a Parloop is
+built from.
+
+Here a GlobalKernel compiles nothing: the CUDA wrapper is generated, compiled
+and cached from the loop's concrete arguments when the Parloop first runs.
+What a GlobalKernel needs is a key that identifies the wrapper it describes,
+and that key is built from the same tables libop2g is given
+(``op2g_map_desc`` / ``op2g_arg_desc``, include/op2g.h): the map descriptors
+are flattened into a table of plain, permuted and composed entries, numbered
+in order of first appearance (by descriptor identity, so two arguments
+through one map share an entry), and each argument becomes a row naming its
+kind, shape and the table entries it reads through.
+
+The class names, constructor fields, properties and error messages are the
+reference's public interface and stay as user code expects them.
+"""
 import collections.abc
-import itertools
-from dataclasses import dataclass
-from typing import Optional, Tuple
+from typing import Any, Optional, Tuple
 
 from pyop2_gb300.types.access import Access
 from pyop2_gb300.types.glob import Constant
 
 
-@dataclass(eq=False, frozen=True)
-class MapKernelArg:
-    """A map argument: arity and extruded offsets (pyop2/global_kernel.py:19-37)."""
-    arity: int
-    offset: Optional[Tuple[int, ...]] = None
-    offset_quotient: Optional[Tuple[int, ...]] = None
+class _Frozen:
+    """Immutable record: fields are set once by the constructor."""
 
-    def __post_init__(self):
-        if not isinstance(self.offset, collections.abc.Hashable):
-            raise ValueError("The provided offset must be hashable")
-        if not isinstance(self.offset_quotient, collections.abc.Hashable):
-            raise ValueError("The provided offset_quotient must be hashable")
+    __slots__ = ()
+
+    def __setattr__(self, name, value):
+        raise AttributeError("%s is immutable" % type(self).__name__)
+
+    def _set(self, **fields):
+        for k, v in fields.items():
+            object.__setattr__(self, k, v)
+
+    def __repr__(self):
+        body = ", ".join("%s=%r" % (k, getattr(self, k)) for k in self.__slots__)
+        return "%s(%s)" % (type(self).__name__, body)
+
+
+def _hashable(value, what):
+    if not isinstance(value, collections.abc.Hashable):
+        raise ValueError("The provided %s must be hashable" % what)
+    return value
+
+
+# ------------------------------------------------------------ map descriptors
+# Map descriptors compare by identity: which arguments share a map is part of
+# the loop's signature.
+class MapKernelArg(_Frozen):
+    """Arity and extruded offsets of a plain map (pyop2/global_kernel.py:19-37)."""
+
+    __slots__ = ("arity", "offset", "offset_quotient")
+
+    def __init__(self, arity: int, offset: Optional[Tuple[int, ...]] = None,
+                 offset_quotient: Optional[Tuple[int, ...]] = None):
+        self._set(arity=arity, offset=_hashable(offset, "offset"),
+                  offset_quotient=_hashable(offset_quotient, "offset_quotient"))
 
     @property
     def cache_key(self):
-        return type(self), self.arity, self.offset, self.offset_quotient
+        return ("plain", self.arity, self.offset, self.offset_quotient)
 
 
-@dataclass(eq=False, frozen=True)
-class PermutedMapKernelArg:
-    base_map: MapKernelArg
-    permutation: Tuple[int, ...]
+class PermutedMapKernelArg(_Frozen):
+    """A plain map read through a permutation of its columns
+    (pyop2/global_kernel.py:40-53)."""
 
-    def __post_init__(self):
-        if not isinstance(self.permutation, collections.abc.Hashable):
-            raise ValueError("The provided permutation must be hashable")
+    __slots__ = ("base_map", "permutation")
+
+    def __init__(self, base_map: MapKernelArg, permutation: Tuple[int, ...]):
+        self._set(base_map=base_map, permutation=_hashable(permutation, "permutation"))
 
     @property
     def cache_key(self):
-        return type(self), self.base_map.cache_key, tuple(self.permutation)
+        return ("permuted", self.base_map.cache_key, tuple(self.permutation))
 
 
-class ComposedMapKernelArg:
+class ComposedMapKernelArg(_Frozen):
+    """A chain of maps, outermost first (pyop2/global_kernel.py:56-74)."""
+
+    __slots__ = ("base_maps",)
+
     def __init__(self, *base_maps):
-        for m in base_maps:
-            if not isinstance(m, (MapKernelArg, PermutedMapKernelArg, ComposedMapKernelArg)):
-                raise TypeError("base_maps must be a combination of MapKernelArgs, "
-                                "PermutedMapKernelArgs, and ComposedMapKernelArgs")
-        self.base_maps = base_maps
+        if not all(isinstance(m, _MAP_DESCS) for m in base_maps):
+            raise TypeError("base_maps must be a combination of MapKernelArgs, "
+                            "PermutedMapKernelArgs, and ComposedMapKernelArgs")
+        self._set(base_maps=tuple(base_maps))
 
     @property
     def cache_key(self):
-        return type(self), tuple(m.cache_key for m in self.base_maps)
+        return ("composed",) + tuple(m.cache_key for m in self.base_maps)
 
 
-@dataclass(frozen=True)
-class GlobalKernelArg:
-    dim: Tuple[int, ...]
+_MAP_DESCS = (MapKernelArg, PermutedMapKernelArg, ComposedMapKernelArg)
 
-    @property
-    def cache_key(self):
-        return type(self), self.dim
+
+# ------------------------------------------------------- argument descriptors
+# These compare by value (two Dat arguments of one shape through one map
+# descriptor are the same argument).
+class _ValueDesc(_Frozen):
+    __slots__ = ()
+
+    def _fields(self):
+        return tuple(getattr(self, k) for k in self.__slots__)
+
+    def __eq__(self, other):
+        return type(other) is type(self) and other._fields() == self._fields()
+
+    def __hash__(self):
+        return hash((type(self).__name__,) + self._fields())
 
     @property
     def maps(self):
         return ()
 
 
-@dataclass(frozen=True)
-class DatKernelArg:
-    dim: Tuple[int, ...]
-    map_: object = None
-    index: Optional[Tuple[int, ...]] = None
+class GlobalKernelArg(_ValueDesc):
+    """An op2.Global argument of shape ``dim`` (pyop2/global_kernel.py:77-88)."""
+
+    __slots__ = ("dim",)
+
+    def __init__(self, dim: Tuple[int, ...]):
+        self._set(dim=dim)
+
+    @property
+    def cache_key(self):
+        return ("global", self.dim)
+
+
+class DatKernelArg(_ValueDesc):
+    """An op2.Dat argument: per-entity shape ``dim``, the map it is read
+    through (None: direct), and for a DatView the component ``index``
+    (pyop2/global_kernel.py:91-125)."""
+
+    __slots__ = ("dim", "map_", "index")
+
+    def __init__(self, dim: Tuple[int, ...], map_: Any = None,
+                 index: Optional[Tuple[int, ...]] = None):
+        self._set(dim=dim, map_=map_, index=index)
 
     @property
     def is_direct(self):
@@ -82,32 +146,33 @@ class DatKernelArg:
 
     @property
     def is_indirect(self):
-        return not self.is_direct
+        return self.map_ is not None
 
     @property
     def cache_key(self):
-        return type(self), self.dim, self.map_.cache_key if self.map_ is not None else None, \
-            self.index
+        return ("dat", self.dim, None if self.map_ is None else self.map_.cache_key, self.index)
 
     @property
     def maps(self):
-        return (self.map_,) if self.map_ is not None else ()
+        return () if self.map_ is None else (self.map_,)
 
 
-@dataclass(frozen=True)
-class MatKernelArg:
-    dims: Tuple[Tuple[int, ...], Tuple[int, ...]]
-    maps: Tuple[MapKernelArg, MapKernelArg]
-    unroll: bool = False
+class MatKernelArg(_ValueDesc):
+    """An op2.Mat argument: block shapes and (row, column) map descriptors
+    (pyop2/global_kernel.py:128-152)."""
+
+    __slots__ = ("dims", "maps", "unroll")
+
+    def __init__(self, dims, maps, unroll: bool = False):
+        self._set(dims=dims, maps=tuple(maps), unroll=unroll)
 
     @property
     def cache_key(self):
-        return type(self), self.dims, tuple(m.cache_key for m in self.maps), self.unroll
+        return ("mat", self.dims, tuple(m.cache_key for m in self.maps), self.unroll)
 
 
-@dataclass(frozen=True)
-class MixedDatKernelArg:
-    arguments: Tuple[DatKernelArg, ...]
+class _MixedDesc(_ValueDesc):
+    __slots__ = ()
 
     def __iter__(self):
         return iter(self.arguments)
@@ -116,49 +181,103 @@ class MixedDatKernelArg:
         return len(self.arguments)
 
     @property
-    def cache_key(self):
-        return tuple(a.cache_key for a in self.arguments)
-
-    @property
     def maps(self):
         return tuple(m for a in self.arguments for m in a.maps)
 
 
-@dataclass(frozen=True)
-class MixedMatKernelArg:
-    arguments: Tuple[MatKernelArg, ...]
-    shape: Tuple[int, ...]
+class MixedDatKernelArg(_MixedDesc):
+    """The components of a MixedDat, one kernel parameter
+    (pyop2/global_kernel.py:155-175)."""
 
-    def __iter__(self):
-        return iter(self.arguments)
+    __slots__ = ("arguments",)
 
-    def __len__(self):
-        return len(self.arguments)
+    def __init__(self, arguments: Tuple[DatKernelArg, ...]):
+        self._set(arguments=tuple(arguments))
 
     @property
     def cache_key(self):
-        return tuple(a.cache_key for a in self.arguments)
-
-    @property
-    def maps(self):
-        return tuple(m for a in self.arguments for m in a.maps)
+        return ("mixed dat",) + tuple(a.cache_key for a in self.arguments)
 
 
-class PassthroughKernelArg:
+class MixedMatKernelArg(_MixedDesc):
+    """The blocks of a mixed Mat in row-major block order, block grid
+    ``shape`` (pyop2/global_kernel.py:178-206)."""
+
+    __slots__ = ("arguments", "shape")
+
+    def __init__(self, arguments: Tuple[MatKernelArg, ...], shape: Tuple[int, ...]):
+        self._set(arguments=tuple(arguments), shape=shape)
+
     @property
     def cache_key(self):
-        return type(self)
+        return ("mixed mat", self.shape) + tuple(a.cache_key for a in self.arguments)
+
+
+class PassthroughKernelArg(_ValueDesc):
+    """A raw pointer handed to the kernel (pyop2/global_kernel.py:209-219)."""
+
+    __slots__ = ()
 
     @property
-    def maps(self):
-        return ()
+    def cache_key(self):
+        return ("passthrough",)
+
+
+# ---------------------------------------------------------- signature tables
+class _DescTable:
+    """Map descriptors in the form of libop2g's map table: one entry per
+    distinct descriptor object, in order of first appearance; permuted
+    entries point at their base map's entry, composed ones list the entries
+    of their chain (innermost maps first registered, as the wrapper reads
+    them)."""
+
+    def __init__(self):
+        self.entries = []
+        self._index = {}
+
+    def add(self, m):
+        hit = self._index.get(id(m))
+        if hit is not None:
+            return hit
+        if isinstance(m, ComposedMapKernelArg):
+            entry = ("composed", tuple(self.add(c) for c in m.base_maps))
+        elif isinstance(m, PermutedMapKernelArg):
+            entry = ("permuted", self.add(m.base_map), tuple(m.permutation))
+        elif isinstance(m, MapKernelArg):
+            entry = ("plain", m.arity, m.offset, m.offset_quotient)
+        else:
+            raise TypeError("not a map descriptor: %r" % (m,))
+        # the descriptors are alive while the table is built, so their ids
+        # are unique for its lifetime
+        self._index[id(m)] = len(self.entries)
+        self.entries.append(entry)
+        return self._index[id(m)]
+
+
+def _arg_rows(arguments, table):
+    """One row per kernel parameter: its kind and shape, with maps replaced
+    by their table entries."""
+    rows = []
+    for a in arguments:
+        if isinstance(a, DatKernelArg):
+            rows.append(("dat", a.dim, -1 if a.map_ is None else table.add(a.map_), a.index))
+        elif isinstance(a, MatKernelArg):
+            rows.append(("mat", a.dims, tuple(table.add(m) for m in a.maps), a.unroll))
+        elif isinstance(a, _MixedDesc):
+            rows.append((type(a).__name__, getattr(a, "shape", None),
+                         tuple(_arg_rows(a.arguments, table))))
+        elif isinstance(a, (GlobalKernelArg, PassthroughKernelArg)):
+            rows.append(a.cache_key)
+        else:
+            raise TypeError("not a kernel argument descriptor: %r" % (a,))
+    return rows
 
 
 class GlobalKernel:
     """``GlobalKernel(local_kernel, arguments, *, extruded=False,
     extruded_periodic=False, constant_layers=False, subset=False,
     iteration_region=None, pass_layer_arg=False)`` (pyop2/global_kernel.py:
-    248-320): validates the description and keys it as the reference does."""
+    248-320): the description of one generated wrapper."""
 
     def __init__(self, local_kernel, arguments, *, extruded=False, extruded_periodic=False,
                  constant_layers=False, subset=False, iteration_region=None,
@@ -171,12 +290,6 @@ class GlobalKernel:
         if constant_layers and not extruded:
             raise ValueError("Cannot request constant_layers argument for non-extruded "
                              "iteration")
-        counter = itertools.count()
-        seen_maps = collections.defaultdict(lambda: next(counter))
-        self.cache_key = (local_kernel.cache_key, *[a.cache_key for a in arguments],
-                          *[seen_maps[m] for a in arguments for m in a.maps],
-                          extruded, extruded_periodic, constant_layers, subset,
-                          iteration_region, pass_layer_arg)
         self.local_kernel = local_kernel
         self.arguments = tuple(arguments)
         self._extruded = extruded
@@ -185,6 +298,12 @@ class GlobalKernel:
         self._subset = subset
         self._iteration_region = iteration_region
         self._pass_layer_arg = pass_layer_arg
+        table = _DescTable()
+        rows = tuple(_arg_rows(self.arguments, table))
+        flags = (("extruded", extruded), ("extruded_periodic", extruded_periodic),
+                 ("constant_layers", constant_layers), ("subset", subset),
+                 ("iteration_region", iteration_region), ("pass_layer_arg", pass_layer_arg))
+        self.cache_key = (local_kernel.cache_key, rows, tuple(table.entries), flags)
 
     @property
     def name(self):
@@ -196,7 +315,7 @@ class GlobalKernel:
 
 
 def check_constants(global_knl, arguments):
-    """Constants may only be READ (pyop2/global_kernel.py:287-294)."""
+    """A Constant may only be read (pyop2/global_kernel.py:287-294)."""
     for acc, parg in zip(global_knl.local_kernel.accesses, arguments):
         if isinstance(getattr(parg, "data", None), Constant) and acc is not Access.READ:
             raise ValueError("Constants can only ever be read in a parloop, not modified")

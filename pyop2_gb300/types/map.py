@@ -109,9 +109,15 @@ class Map:
 
     @property
     def _global_kernel_arg(self):
-        from pyop2_gb300.global_kernel import MapKernelArg
-        return MapKernelArg(self.arity, utils.tuplify(self.offset),
-                            utils.tuplify(self.offset_quotient))
+        """This map's descriptor, one object per map (arguments through the
+        same map share it, which is how a GlobalKernel's key sees the map
+        shared)."""
+        d = self.__dict__.get("_gk_arg")
+        if d is None:
+            from pyop2_gb300.global_kernel import MapKernelArg
+            d = self.__dict__["_gk_arg"] = MapKernelArg(
+                self.arity, utils.tuplify(self.offset), utils.tuplify(self.offset_quotient))
+        return d
 
     @property
     def _cache_key(self):
@@ -191,8 +197,12 @@ class PermutedMap(Map):
 
     @property
     def _global_kernel_arg(self):
-        from pyop2_gb300.global_kernel import PermutedMapKernelArg
-        return PermutedMapKernelArg(self.map_._global_kernel_arg, tuple(self.permutation))
+        d = self.__dict__.get("_gk_arg")
+        if d is None:
+            from pyop2_gb300.global_kernel import PermutedMapKernelArg
+            d = self.__dict__["_gk_arg"] = PermutedMapKernelArg(self.map_._global_kernel_arg,
+                                                                tuple(self.permutation))
+        return d
 
     def __init__(self, map_, permutation):
         if not isinstance(map_, Map):
@@ -253,8 +263,12 @@ class ComposedMap(Map):
 
     @property
     def _global_kernel_arg(self):
-        from pyop2_gb300.global_kernel import ComposedMapKernelArg
-        return ComposedMapKernelArg(*(m._global_kernel_arg for m in self.maps_))
+        d = self.__dict__.get("_gk_arg")
+        if d is None:
+            from pyop2_gb300.global_kernel import ComposedMapKernelArg
+            d = self.__dict__["_gk_arg"] = ComposedMapKernelArg(
+                *(m._global_kernel_arg for m in self.maps_))
+        return d
 
     def __init__(self, *maps_, name=None):
         if not all(isinstance(m, Map) for m in maps_):

@@ -77,3 +77,28 @@ def test_new_style_parloop_runs_and_replaces_data(gpu_op2):
     pl.compute()
     assert np.array_equal(y2.data_ro, expect) and np.array_equal(y.data_ro, expect)
     assert pl.arguments[0].data is y2
+
+
+def test_global_kernel_key_sees_shared_maps():
+    """Two arguments through one map give another key than two arguments
+    through two maps of the same shape (the map table entry is shared)."""
+    cells, verts, m, x, y, g, vals = _setup()
+    m2 = op2.Map(cells, verts, 3, vals)
+    k = op2.Kernel("static void k(double *y, const double *x) {}", "k",
+                   accesses=(op2.INC, op2.READ))
+    same = op2.GlobalKernel(k, (op2.DatKernelArg((1,), m._global_kernel_arg),
+                                op2.DatKernelArg((1,), m._global_kernel_arg)))
+    same2 = op2.GlobalKernel(k, (op2.DatKernelArg((1,), m._global_kernel_arg),
+                                 op2.DatKernelArg((1,), m._global_kernel_arg)))
+    other = op2.GlobalKernel(k, (op2.DatKernelArg((1,), m._global_kernel_arg),
+                                 op2.DatKernelArg((1,), m2._global_kernel_arg)))
+    assert same.cache_key == same2.cache_key
+    assert same.cache_key != other.cache_key
+    assert op2.DatKernelArg((1,), m._global_kernel_arg) == \
+        op2.DatKernelArg((1,), m._global_kernel_arg)
+    with pytest.raises(ValueError):
+        op2.MapKernelArg(3, offset=[1, 1, 1])          # unhashable offset
+    with pytest.raises(TypeError):
+        op2.ComposedMapKernelArg(object())
+    with pytest.raises(AttributeError):
+        m._global_kernel_arg.arity = 4                  # descriptors are immutable
