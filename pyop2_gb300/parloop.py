@@ -837,7 +837,11 @@ class ColourPlan:
                 return False
             for m in maps:
                 vals = m._device_values()[:m.values_with_halo.nbytes].view(torch.int32)
-                t = vals.view(-1, m.arity)[seg].reshape(-1)
+                t = vals.view(-1, m.arity)[seg]
+                # a cell may name one target twice: count each target once per cell
+                t, _ = torch.sort(t, dim=1)
+                t[:, 1:][t[:, 1:] == t[:, :-1]] = -1
+                t = t.reshape(-1)
                 t = t[t >= 0]
                 if torch.unique(t).numel() != t.numel():
                     return False
