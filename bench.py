@@ -241,6 +241,15 @@ def cpu_baseline(problem_np, threads=1, reps=3, max_cells=None):
     return C / best, C, best
 
 
+def _config(cells, vertices, permute):
+    """The workload description, identical in both arms."""
+    from pyop2_gb300 import workloads
+    alg = workloads.bytes_c2a(cells, vertices)
+    return {"workload": "p1_tet_laplace_action_128cube", "cells": cells, "vertices": vertices,
+            "numbering": "random_permutation" if permute else "lexicographic",
+            "l2": "working set %.0f MB > 129 MB L2, no flush" % (alg / 1e6)}
+
+
 def run_reference(args):
     world, rank, local = _dist()
     if rank != 0:
@@ -262,8 +271,7 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "p1_tet_laplace_action_128cube", "cells": int(cells.shape[0]),
-                   "vertices": int(coords.shape[0]), "numbering": "lexicographic"},
+        "config": _config(int(cells.shape[0]), int(coords.shape[0]), False),
         "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port",
                          "sample": "full workload per step; oracle C wrapper built with the "
                                    "reference's flags, one thread per contiguous cell range "
@@ -342,6 +350,32 @@ def e2e_pipelined(op2, p, loop0, steps, barrier):
     return max_over_ranks(e0.elapsed_time(e1), device=torch.device("cuda"))
 
 
+def e2e_serial(op2, p, steps, warmup, barrier):
+    """Wall-clock ms for `steps` end-to-end steps through PyOP2's own data
+    API, one after another: ``x.data[:] = host`` (the host array becomes the
+    newer copy), ``y.zero()``, ``op2.par_loop(...)`` (uploads x, runs the
+    action) and ``y.data_ro`` (waits, downloads y).  Nothing overlaps.
+    Returns the max over ranks."""
+    import torch
+    x_host = p["x"].data_ro.copy()
+
+    def step():
+        p["x"].data[:] = x_host
+        p["y"].zero()
+        op2.par_loop(p["kernel"], p["cells"], p["y"](op2.INC, p["c2v"]),
+                     p["X"](op2.READ, p["c2v"]), p["x"](op2.READ, p["c2v"]))
+        return p["y"].data_ro
+    for _ in range(warmup):
+        step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    ms = 1e3 * (time.perf_counter() - t0)
+    barrier()
+    return max_over_ranks(ms, device=torch.device("cuda"))
+
+
 def measure_strategies(op2, p, steps, warmup):
     """The benchmark action under each INC conflict strategy (hardware
     atomics, warp-aggregated atomics, greedy colouring, per-CTA shared-memory
@@ -350,7 +384,7 @@ def measure_strategies(op2, p, steps, warmup):
     out = {}
     old = configuration["scatter"]
     try:
-        for sc in ("atomic", "warp", "colour", "shared"):
+        for sc in ("atomic", "warp", "colour", "shared", "staged"):
             configuration["scatter"] = sc
             lp = op2.ParLoop(p["kernel"], p["cells"], p["y"](op2.INC, p["c2v"]),
                              p["X"](op2.READ, p["c2v"]), p["x"](op2.READ, p["c2v"]))
@@ -393,10 +427,60 @@ def measure_adjoint(op2, steps, warmup, n=64):
     tf = _time_loop(fwd, steps, warmup)
     tb = _time_loop(bwd, steps, warmup)
     tu = _time_loop(fus, steps, warmup)
-    return {"workload": "nonlinear_residual_p1_tet_64cube", "cells": C, "vertices": V,
-            "forward_ms": tf, "adjoint_ms": tb, "fused_forward_adjoint_ms": tu,
-            "ratio_forward_plus_adjoint_over_forward": (tf + tb) / tf,
-            "ratio_fused_over_forward": tu / tf, "launches": 3 * (steps + warmup)}
+    out = {"workload": "nonlinear_residual_p1_tet_64cube", "cells": C, "vertices": V,
+           "forward_ms": tf, "adjoint_ms": tb, "fused_forward_adjoint_ms": tu,
+           "ratio_forward_plus_adjoint_over_forward": (tf + tb) / tf,
+           "ratio_fused_over_forward": tu / tf, "launches": 3 * (steps + warmup)}
+    out["autograd"] = measure_adjoint_autograd(op2, p, steps, warmup)
+    return out
+
+
+def measure_adjoint_autograd(op2, p, steps, warmup):
+    """The adjoint on the path a user takes: AdjointParLoop behind
+    torch.autograd.Function.  Forward = F = loop(u, kappa) with u and kappa
+    requiring gradients; forward + backward = the same followed by
+    F.backward(lambda), which runs the VJP loop and fills u.grad and
+    kappa.grad.  Timed with CUDA events on the launch stream and on the wall
+    clock (host overhead included), per step."""
+    import torch
+    from pyop2_gb300 import workloads as W
+    from pyop2_gb300.adjoint import AdjointParLoop
+    loop = AdjointParLoop(
+        p["cells"], op2.Kernel(W.NL_RESIDUAL, "nl_residual"),
+        op2.Kernel(W.NL_RESIDUAL_VJP, "nl_residual_vjp"),
+        output=(p["verts"] ** 1, p["c2v"]),
+        inputs=[(p["verts"] ** 1, p["c2v"]), (p["cells"] ** 1, None)],
+        constants=[(p["X"], p["c2v"])])
+    dev = torch.device("cuda")
+    u = torch.tensor(p["u"], device=dev, requires_grad=True)
+    k = torch.tensor(p["kappa"], device=dev, requires_grad=True)
+    lam = torch.tensor(p["lam"], device=dev)
+
+    def fwd():
+        return loop(u, k)
+
+    def fwd_bwd():
+        u.grad = None
+        k.grad = None
+        loop(u, k).backward(lam)
+
+    res = {}
+    for name, fn in (("forward", fwd), ("forward_backward", fwd_bwd)):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        e1.synchronize()
+        res[name + "_ms"] = e0.elapsed_time(e1) / steps
+        res[name + "_wall_ms"] = 1e3 * (time.perf_counter() - t0) / steps
+    res["ratio_forward_backward_over_forward"] = res["forward_backward_ms"] / res["forward_ms"]
+    res["ratio_wall"] = res["forward_backward_wall_ms"] / res["forward_wall_ms"]
+    return res
 
 
 def measure_batch(op2, steps, warmup, nmeshes=256):
@@ -743,7 +827,13 @@ def measure_data_path(op2, p, steps, warmup):
                                       cells, y(op2.INC, c2v), w(op2.READ)), 24 * C + 16 * V),
     }
     from pyop2_gb300 import _lib
-    for sc, nm in ((_lib.SCATTER_WARP, "scatter_inc_warp"), (_lib.SCATTER_SHARED, "scatter_inc_shared")):
+    pl = LegacyParloop(K("static void ga(double *o, const double *x) "
+                         "{ o[0] = x[0] + x[1] + x[2] + x[3]; }", "ga"),
+                       cells, out(op2.WRITE), x(op2.READ, c2v))
+    pl.build(_lib.SCATTER_STAGED)
+    loops["gather_staged"] = (pl, 24 * C + 8 * V)
+    for sc, nm in ((_lib.SCATTER_WARP, "scatter_inc_warp"), (_lib.SCATTER_SHARED, "scatter_inc_shared"),
+                   (_lib.SCATTER_STAGED, "scatter_inc_staged")):
         pl = LegacyParloop(K("static void sc(double *y, const double *w) "
                              "{ for (int i = 0; i < 4; ++i) y[i] += w[0]; }", "sc"),
                            cells, y(op2.INC, c2v), w(op2.READ))
@@ -847,12 +937,17 @@ def run_ours(args):
     # the copies of steps k-1 and k+1, as a user streaming inputs would.
     e2e_ms = e2e_pipelined(op2, p, loop, args.steps, barrier)
     e2e = job_rate(C, args.steps, e2e_ms, world)
+    # ... and one step after another through the PyOP2 data API
+    e2e_serial_ms = e2e_serial(op2, p, args.steps, args.warmup, barrier)
 
-    # FP64 ceiling: measured DFMA throughput of this GPU
+    # FP64 ceiling: measured DFMA throughput of this GPU, with the SM clock
+    # sampled while the probe runs
     import ctypes
     fl = ctypes.c_double()
-    _lib.call("op2g_probe_fp64_peak", ctypes.byref(fl), device.stream_handle())
+    with ClockSampler(local) as pclk:
+        _lib.call("op2g_probe_fp64_peak", ctypes.byref(fl), device.stream_handle())
     fp64_peak = fl.value / 1e12
+    probe_clocks = pclk.summary()
 
     if rank != 0:
         return 0
@@ -872,6 +967,12 @@ def run_ours(args):
     # FP64 issue roofline: the kernel's FP64 instructions per cell (ncu
     # instruction mix, recorded in the profile) at the sampled clock
     clocks = clk.summary()
+    sms = device.sm_count()
+    # the nominal FP64 rate at a clock: 2 FMA lanes per SM per clock (304 per
+    # clock on 152 SMs), 2 flop each
+    nominal_at = (lambda mhz: sms * 2 * 2 * mhz * 1e6 / 1e12) if sms else None
+    probe_mhz = probe_clocks.get("sm_mhz")
+    kern_mhz = clocks.get("sm_mhz")
     fp64_ipc = _profile_number("op2g_wrap_p1_laplace_3d_128cube.md", "fp64_instructions_per_cell")
     issue_frac = None
     if fp64_ipc and clocks.get("sm_mhz"):
@@ -913,29 +1014,52 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_launch_ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": "p1_tet_laplace_action_128cube", "cells": C, "vertices": V,
-                   "numbering": "random_permutation" if args.permute else "lexicographic",
-                   "scatter": configuration["scatter"], "l2": "working set %.0f MB > 129 MB L2, "
-                   "no flush" % (alg_bytes / 1e6), "parallelism": "replicas" if world > 1 else "1gpu"},
+        "config": _config(C, V, args.permute),
+        "scatter": configuration["scatter"],
+        "parallelism": "replicas" if world > 1 else "1gpu",
         "pct_hbm_peak": 100.0 * achieved / peak,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu "
+                                       "capture of this kernel on this workload, recorded in "
+                                       "profiles/op2g_wrap_p1_laplace_3d_128cube.md",
                      "alg_bytes_per_launch": alg_bytes},
         "roofline_fp64": {"achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                           "frac": fp64_achieved / fp64_peak, "flops_per_cell": workloads.P1_3D_FLOPS,
-                          "peak_source": "measured live (DFMA probe)",
-                          "nominal_peak": 304 * 2 * 2.07e9 / 1e12,
-                          "frac_of_nominal": fp64_achieved / (304 * 2 * 2.07e9 / 1e12),
-                          "nominal_source": "ncu sm__sass_thread_inst_executed_op_dfma peak "
-                                            "304 DFMA/clk x 2 flop x 2.07 GHz",
+                          "peak_source": "measured live (DFMA probe: 16 independent FMA chains "
+                                         "per thread, 8 x 256 threads per SM, best of 5)",
+                          "probe_clocks": probe_clocks,
+                          "probe_fma_per_sm_per_clk": (fl.value / 2 / sms / (probe_mhz * 1e6)
+                                                       if probe_mhz and sms else None),
+                          "nominal_peak_at_probe_clock": nominal_at(probe_mhz) if probe_mhz else None,
+                          "probe_frac_of_nominal_at_its_clock": (fp64_peak / nominal_at(probe_mhz)
+                                                                 if probe_mhz else None),
+                          "nominal_peak_at_kernel_clock": nominal_at(kern_mhz) if kern_mhz else None,
+                          "frac_of_nominal_at_kernel_clock": (fp64_achieved / nominal_at(kern_mhz)
+                                                              if kern_mhz else None),
+                          "nominal_source": "2 FP64 FMA lanes per SM per clock (ncu peak of "
+                                            "sm__sass_thread_inst_executed_op_dfma: 304 per "
+                                            "clock on 152 SMs) x 2 flop x the sampled SM clock",
                           "fp64_pipe_active_ncu": 0.887,
                           "fp64_instr_per_cell_ncu": fp64_ipc,
+                          "fp64_instr_source": "profiles/op2g_wrap_p1_laplace_3d_128cube.md "
+                                               "(ncu instruction mix of this kernel)",
                           "issue_frac": issue_frac,
                           "issue_peak_source": "304 FP64 instructions/clk x median SM clock "
                                                "sampled in the timed region"},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "cells/s", "h2d_bytes_per_step": 8 * V,
-                "d2h_bytes_per_step": 8 * V},
+                "d2h_bytes_per_step": 8 * V,
+                "mode": "streaming throughput: x in from pinned host memory and y back every "
+                        "step, two buffer sets, copies on their own streams overlapped with "
+                        "the previous and next steps' compute (CUDA events on the compute "
+                        "stream)"},
+        "e2e_serial": {"value": job_rate(C, args.steps, e2e_serial_ms, world), "unit": "cells/s",
+                       "ms_per_step": e2e_serial_ms / args.steps,
+                       "h2d_bytes_per_step": 8 * V, "d2h_bytes_per_step": 8 * V,
+                       "mode": "one step after another through the PyOP2 data API: "
+                               "x.data[:] = host; y.zero(); op2.par_loop(...); y.data_ro "
+                               "(pageable numpy arrays, wall clock)"},
         "strategies": strategies,
         "sparsity_assembly": sparsity,
         "adjoint": adjoint,
@@ -982,7 +1106,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--permute", action="store_true", help="random vertex numbering")
-    ap.add_argument("--scatter", default=None, choices=["atomic", "warp", "colour"])
+    ap.add_argument("--scatter", default=None, choices=["atomic", "warp", "colour", "staged"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the headline action (no adjoint / batch measurements)")

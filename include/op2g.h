@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define OP2G_ABI_VERSION 3
+#define OP2G_ABI_VERSION 4
 
 /* ---------------------------------------------------------------- status */
 typedef int32_t op2g_status;
@@ -92,10 +92,18 @@ enum {
                                   shuffle-reduced atomic per group                    */
     OP2G_SCATTER_PLAIN = 2,    /* plain read-modify-write: only legal when the caller
                                   launches one colour (conflict-free cell set) at a time */
-    OP2G_SCATTER_SHARED = 3    /* each CTA sums its INC contributions per target in a
+    OP2G_SCATTER_SHARED = 3,   /* each CTA sums its INC contributions per target in a
                                   shared-memory hash table, then adds each distinct
                                   target once with a global atomic (non-extruded loops;
                                   atomics elsewhere)                                    */
+    OP2G_SCATTER_STAGED = 4    /* the loop runs on a staging plan (op2g_stage_plan_*):
+                                  per mini-partition, the data of READ and INC Dat
+                                  arguments through plain or permuted maps are staged in
+                                  shared memory at the partition's distinct targets, INC
+                                  contributions are summed there, and each distinct
+                                  target receives one global atomic per partition
+                                  (non-extruded, non-indexed loops; the launch passes the
+                                  plan in op2g_launch_desc.stage)                        */
 };
 
 #define OP2G_MAX_ARGS 32
@@ -192,6 +200,22 @@ int32_t op2g_kernel_num_ptrs(const op2g_kernel *k);
 /* Registers per thread of the loaded kernel (-1 before first launch). */
 int32_t op2g_kernel_num_regs(const op2g_kernel *k);
 
+/* The staging plan of a launch of a wrapper built with OP2G_SCATTER_STAGED:
+ * the iteration range is cut into mini-partitions of `block` iterations
+ * (partition p = [p * block, (p + 1) * block)); for every map of the map table
+ * that the plan covers (entry m; a permuted map uses its base map's entry),
+ * ind_map[m] + ind_off[m][p] .. ind_off[m][p + 1] lists the distinct targets
+ * of partition p in ascending order and loc_map[m][i * arity + j] is the
+ * position of entry (i, j) in its partition's list (0xFFFF for a negative
+ * entry).  Built by op2g_stage_plan_count / _fill; all arrays on the device. */
+typedef struct op2g_stage_desc {
+    int64_t block;
+    const int32_t *ind_map[OP2G_MAX_MAPS];
+    const int64_t *ind_off[OP2G_MAX_MAPS];
+    const uint16_t *loc_map[OP2G_MAX_MAPS];
+    int32_t max_unique[OP2G_MAX_MAPS];  /* largest distinct count of a partition; 0 = no plan */
+} op2g_stage_desc;
+
 typedef struct op2g_launch_desc {
     int64_t start, end;        /* iteration range (entities; indices range if indexed)    */
     const int32_t *layers;     /* device layers array [*, 2] (extruded) or NULL          */
@@ -209,6 +233,8 @@ typedef struct op2g_launch_desc {
                                   (wrappers without shared-memory staging);
                                   -1: one per block_size iterations, no cap;
                                   > 0: exactly this many                               */
+    const op2g_stage_desc *stage; /* OP2G_SCATTER_STAGED wrappers: the plan (host struct,
+                                     read during the call); NULL otherwise             */
 } op2g_launch_desc;
 
 /* Launch the wrapper over [start, end) on `stream`.  Asynchronous. */
@@ -292,6 +318,24 @@ op2g_status op2g_sparsity_count(const op2g_sparsity_desc *d, void *workspace, si
  * workspace (it reuses the row->entity transpose kept there). */
 op2g_status op2g_sparsity_fill(const op2g_sparsity_desc *d, void *workspace, size_t ws_bytes,
                                const int64_t *rowptr, int32_t *colidx, void *stream);
+
+/* ------------------------------------------------------- staging plans */
+/* The staging plan of one map over n iterations in partitions of `block`
+ * iterations (block * arity <= 4096): the local renumbering of the
+ * historical OP2 execution plan, doc/sphinx/source/plan.rst:21-39 (no code
+ * counterpart in this checkout).  `map` is the device int32 [n, arity]
+ * array.  op2g_stage_plan_count writes ind_off[nblocks + 1] (device int64,
+ * exclusive prefix sums of the per-partition distinct counts) and returns the
+ * total and the largest count (synchronises `stream`); op2g_stage_plan_fill
+ * then writes ind_map[total] and loc_map[n * arity] (device).  workspace:
+ * op2g_stage_plan_workspace bytes of device memory. */
+op2g_status op2g_stage_plan_workspace(int64_t n, int32_t arity, int64_t block, size_t *bytes);
+op2g_status op2g_stage_plan_count(int64_t n, int32_t arity, const int32_t *map, int64_t block,
+                                  void *workspace, size_t ws_bytes, int64_t *ind_off,
+                                  int64_t *total, int32_t *max_unique, void *stream);
+op2g_status op2g_stage_plan_fill(int64_t n, int32_t arity, const int32_t *map, int64_t block,
+                                 const int64_t *ind_off, int32_t *ind_map, uint16_t *loc_map,
+                                 void *stream);
 
 /* ----------------------------------------------------------- matrices */
 /* Block-CSR matrix with rdim x cdim row-major blocks (rdim = cdim = 1 is CSR). */

@@ -18,10 +18,10 @@ ERR_INVALID, ERR_COMPILE, ERR_CUDA, ERR_BOUNDS, ERR_NEW_NONZERO, ERR_CAPACITY, \
 DEVERR_MAP_BOUNDS, DEVERR_NEW_NONZERO, DEVERR_CAPACITY = 1, 2, 4
 
 F64, F32, I32, U32, I64, U64, I16, U16, I8, U8 = range(10)
-ABI_VERSION = 3
+ABI_VERSION = 4
 ARG_DAT, ARG_GLOBAL, ARG_MAT, ARG_PASSTHROUGH = range(4)
 MAP_PLAIN, MAP_PERMUTED, MAP_COMPOSED = range(3)
-SCATTER_ATOMIC, SCATTER_WARP, SCATTER_PLAIN, SCATTER_SHARED = range(4)
+SCATTER_ATOMIC, SCATTER_WARP, SCATTER_PLAIN, SCATTER_SHARED, SCATTER_STAGED = range(5)
 MAX_ARGS = 32
 MAX_MAPS = 32
 MAX_COMPOSED = 8
@@ -51,10 +51,15 @@ class LoopDesc(ctypes.Structure):
                 ("batched", _i32), ("prefetch", _i32), ("nc_reads", _i32)]
 
 
+class StageDesc(ctypes.Structure):
+    _fields_ = [("block", _i64), ("ind_map", _p * MAX_MAPS), ("ind_off", _p * MAX_MAPS),
+                ("loc_map", _p * MAX_MAPS), ("max_unique", _i32 * MAX_MAPS)]
+
+
 class LaunchDesc(ctypes.Structure):
     _fields_ = [("start", _i64), ("end", _i64), ("layers", _p), ("indices", _p), ("err", _p),
                 ("ptrs", ctypes.POINTER(_p)), ("map_toset", ctypes.POINTER(_i64)),
-                ("layers_per_entity", _i64), ("grid", _i32)]
+                ("layers_per_entity", _i64), ("grid", _i32), ("stage", ctypes.POINTER(StageDesc))]
 
 
 class SparsityPair(ctypes.Structure):
@@ -114,6 +119,10 @@ SIGNATURES = {
     "op2g_colour_noalloc": (_i32, [_i64, _i32, ctypes.POINTER(_p), _pi32, ctypes.POINTER(_i64),
                                    _i32, _p, _p, _p, _pi32, _p]),
     "op2g_probe_fp64_peak": (_i32, [ctypes.POINTER(ctypes.c_double), _p]),
+    "op2g_stage_plan_workspace": (_i32, [_i64, _i32, _i64, ctypes.POINTER(ctypes.c_size_t)]),
+    "op2g_stage_plan_count": (_i32, [_i64, _i32, _p, _i64, _p, ctypes.c_size_t, _p,
+                                     ctypes.POINTER(_i64), _pi32, _p]),
+    "op2g_stage_plan_fill": (_i32, [_i64, _i32, _p, _i64, _p, _p, _p, _p]),
 }
 
 _lib = None

@@ -30,6 +30,11 @@ class AdjointParLoop:
     constants: list of (Dat, map or None) read-only, not differentiated.
     Call it with one torch tensor per input; it returns the residual tensor
     and is differentiable with respect to every input.
+
+    The forward, VJP and fused loops are built once, on the first call that
+    needs them, over Dats that wrap the call's tensors; later calls rebind
+    those Dats to their own tensors (no copy) and launch the built loops, so
+    a call costs a launch, not a loop construction.
     """
 
     def __init__(self, iterset, kernel, vjp_kernel, output, inputs, constants=(),
@@ -41,63 +46,81 @@ class AdjointParLoop:
         self.output = output
         self.inputs = list(inputs)
         self.constants = list(constants)
+        self._loops = {}       # "forward" / "vjp" / "fused" -> (ParLoop, Dats to rebind)
 
     def _shape(self, dataset):
         return (dataset.total_size,) + (() if dataset.cdim == 1 else tuple(dataset.dim))
 
-    def _wrap(self, dataset, t):
-        return Dat.from_tensor(dataset, t.contiguous())
+    def _zeros(self, dataset):
+        return torch.zeros(self._shape(dataset), dtype=torch.float64, device=device.device())
 
     def _const_args(self):
         return [d(READ, m) if m is not None else d(READ) for d, m in self.constants]
 
-    def _input_args(self, xs):
-        out = []
-        for (ds, m), x in zip(self.inputs, xs):
-            d = self._wrap(ds, x.detach())
-            out.append(d(READ, m) if m is not None else d(READ))
-        return out
+    def _run(self, which, tensors, build):
+        """Launch loop `which` on `tensors` (one per Dat it rebinds, in the
+        order `build` created them); `build(dats)` returns its arguments."""
+        hit = self._loops.get(which)
+        if hit is None:
+            from pyop2_gb300.parloop import ParLoop
+            specs = self._specs(which)
+            dats = [Dat.from_tensor(ds, t) for (ds, _), t in zip(specs, tensors)]
+            knl = {"forward": self.kernel, "vjp": self.vjp_kernel,
+                   "fused": self.fused_kernel}[which]
+            hit = (ParLoop(knl, self.iterset, *build(dats)), dats)
+            self._loops[which] = hit
+        else:
+            for d, t in zip(hit[1], tensors):
+                d._rebind(t)
+        hit[0].compute()
 
-    def _grad_args(self, grads):
-        out = []
-        for (ds, m), g in zip(self.inputs, grads):
-            d = self._wrap(ds, g)
-            out.append(d(INC, m) if m is not None else d(WRITE))
-        return out
+    def _specs(self, which):
+        """(dataset, map) of every rebound Dat of loop `which`, in order."""
+        out = [self.output]
+        if which == "fused":
+            out = [self.output, self.output]          # F, lambda
+        elif which == "vjp":
+            out = [self.output]                       # lambda
+        return out + self.inputs + ([] if which == "forward" else self.inputs)
+
+    def _input_args(self, dats):
+        return [d(READ, m) if m is not None else d(READ) for (_, m), d in zip(self.inputs, dats)]
+
+    def _grad_args(self, dats):
+        return [d(INC, m) if m is not None else d(WRITE) for (_, m), d in zip(self.inputs, dats)]
 
     def forward_values(self, *xs):
         """Residual for inputs xs (no autograd)."""
-        from pyop2_gb300.parloop import par_loop
-        ods, omap = self.output
-        F = torch.zeros(self._shape(ods), dtype=torch.float64, device=device.device())
-        Fd = self._wrap(ods, F)
-        par_loop(self.kernel, self.iterset, Fd(INC, omap), *self._const_args(),
-                 *self._input_args(xs))
+        F = self._zeros(self.output[0])
+        omap = self.output[1]
+        n = len(self.inputs)
+        self._run("forward", [F] + [x.detach().contiguous() for x in xs],
+                  lambda d: [d[0](INC, omap), *self._const_args(), *self._input_args(d[1:1 + n])])
         return F
 
     def vjp(self, lam, *xs):
         """Gradients of lam . F with respect to every input."""
-        from pyop2_gb300.parloop import par_loop
-        ods, omap = self.output
-        grads = [torch.zeros(self._shape(ds), dtype=torch.float64, device=device.device())
-                 for ds, _ in self.inputs]
-        ld = self._wrap(ods, lam.detach())
-        par_loop(self.vjp_kernel, self.iterset, ld(READ, omap), *self._const_args(),
-                 *self._input_args(xs), *self._grad_args(grads))
+        grads = [self._zeros(ds) for ds, _ in self.inputs]
+        omap = self.output[1]
+        n = len(self.inputs)
+        self._run("vjp", [lam.detach().contiguous()] + [x.detach().contiguous() for x in xs] +
+                  grads,
+                  lambda d: [d[0](READ, omap), *self._const_args(),
+                             *self._input_args(d[1:1 + n]), *self._grad_args(d[1 + n:])])
         return grads
 
     def fused(self, lam, *xs):
         """Residual and the gradients of lam . F in one pass."""
-        from pyop2_gb300.parloop import par_loop
         if self.fused_kernel is None:
             raise ValueError("no fused kernel given")
-        ods, omap = self.output
-        F = torch.zeros(self._shape(ods), dtype=torch.float64, device=device.device())
-        grads = [torch.zeros(self._shape(ds), dtype=torch.float64, device=device.device())
-                 for ds, _ in self.inputs]
-        ld = self._wrap(ods, lam.detach())
-        par_loop(self.fused_kernel, self.iterset, self._wrap(ods, F)(INC, omap), ld(READ, omap),
-                 *self._const_args(), *self._input_args(xs), *self._grad_args(grads))
+        F = self._zeros(self.output[0])
+        grads = [self._zeros(ds) for ds, _ in self.inputs]
+        omap = self.output[1]
+        n = len(self.inputs)
+        self._run("fused", [F, lam.detach().contiguous()] +
+                  [x.detach().contiguous() for x in xs] + grads,
+                  lambda d: [d[0](INC, omap), d[1](READ, omap), *self._const_args(),
+                             *self._input_args(d[2:2 + n]), *self._grad_args(d[2 + n:])])
         return F, grads
 
     def __call__(self, *xs):

@@ -13,13 +13,19 @@ _CHOICES = {}
 def candidates(loop):
     """(scatter, block size, prefetch, grid) tuples worth timing for this
     loop: every INC strategy that applies (atomics, warp aggregation,
-    shared-memory staging, colouring), three CTA sizes, for non-extruded
+    shared-memory hash tables, colouring, a staging plan), three CTA sizes,
+    for non-extruded
     loops the map-row prefetch on and off (the staging depth), and the two
     grid policies (up to 4 resident waves, or one CTA per block of cells)."""
     it = loop.iterset
     pfs = (0, 1) if not it._extruded else (0,)
     out = []
+    staged = loop._stageable()
     for bs in (128, 256, 512):
+        if staged:
+            # staged partitions take their partition in turn; prefetch and the
+            # grid policy do not apply
+            out.append((_lib.SCATTER_STAGED, bs, 0, 0))
         for pf in pfs:
             for grid in (0, -1):
                 out.append((_lib.SCATTER_ATOMIC, bs, pf, grid))

@@ -28,8 +28,12 @@ class Configuration(dict):
         "compute_kernel_flops": ("PYOP2_COMPUTE_KERNEL_FLOPS", bool, False),
         "print_cache_info": ("PYOP2_CACHE_INFO", bool, False),
         # INC conflict resolution: "atomic", "warp", "colour", "shared" (per-CTA
-        # shared-memory sums, one atomic per distinct target) or "auto" (autotuner)
+        # shared-memory sums, one atomic per distinct target), "staged" (a
+        # staging plan: READ and INC data of each mini-partition in shared
+        # memory at its distinct targets) or "auto" (autotuner)
         "scatter": ("OP2G_SCATTER", str, "atomic"),
+        # iterations per mini-partition of a staging plan (at most 4096 / arity)
+        "stage_cells": ("OP2G_STAGE_CELLS", int, 512),
         # threads per CTA of generated wrappers
         "block_size": ("OP2G_BLOCK_SIZE", int, 256),
         # let the autotuner pick scatter strategy, block size and prefetch per kernel
@@ -92,8 +96,10 @@ class Configuration(dict):
             if not ok:
                 raise ConfigurationError("Values for configuration key %s must be of type %r, "
                                          "not %r" % (key, typ, type(value)))
-        if key == "scatter" and value not in ("atomic", "warp", "colour", "shared", "auto"):
-            raise ConfigurationError("scatter must be atomic, warp, colour, shared or auto")
+        if key == "scatter" and value not in ("atomic", "warp", "colour", "shared", "staged",
+                                              "auto"):
+            raise ConfigurationError("scatter must be atomic, warp, colour, shared, staged or "
+                                     "auto")
         self._set.add(key)
         super().__setitem__(key, value)
 

@@ -20,7 +20,7 @@ ROOT = os.path.dirname(PKG)
 OUT = os.path.join(PKG, "libop2g.so")
 BUILD_DIR = os.path.join(HERE, "_build")
 
-SOURCES = ["op2g_runtime.cpp", "op2g_codegen.cpp", "op2g_kernels.cu"]
+SOURCES = ["op2g_runtime.cpp", "op2g_codegen.cpp", "op2g_kernels.cu", "op2g_stage.cu"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

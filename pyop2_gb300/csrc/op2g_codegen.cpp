@@ -93,6 +93,66 @@ static bool declared_without_parameters(const std::string &src, const std::strin
 }
 
 // ---------------------------------------------------------------------------
+// Which arguments a staged wrapper (OP2G_SCATTER_STAGED) stages in shared
+// memory: Dat arguments (not parts of a mixed argument) through a plain map
+// or a permuted one, READ when no argument of the loop writes a Dat that a
+// READ argument reads (staged values are read once per partition), and INC
+// with an element type shared-memory atomics support.  Entry a is the plain
+// map whose plan the argument uses, or -1.  Non-extruded, non-indexed loops
+// only; an empty result means the wrapper runs as OP2G_SCATTER_ATOMIC.
+std::vector<int> staged_args(const Signature &S) {
+    std::vector<int> st(S.args.size(), -1);
+    if (S.loop.scatter != OP2G_SCATTER_STAGED || S.loop.extruded || S.loop.indexed) return st;
+    bool any = false;
+    for (size_t a = 0; a < S.args.size(); ++a) {
+        const op2g_arg_desc &d = S.args[a].d;
+        if (d.kind != OP2G_ARG_DAT || d.map < 0 || d.group != 0) continue;
+        const MapInfo &mi = S.maps[d.map];
+        int root = -1;
+        if (mi.kind == OP2G_MAP_PLAIN) root = d.map;
+        else if (mi.kind == OP2G_MAP_PERMUTED) root = mi.base;
+        if (root < 0) continue;
+        const bool inc_ok = d.access == OP2G_INC &&
+                            (d.dtype == OP2G_F64 || d.dtype == OP2G_F32 || d.dtype == OP2G_I32 ||
+                             d.dtype == OP2G_U32 || d.dtype == OP2G_U64 || d.dtype == OP2G_I64);
+        const bool read_ok = d.access == OP2G_READ && S.loop.nc_reads;
+        if (!inc_ok && !read_ok) continue;
+        st[a] = root;
+        any = true;
+    }
+    (void)any;
+    return st;
+}
+
+static size_t elt_size(int dt) {
+    switch (dt) {
+        case OP2G_F64: case OP2G_I64: case OP2G_U64: return 8;
+        case OP2G_F32: case OP2G_I32: case OP2G_U32: return 4;
+        case OP2G_I16: case OP2G_U16: return 2;
+        default: return 1;
+    }
+}
+
+// Bytes of dynamic shared memory a staged wrapper takes for partitions whose
+// largest distinct-target counts are max_unique[m] (the layout the generated
+// code computes: per staged map its target list, per staged argument its
+// values, each region rounded up to 16 bytes).
+size_t staged_smem_bytes(const Signature &S, const int32_t *max_unique) {
+    std::vector<int> st = staged_args(S);
+    auto r16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+    size_t bytes = 0;
+    std::vector<bool> seen(S.maps.size(), false);
+    for (size_t a = 0; a < st.size(); ++a)
+        if (st[a] >= 0 && !seen[st[a]]) {
+            seen[st[a]] = true;
+            bytes += r16((size_t)max_unique[st[a]] * 4);
+        }
+    for (size_t a = 0; a < st.size(); ++a)
+        if (st[a] >= 0)
+            bytes += r16((size_t)max_unique[st[a]] * S.args[a].d.dim * elt_size(S.args[a].d.dtype));
+    return bytes;
+}
+
 struct Gen {
     const Signature &S;
     std::ostringstream o;
@@ -108,9 +168,23 @@ struct Gen {
     std::vector<int> psize;   // at first: size of the parameter's pack
     bool has_groups = false;
 
+    // Staging (OP2G_SCATTER_STAGED): per argument the plain map of its plan
+    // or -1; per map whether the wrapper loads its plan; set while the
+    // staged run function is written.
+    std::vector<int> st_arg;
+    std::vector<bool> st_map;
+    bool any_staged = false, staging = false;
+
     explicit Gen(const Signature &s) : S(s) {
         nf = (S.loop.extruded && S.loop.iteration_region == OP2G_ON_INTERIOR_FACETS) ? 2 : 1;
         layout();
+        st_arg = staged_args(S);
+        st_map.assign(S.maps.size(), false);
+        for (int r : st_arg)
+            if (r >= 0) {
+                st_map[r] = true;
+                any_staged = true;
+            }
     }
 
     // Elements between consecutive entities' values of a Dat argument.
@@ -361,6 +435,162 @@ struct Gen {
         }
     }
 
+    // Staged row of plain map m at entity n: local indices lv<m> from the
+    // plan's loc_map (16-bit, read as vectors when the arity allows) and the
+    // global targets mv<m> from the partition's target list in shared memory.
+    void emit_staged_row(int m, const std::string &ind) {
+        const int ar = S.maps[m].arity;
+        const std::string lv = "lv" + std::to_string(m), mv = base_row(m);
+        o << ind << "unsigned short " << lv << "[" << ar << "];\n";
+        o << ind << "int " << mv << "[" << ar << "];\n";
+        o << ind << "{ const unsigned short *r_ = p.sloc[" << m << "] + n * " << ar << ";\n";
+        if (ar % 4 == 0) {
+            for (int q = 0; q < ar / 4; ++q)
+                o << ind << "  { const ushort4 v_ = __ldg((const ushort4 *)r_ + " << q << "); " << lv
+                  << "[" << 4 * q << "] = v_.x; " << lv << "[" << 4 * q + 1 << "] = v_.y; " << lv
+                  << "[" << 4 * q + 2 << "] = v_.z; " << lv << "[" << 4 * q + 3 << "] = v_.w; }\n";
+        } else if (ar % 2 == 0) {
+            for (int q = 0; q < ar / 2; ++q)
+                o << ind << "  { const ushort2 v_ = __ldg((const ushort2 *)r_ + " << q << "); " << lv
+                  << "[" << 2 * q << "] = v_.x; " << lv << "[" << 2 * q + 1 << "] = v_.y; }\n";
+        } else {
+            o << ind << "#pragma unroll\n";
+            o << ind << "  for (int i = 0; i < " << ar << "; ++i) " << lv << "[i] = __ldg(r_ + i);\n";
+        }
+        o << ind << "#pragma unroll\n";
+        o << ind << "  for (int i = 0; i < " << ar << "; ++i) " << mv << "[i] = " << lv
+          << "[i] == 0xFFFF ? -1 : si" << m << "[" << lv << "[i]];\n";
+        o << ind << "}\n";
+    }
+
+    // Local index (in its partition's target list) of entry `i` of staged
+    // argument a's map: the plain map's own entry, or the permuted one.
+    std::string local_index(size_t a, const std::string &i) const {
+        const int m = S.args[a].d.map;
+        const int r = st_arg[a];
+        if (m == r) return "(int)lv" + std::to_string(r) + "[" + i + "]";
+        return "(int)lv" + std::to_string(r) + "[op2g_perm" + std::to_string(m) + "[" + i + "]]";
+    }
+
+    // The staged run function: CTAs take mini-partitions of the plan in turn;
+    // per partition the target lists of the staged maps and the values of
+    // staged READ arguments are loaded into shared memory (each distinct
+    // target once), staged INC arguments are summed there, and every
+    // distinct target gets one global atomic when the partition is done.
+    void emit_staged_run() {
+        std::ostringstream &O = o;
+        const int BS = S.block_size;
+        staging = true;
+        O << "__device__ __forceinline__ void op2g_run_staged(const op2g_params_t &p) {\n";
+        O << "  extern __shared__ __align__(16) unsigned char op2g_smem[];\n";
+        emit_global_init();
+        O << "  size_t so_ = 0;\n";
+        for (size_t m = 0; m < S.maps.size(); ++m)
+            if (st_map[m]) {
+                O << "  int *si" << m << " = (int *)(op2g_smem + so_); so_ += ((size_t)p.smax[" << m
+                  << "] * 4 + 15) & ~(size_t)15;\n";
+            }
+        for (size_t a = 0; a < S.args.size(); ++a)
+            if (st_arg[a] >= 0) {
+                const char *T = ctype_of(S.args[a].d.dtype);
+                O << "  " << T << " *sv" << a << " = (" << T << " *)(op2g_smem + so_); so_ += ((size_t)p.smax["
+                  << st_arg[a] << "] * " << S.args[a].d.dim << " * sizeof(" << T
+                  << ") + 15) & ~(size_t)15;\n";
+            }
+        O << "  const long long pb0_ = p.start / p.sblock, pb1_ = (p.end + p.sblock - 1) / p.sblock;\n";
+        O << "  for (long long pb_ = pb0_ + blockIdx.x; pb_ < pb1_; pb_ += gridDim.x) {\n";
+        O << "    const long long c0_ = pb_ * p.sblock > p.start ? pb_ * p.sblock : p.start;\n";
+        O << "    const long long c1_ = (pb_ + 1) * p.sblock < p.end ? (pb_ + 1) * p.sblock : p.end;\n";
+        for (size_t m = 0; m < S.maps.size(); ++m)
+            if (st_map[m]) {
+                O << "    const long long so" << m << "_ = p.soff[" << m << "][pb_];\n";
+                O << "    const int nu" << m << "_ = (int)(p.soff[" << m << "][pb_ + 1] - so" << m << "_);\n";
+                O << "    for (int k_ = threadIdx.x; k_ < nu" << m << "_; k_ += " << BS << ") si" << m
+                  << "[k_] = __ldg(p.sind[" << m << "] + so" << m << "_ + k_);\n";
+            }
+        O << "    __syncthreads();\n";
+        for (size_t a = 0; a < S.args.size(); ++a) {
+            if (st_arg[a] < 0) continue;
+            const op2g_arg_desc &d = S.args[a].d;
+            const char *T = ctype_of(d.dtype);
+            const int D = d.dim, r = st_arg[a];
+            O << "    for (int k_ = threadIdx.x; k_ < nu" << r << "_ * " << D << "; k_ += " << BS
+              << ") {\n";
+            if (d.access == OP2G_READ) {
+                O << "      const int v_ = k_ / " << D << ";\n";
+                O << "      sv" << a << "[k_] = __ldg((const " << T << " *)p.ptr[" << S.args[a].slot
+                  << "] + (long long)si" << r << "[v_] * " << gstride(a) << " + (k_ - v_ * " << D
+                  << "));\n";
+            } else {
+                O << "      sv" << a << "[k_] = (" << T << ")0;\n";
+            }
+            O << "    }\n";
+        }
+        O << "    __syncthreads();\n";
+        O << "    for (long long it = c0_ + threadIdx.x; it < c1_; it += " << BS << ") {\n";
+        O << "      const long long n = it;\n";
+        emit_body("      ", false, false);
+        O << "    }\n";
+        O << "    __syncthreads();\n";
+        for (size_t a = 0; a < S.args.size(); ++a) {
+            if (st_arg[a] < 0 || S.args[a].d.access != OP2G_INC) continue;
+            const op2g_arg_desc &d = S.args[a].d;
+            const char *T = ctype_of(d.dtype);
+            const int D = d.dim, r = st_arg[a];
+            O << "    for (int k_ = threadIdx.x; k_ < nu" << r << "_ * " << D << "; k_ += " << BS
+              << ") {\n";
+            O << "      const int v_ = k_ / " << D << ";\n";
+            O << "      op2g::atomic_inc((" << T << " *)p.ptr[" << S.args[a].slot << "] + (long long)si"
+              << r << "[v_] * " << gstride(a) << " + (k_ - v_ * " << D << "), sv" << a << "[k_]);\n";
+            O << "    }\n";
+        }
+        O << "    __syncthreads();\n";
+        O << "  }\n";
+        emit_global_reductions();
+        O << "}\n\n";
+        staging = false;
+    }
+
+    // Per-thread accumulators of Global INC/MIN/MAX arguments.
+    void emit_global_init() {
+        std::ostringstream &O = o;
+        for (size_t a = 0; a < S.args.size(); ++a) {
+            const ArgInfo &A = S.args[a];
+            if (A.d.kind != OP2G_ARG_GLOBAL) continue;
+            const char *T = ctype_of(A.d.dtype);
+            if (A.d.access == OP2G_INC) {
+                O << "  " << T << " gacc" << a << "[" << A.d.dim << "];\n";
+                O << "  for (int j = 0; j < " << A.d.dim << "; ++j) gacc" << a << "[j] = (" << T
+                  << ")0;\n";
+            } else if (A.d.access == OP2G_MIN || A.d.access == OP2G_MAX) {
+                O << "  " << T << " gacc" << a << "[" << A.d.dim << "];\n";
+                O << "  for (int j = 0; j < " << A.d.dim << "; ++j) gacc" << a << "[j] = ((const "
+                  << T << " *)p.ptr[" << A.slot << "])[j];\n";
+            }
+        }
+    }
+
+    // Warp-reduced Global results, one atomic per warp (pyop2/parloop.py:
+    // 409-452 semantics on one device: INC goes to the zeroed temporary,
+    // MIN/MAX straight into the Global).
+    void emit_global_reductions() {
+        std::ostringstream &O = o;
+        for (size_t a = 0; a < S.args.size(); ++a) {
+            const ArgInfo &A = S.args[a];
+            if (A.d.kind != OP2G_ARG_GLOBAL || A.d.access == OP2G_READ) continue;
+            const char *T = ctype_of(A.d.dtype);
+            const char *red = A.d.access == OP2G_INC ? "warp_sum"
+                              : A.d.access == OP2G_MIN ? "warp_min" : "warp_max";
+            const char *atom = A.d.access == OP2G_INC ? "atomic_inc"
+                               : A.d.access == OP2G_MIN ? "atomic_min" : "atomic_max";
+            O << "  for (int j = 0; j < " << A.d.dim << "; ++j) {\n";
+            O << "    " << T << " v_ = op2g::" << red << "(gacc" << a << "[j]);\n";
+            O << "    if ((threadIdx.x & 31) == 0) op2g::" << atom << "(((" << T << " *)p.ptr["
+              << A.slot << "]) + j, v_);\n";
+            O << "  }\n";
+        }
+    }
+
     std::string emit() {
         std::ostringstream &O = o;
         O << "// generated by op2g_codegen.cpp for kernel '" << S.kernel_name << "'\n";
@@ -382,8 +612,17 @@ struct Gen {
           << "  const int *indices;\n"
           << "  int *err;\n"
           << "  void *ptr[" << (nptr > 0 ? nptr : 1) << "];\n"
-          << "  long long toset[" << (nmaps > 0 ? nmaps : 1) << "];\n"
-          << "};\n";
+          << "  long long toset[" << (nmaps > 0 ? nmaps : 1) << "];\n";
+        if (any_staged) {
+            // the staging plan (op2g_stage_desc), one entry per map
+            const int nm = nmaps > 0 ? nmaps : 1;
+            O << "  long long sblock;\n"
+              << "  long long smax[" << nm << "];\n"
+              << "  const int *sind[" << nm << "];\n"
+              << "  const long long *soff[" << nm << "];\n"
+              << "  const unsigned short *sloc[" << nm << "];\n";
+        }
+        O << "};\n";
 
         const int BS = S.block_size;
         bool warp = S.loop.scatter == OP2G_SCATTER_WARP;
@@ -406,21 +645,7 @@ struct Gen {
         // ----- the run function: a strided sweep of [start, end) plus reductions
         O << "__device__ __forceinline__ void op2g_run(const op2g_params_t &p, long long start, "
              "long long end, long long first, long long stride) {\n";
-        // Global accumulators
-        for (size_t a = 0; a < S.args.size(); ++a) {
-            const ArgInfo &A = S.args[a];
-            if (A.d.kind != OP2G_ARG_GLOBAL) continue;
-            const char *T = ctype_of(A.d.dtype);
-            if (A.d.access == OP2G_INC) {
-                O << "  " << T << " gacc" << a << "[" << A.d.dim << "];\n";
-                O << "  for (int j = 0; j < " << A.d.dim << "; ++j) gacc" << a << "[j] = (" << T
-                  << ")0;\n";
-            } else if (A.d.access == OP2G_MIN || A.d.access == OP2G_MAX) {
-                O << "  " << T << " gacc" << a << "[" << A.d.dim << "];\n";
-                O << "  for (int j = 0; j < " << A.d.dim << "; ++j) gacc" << a << "[j] = ((const "
-                  << T << " *)p.ptr[" << A.slot << "])[j];\n";
-            }
-        }
+        emit_global_init();
         if (extr) {
             // pyop2/codegen/builder.py:771-812 (layer extents per iteration region)
             O << "  const int *lay_ = p.layers;\n";
@@ -580,22 +805,7 @@ struct Gen {
             O << "    par_ ^= 1;\n";
         }
         O << "  }\n";  // sweep loop
-        // Global reductions (pyop2/parloop.py:409-452 semantics on one device:
-        // INC goes to the zeroed temporary, MIN/MAX straight into the Global).
-        for (size_t a = 0; a < S.args.size(); ++a) {
-            const ArgInfo &A = S.args[a];
-            if (A.d.kind != OP2G_ARG_GLOBAL || A.d.access == OP2G_READ) continue;
-            const char *T = ctype_of(A.d.dtype);
-            const char *red = A.d.access == OP2G_INC ? "warp_sum"
-                              : A.d.access == OP2G_MIN ? "warp_min" : "warp_max";
-            const char *atom = A.d.access == OP2G_INC ? "atomic_inc"
-                               : A.d.access == OP2G_MIN ? "atomic_min" : "atomic_max";
-            O << "  for (int j = 0; j < " << A.d.dim << "; ++j) {\n";
-            O << "    " << T << " v_ = op2g::" << red << "(gacc" << a << "[j]);\n";
-            O << "    if ((threadIdx.x & 31) == 0) op2g::" << atom << "(((" << T << " *)p.ptr["
-              << A.slot << "]) + j, v_);\n";
-            O << "  }\n";
-        }
+        emit_global_reductions();
         O << "}\n\n";
 
         // ----- the entry points.  Without shared-memory staging (whose
@@ -603,11 +813,18 @@ struct Gen {
         // fewer threads per CTA than BS: a small iteration set is then
         // spread over more SMs (each SM issues FP64 at 2 per clock).
         const std::string bdim = any_shared ? std::to_string(BS) : std::string("blockDim.x");
-        O << "extern \"C\" __global__ void __launch_bounds__(" << BS
-          << ") op2g_wrap(const __grid_constant__ op2g_params_t p) {\n"
-          << "  op2g_run(p, p.start, p.end, (long long)blockIdx.x * " << bdim
-          << ", (long long)gridDim.x * " << bdim << ");\n}\n";
-        if (!any_shared) {
+        if (any_staged) {
+            emit_staged_run();
+            O << "extern \"C\" __global__ void __launch_bounds__(" << BS
+              << ") op2g_wrap(const __grid_constant__ op2g_params_t p) {\n"
+              << "  op2g_run_staged(p);\n}\n";
+        } else {
+            O << "extern \"C\" __global__ void __launch_bounds__(" << BS
+              << ") op2g_wrap(const __grid_constant__ op2g_params_t p) {\n"
+              << "  op2g_run(p, p.start, p.end, (long long)blockIdx.x * " << bdim
+              << ", (long long)gridDim.x * " << bdim << ");\n}\n";
+        }
+        if (!any_shared && !any_staged) {
             // Balanced form for launches of a few CTAs per SM: CTA b takes the
             // b-th of gridDim.x equal contiguous chunks of the entities, so a
             // grid of k CTAs per SM gives every SM the same work.
@@ -658,6 +875,10 @@ struct Gen {
         std::vector<bool> need_row = row_maps();
         for (size_t m = 0; m < S.maps.size(); ++m) {
             if (!need_row[m]) continue;
+            if (staging && st_map[m]) {
+                emit_staged_row((int)m, J);
+                continue;
+            }
             if (rows_prefetched) {
                 O << J << "int " << base_row((int)m) << "[" << S.maps[m].arity << "];\n";
                 O << J << "#pragma unroll\n" << J << "for (int i = 0; i < " << S.maps[m].arity
@@ -714,6 +935,16 @@ struct Gen {
                         O << J << "for (int k = 0; k < " << tot << "; ++k) " << tn << "[k] = ("
                           << T << ")0;\n";
                     }
+                } else if (staging && st_arg[a] >= 0) {
+                    // staged: the partition's values sit at the entry's local index
+                    O << J << "#pragma unroll\n";
+                    O << J << "for (int i = 0; i < " << ar << "; ++i) {\n";
+                    O << J << "  const int l_ = " << local_index(a, "i") << ";\n";
+                    O << J << "#pragma unroll\n";
+                    O << J << "  for (int j = 0; j < " << D << "; ++j) " << tn << "[" << po
+                      << "i * " << D << " + j] = l_ != 0xFFFF ? sv" << a << "[l_ * " << D
+                      << " + j] : (" << T << ")0;\n";
+                    O << J << "}\n";
                 } else {
                     O << J << "{ const " << T << " *d_ = (const " << T << " *)p.ptr[" << A.slot
                       << "];\n";
@@ -772,6 +1003,19 @@ struct Gen {
                         O << J << "for (int i = 0; i < " << ar << "; ++i) ti" << an << "[" << f * ar
                           << " + i] = " << idx_arr(A.d.map, f) << "[i];\n";
                     continue;  // scattered after the active block
+                }
+                if (staging && st_arg[a] >= 0) {
+                    // staged INC: summed in shared memory, flushed per partition
+                    O << J << "#pragma unroll\n";
+                    O << J << "for (int i = 0; i < " << ar << "; ++i) {\n";
+                    O << J << "  const int l_ = " << local_index(a, "i") << ";\n";
+                    O << J << "  if (l_ == 0xFFFF) continue;\n";
+                    O << J << "#pragma unroll\n";
+                    O << J << "  for (int j = 0; j < " << D << "; ++j) op2g::atomic_inc(&sv" << a
+                      << "[l_ * " << D << " + j], t" << first[a] << "[" << poff[a] << " + i * " << D
+                      << " + j]);\n";
+                    O << J << "}\n";
+                    continue;
                 }
                 O << J << "{ " << T << " *d_ = (" << T << " *)p.ptr[" << A.slot << "];\n";
                 for (int f = 0; f < nf; ++f) {
@@ -970,7 +1214,7 @@ std::string validate_signature(const Signature &S) {
         a = b;
     }
     if (S.loop.pass_layer_arg && !S.loop.extruded) return "layer argument needs an extruded loop";
-    if (S.loop.scatter < OP2G_SCATTER_ATOMIC || S.loop.scatter > OP2G_SCATTER_SHARED)
+    if (S.loop.scatter < OP2G_SCATTER_ATOMIC || S.loop.scatter > OP2G_SCATTER_STAGED)
         return "unknown scatter strategy";
     return "";
 }

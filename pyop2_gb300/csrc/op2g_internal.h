@@ -40,6 +40,15 @@ struct Signature {
 
 std::string validate_signature(const Signature &S);
 std::string generate_source(const Signature &S);
+// Staged wrappers (OP2G_SCATTER_STAGED): per argument the plain map whose
+// staging plan it uses, or -1; and the dynamic shared memory they take.
+std::vector<int> staged_args(const Signature &S);
+size_t staged_smem_bytes(const Signature &S, const int32_t *max_unique);
+
+// Exclusive in-place prefix sum of d[0..n) on `st` (device memory); tmp holds
+// scan_tmp_elems(n) elements (op2g_kernels.cu).
+size_t scan_tmp_elems(long long n);
+op2g_status scan_exclusive(long long *d, long long n, long long *tmp, struct CUstream_st *st);
 
 // Text of op2g_device.cuh, embedded at build time.
 extern const char *const device_header_src;

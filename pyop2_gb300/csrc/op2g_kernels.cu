@@ -315,7 +315,12 @@ __global__ void k_rows_copy(long long nrows, const long long *__restrict__ candp
     }
 }
 
+}  // namespace
+
+namespace op2g {
+
 // ---------------------------------------------------------------- scan
+// (shared with the staging plan in op2g_stage.cu)
 constexpr int SCAN_T = 1024, SCAN_V = 4, SCAN_B = SCAN_T * SCAN_V;
 
 __global__ void __launch_bounds__(SCAN_T) k_scan_block(long long *__restrict__ d, long long n,
@@ -385,6 +390,13 @@ op2g_status scan_exclusive(long long *d, long long n, long long *tmp, cudaStream
     CK(cudaGetLastError());
     return OP2G_OK;
 }
+
+}  // namespace op2g
+
+namespace {
+
+using op2g::scan_exclusive;
+using op2g::scan_tmp_elems;
 
 // ------------------------------------------------------- sparsity driver
 struct SpLayout {
@@ -1387,16 +1399,23 @@ extern "C" op2g_status op2g_colour_noalloc(int64_t ncells, int32_t nmaps,
 }
 
 // ---------------------------------------------------------------- probe
+// FP64 FMA throughput: every thread runs CHAINS independent FMA chains
+// (x = x * a + b), so each warp always has CHAINS instructions ready while
+// earlier ones are in flight; the grid holds 8 CTAs of 256 threads per SM.
 namespace {
+constexpr int CHAINS = 16;
 __device__ double g_dfma_sink;
 __global__ void __launch_bounds__(256) k_dfma(int iters, double a, double b) {
-    double x0 = threadIdx.x * 1e-9, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
-    double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    double x[CHAINS];
+#pragma unroll
+    for (int c = 0; c < CHAINS; ++c) x[c] = threadIdx.x * 1e-9 + c;
     for (int i = 0; i < iters; ++i) {
-        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
-        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+#pragma unroll
+        for (int c = 0; c < CHAINS; ++c) x[c] = fma(x[c], a, b);
     }
-    const double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < CHAINS; ++c) s += x[c];
     if (s == 1234.5678) g_dfma_sink = s;  // keeps the chains alive
 }
 }  // namespace
@@ -1405,7 +1424,7 @@ extern "C" op2g_status op2g_probe_fp64_peak(double *flops, void *stream) {
     if (!flops) return op2g::fail(OP2G_ERR_INVALID, "NULL output");
     cudaStream_t st = (cudaStream_t)stream;
     const int sms = sms_of_current();
-    const int blocks = sms * 8, threads = 256, iters = 4096;
+    const int blocks = sms * 8, threads = 256, iters = 2048;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
@@ -1422,6 +1441,6 @@ extern "C" op2g_status op2g_probe_fp64_peak(double *flops, void *stream) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    *flops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3);
+    *flops = 2.0 * CHAINS * (double)iters * (double)blocks * threads / (best * 1e-3);
     return OP2G_OK;
 }

@@ -49,6 +49,7 @@ struct Driver {
     CUresult (*FuncGetAttribute)(int *, CUfunction_attribute, CUfunction) = nullptr;
     CUresult (*OccupancyMaxActiveBlocksPerMultiprocessor)(int *, CUfunction, int,
                                                           size_t) = nullptr;
+    CUresult (*FuncSetAttribute)(CUfunction, CUfunction_attribute, int) = nullptr;
     CUresult (*GetErrorString)(CUresult, const char **) = nullptr;
     bool ok = false;
     std::string why;
@@ -70,6 +71,7 @@ static Driver &driver() {
             {"cuOccupancyMaxActiveBlocksPerMultiprocessor",
              (void **)&d.OccupancyMaxActiveBlocksPerMultiprocessor},
             {"cuGetErrorString", (void **)&d.GetErrorString},
+            {"cuFuncSetAttribute", (void **)&d.FuncSetAttribute},
         };
         for (auto &s : syms) {
             cudaDriverEntryPointQueryResult q;
@@ -213,6 +215,11 @@ struct Loaded {
     int regs = -1;
     int occ = 0;  // resident CTAs per SM
     int sms = 0;
+    // staged wrappers: dynamic shared memory the function is set up for, and
+    // the resident CTAs per SM at the last size asked for
+    int smem_attr = 0;
+    size_t occ_smem = (size_t)-1;
+    int occ_at_smem = 0;
 };
 
 // Load `cubin` on the current device (cached per device in `per_dev`).
@@ -252,8 +259,9 @@ op2g_status load_module(const std::string &cubin, const char *fname, const char 
     return OP2G_OK;
 }
 
-op2g_status launch(CUfunction f, unsigned grid, unsigned block, void **params, void *stream) {
-    CUresult r = driver().LaunchKernel(f, grid, 1, 1, block, 1, 1, 0, (CUstream)stream, params,
+op2g_status launch(CUfunction f, unsigned grid, unsigned block, void **params, void *stream,
+                   unsigned smem = 0) {
+    CUresult r = driver().LaunchKernel(f, grid, 1, 1, block, 1, 1, smem, (CUstream)stream, params,
                                        nullptr);
     if (r != CUDA_SUCCESS) return cu_fail(r, "cuLaunchKernel");
     return OP2G_OK;
@@ -279,6 +287,7 @@ struct op2g_kernel {
     std::mutex mu;
     std::map<int, Loaded> per_dev;
     int param_bytes = 0;
+    bool staged = false;   // the wrapper stages arguments on a plan (OP2G_SCATTER_STAGED)
 };
 
 extern "C" {
@@ -362,6 +371,9 @@ op2g_status op2g_kernel_create(const char *user_src, const char *kernel_name,
     k->sig = S;
     k->source = generate_source(S);
     k->param_bytes = 8 * (5 + (S.nptrs > 0 ? S.nptrs : 1) + (nmaps > 0 ? nmaps : 1));
+    for (int r : staged_args(S))
+        if (r >= 0) k->staged = true;
+    if (k->staged) k->param_bytes += 8 * (1 + 4 * (nmaps > 0 ? nmaps : 1));
     op2g_status st = OP2G_OK;
     k->arch = (arch && *arch) ? std::string(arch) : current_arch(&st);
     if (st != OP2G_OK) {
@@ -433,6 +445,29 @@ op2g_status op2g_kernel_pack_params(const op2g_kernel *k, const op2g_launch_desc
     const int np = S.nptrs > 0 ? S.nptrs : 1;
     for (size_t m = 0; m < S.maps.size(); ++m)
         w[5 + np + m] = d->map_toset ? d->map_toset[m] : INT64_MAX;
+    if (k->staged) {
+        // sblock, smax[nm], sind[nm], soff[nm], sloc[nm]
+        const op2g_stage_desc *g = d->stage;
+        if (!g || g->block <= 0) return fail(OP2G_ERR_INVALID, "staged wrapper launched without a plan");
+        const int nm = S.maps.empty() ? 1 : (int)S.maps.size();
+        int64_t *x = w + 5 + np + nm;
+        x[0] = g->block;
+        std::vector<int> st = staged_args(S);
+        for (size_t a = 0; a < st.size(); ++a) {
+            const int m = st[a];
+            if (m < 0) continue;
+            if (!g->ind_map[m] || !g->ind_off[m] || !g->loc_map[m] || g->max_unique[m] < 0)
+                return fail(OP2G_ERR_INVALID, "staging plan lacks map " + std::to_string(m));
+            if ((uintptr_t)g->loc_map[m] % 8)
+                return fail(OP2G_ERR_INVALID, "loc_map array is not 8-byte aligned");
+        }
+        for (int m = 0; m < (int)S.maps.size(); ++m) {
+            x[1 + m] = g->max_unique[m];
+            x[1 + nm + m] = (int64_t)(intptr_t)g->ind_map[m];
+            x[1 + 2 * nm + m] = (int64_t)(intptr_t)g->ind_off[m];
+            x[1 + 3 * nm + m] = (int64_t)(intptr_t)g->loc_map[m];
+        }
+    }
     // Every slot the generated code dereferences must be non-NULL.
     for (const ArgInfo &A : S.args) {
         int nslots = A.d.kind == OP2G_ARG_MAT ? 3 : 1;
@@ -472,6 +507,42 @@ op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *
     st = load_module(k->cubin, "op2g_wrap", "op2g_wrap_batched", k->sig.block_size, k->per_dev,
                      k->mu, &L);
     if (st != OP2G_OK) return st;
+    if (k->staged) {
+        if (d->end <= d->start) return OP2G_OK;
+        // one CTA per mini-partition, up to 4 waves of resident CTAs (CTAs
+        // then take partitions in turn); the partitions' target lists and
+        // staged values take dynamic shared memory
+        const size_t smem = staged_smem_bytes(k->sig, d->stage->max_unique);
+        Driver &D = driver();
+        {
+            std::lock_guard<std::mutex> g(k->mu);
+            if ((int)smem > L->smem_attr && smem > 48 * 1024) {
+                CUresult r = D.FuncSetAttribute(L->f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                                                (int)smem);
+                if (r != CUDA_SUCCESS) return cu_fail(r, "cuFuncSetAttribute (shared memory)");
+                L->smem_attr = (int)smem;
+            }
+            if (smem != L->occ_smem) {
+                int occ = 0;
+                if (D.OccupancyMaxActiveBlocksPerMultiprocessor(&occ, L->f, k->sig.block_size, smem) !=
+                    CUDA_SUCCESS)
+                    occ = 1;
+                if (occ < 1)
+                    return fail(OP2G_ERR_CAPACITY, "staged partitions need " + std::to_string(smem) +
+                                                       " bytes of shared memory per CTA");
+                L->occ_smem = smem;
+                L->occ_at_smem = occ;
+            }
+        }
+        const int64_t B = d->stage->block;
+        const int64_t nparts = (d->end + B - 1) / B - d->start / B;
+        int64_t grid = d->grid > 0 ? d->grid : (int64_t)L->occ_at_smem * L->sms * 4;
+        if (grid > nparts) grid = nparts;
+        if (grid < 1) grid = 1;
+        void *params[] = {buf};
+        return launch(L->f, (unsigned)grid, (unsigned)k->sig.block_size, params, stream,
+                      (unsigned)smem);
+    }
     const int64_t per = d->layers_per_entity > 0 ? d->layers_per_entity : 1;
     const int64_t items = (d->end - d->start) * (k->sig.loop.extruded && k->sig.loop.constant_layers &&
                                                  column_parallel(k->sig) ? per : 1);

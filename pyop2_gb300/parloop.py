@@ -454,6 +454,7 @@ class Parloop:
         self.pass_layer_arg = bool(pass_layer_arg)
         self._built = None
         self._plan = None
+        self._stage = None
         self._flatten()
 
     def _flatten(self):
@@ -504,6 +505,7 @@ class Parloop:
         self._flatten()
         self._launch_cache = None
         self._plan = None
+        self._stage = None
         if self.cache_key() != old_key:
             self._built = None
 
@@ -575,6 +577,8 @@ class Parloop:
         if mode == "auto" or configuration["autotune"]:
             from pyop2_gb300 import autotune
             return autotune.choose(self)
+        if mode == "staged" and self._stageable():
+            return _lib.SCATTER_STAGED, bs, pf, grid
         if not self._needs_conflict_handling():
             return _lib.SCATTER_ATOMIC, bs, pf, grid
         if mode == "warp":
@@ -587,6 +591,35 @@ class Parloop:
         if mode == "shared" and not self.iterset._extruded:
             return _lib.SCATTER_SHARED, bs, pf, grid
         return _lib.SCATTER_ATOMIC, bs, pf, grid
+
+    def _stage_roots(self):
+        """Plain maps (in first-seen order) whose staging plans a staged
+        wrapper of this loop may read: those of Dat arguments (not parts of a
+        mixed argument) through a plain or permuted map, READ or INC."""
+        roots, seen = [], set()
+        for a, group, _ in self._flat:
+            if not isinstance(a, DatLegacyArg) or a.map_ is None or group:
+                continue
+            if a.access not in (Access.READ, Access.INC):
+                continue
+            m = a.map_
+            if isinstance(m, PermutedMap):
+                m = m.map_
+            if isinstance(m, (ComposedMap, MixedMap)) or not isinstance(m, Map):
+                continue
+            if m._serial not in seen:
+                seen.add(m._serial)
+                roots.append(m)
+        return roots
+
+    def _stageable(self):
+        """True when a staged wrapper applies: a non-extruded loop over a
+        whole set with at least one Dat argument it can stage, whose staged
+        values fit in shared memory."""
+        it = self.iterset
+        if it._extruded or isinstance(it, Subset) or not self._stage_roots():
+            return False
+        return stage_plan(self) is not None
 
     def _colourable(self):
         if self.iterset._extruded or isinstance(self.iterset, Subset):
@@ -621,9 +654,12 @@ class Parloop:
                               table.key())
         device.require()
         _lib.call("op2g_kernel_prepare", k.handle)   # module loaded outside any capture
+        if scatter == _lib.SCATTER_STAGED and stage_plan(self) is None:
+            raise ValueError("staged execution does not apply to this loop")
         self._built = (scatter, block_size, k, table, argdescs)
         self._launch_cache = None
         self._plan = None
+        self._stage = None
         return k
 
     # ---- execution
@@ -720,6 +756,10 @@ class Parloop:
         D.grid = getattr(self, "_grid", 0)
         D.indices = it._indices_mirror.dev().data_ptr() if isinstance(it, Subset) else None
         D.start, D.end = 0, it.size
+        if scatter == _lib.SCATTER_STAGED:
+            if self._stage is None:
+                self._stage = stage_plan(self)
+            D.stage = ctypes.pointer(self._stage.desc(table))
         self._keep = (P, toset)
         self._launch_cache = (ptrs, dbg, D)
         return D
@@ -767,7 +807,7 @@ class Parloop:
     def _prepare_capture(self):
         """Everything a launch does besides launching: build, upload, load the
         module, colour (none of it may happen inside a stream capture)."""
-        self.launch_desc()
+        self.launch_desc()          # also builds a staging plan
         _lib.call("op2g_kernel_prepare", self._built[2].handle)
         if self._built[0] == _lib.SCATTER_PLAIN:
             colour_plan(self)
@@ -898,6 +938,106 @@ def colour_plan(loop, max_colours=256):
     plan = ColourPlan(order, ptr, nc.value, colour)
     it._cache[key] = plan
     return plan
+
+
+# ---------------------------------------------------------- staging plans
+class MapStagePlan:
+    """The staging plan of one map: partitions of ``block`` iterations; per
+    partition the sorted distinct targets (``ind_map[ind_off[p]:ind_off[p+1]]``)
+    and per map entry its local index (``loc_map``, uint16, 0xFFFF for a
+    negative entry) -- the local renumbering of the historical OP2 execution
+    plan (doc/sphinx/source/plan.rst:21-39), built on the device."""
+
+    def __init__(self, m, block):
+        n, ar = m.iterset.total_size, m.arity
+        dev = device.device()
+        nb = (n + block - 1) // block
+        st = device.stream_handle()
+        vals = m._device_values()
+        ws = ctypes.c_size_t()
+        _lib.call("op2g_stage_plan_workspace", n, ar, block, ctypes.byref(ws))
+        work = device.empty_bytes(ws.value)
+        self.ind_off = torch.empty(nb + 1, dtype=torch.int64, device=dev)
+        total = ctypes.c_int64()
+        mx = ctypes.c_int32()
+        _lib.call("op2g_stage_plan_count", n, ar, vals.data_ptr(), block, work.data_ptr(),
+                  ws.value, self.ind_off.data_ptr(), ctypes.byref(total), ctypes.byref(mx), st)
+        self.ind_map = torch.empty(max(total.value, 1), dtype=torch.int32, device=dev)
+        self.loc_map = torch.empty(max(n * ar, 4), dtype=torch.int16, device=dev)
+        _lib.call("op2g_stage_plan_fill", n, ar, vals.data_ptr(), block,
+                  self.ind_off.data_ptr(), self.ind_map.data_ptr(), self.loc_map.data_ptr(), st)
+        self.block = block
+        self.max_unique = mx.value
+        self.total = total.value
+        self.nblocks = nb
+
+
+class StagePlan:
+    """The staging plans of a loop's maps, all with one partition size."""
+
+    def __init__(self, plans, block):
+        self.plans = plans          # map serial -> MapStagePlan
+        self.block = block
+        self._descs = {}
+
+    def desc(self, table):
+        """op2g_stage_desc for the loop's map table (entries in table order)."""
+        key = tuple(id(o) for o in table.objs)
+        d = self._descs.get(key)
+        if d is None:
+            d = _lib.StageDesc()
+            d.block = self.block
+            for i, obj in enumerate(table.objs):
+                mp = self.plans.get(obj._serial) if obj is not None else None
+                if mp is None:
+                    continue
+                d.ind_map[i] = mp.ind_map.data_ptr()
+                d.ind_off[i] = mp.ind_off.data_ptr()
+                d.loc_map[i] = mp.loc_map.data_ptr()
+                d.max_unique[i] = mp.max_unique
+            self._descs[key] = d
+        return d
+
+
+_STAGE_SMEM_LIMIT = 200 * 1024
+
+
+def stage_plan(loop):
+    """Staging plan of a loop's stageable maps (cached on each map per
+    partition size), or None when its staged values would not fit in shared
+    memory.  The partition size is configuration["stage_cells"], capped at
+    4096 map entries per partition and rounded down to a multiple of 32."""
+    roots = loop._stage_roots()
+    if not roots:
+        return None
+    arity = max(m.arity for m in roots)
+    block = min(int(configuration["stage_cells"]), 4096 // arity)
+    block = max(32, block - block % 32)
+    if 4096 // arity < 32:
+        return None
+    plans = {}
+    for m in roots:
+        key = ("stage", block)
+        mp = m._cache.get(key)
+        if mp is None:
+            mp = MapStagePlan(m, block)
+            m._cache[key] = mp
+        plans[m._serial] = mp
+    # shared memory of the staged wrapper: each staged map's target list and
+    # each staged argument's values at the largest partition
+    smem = 0
+    for m in roots:
+        smem += (plans[m._serial].max_unique * 4 + 15) // 16 * 16
+    for a, group, _ in loop._flat:
+        if isinstance(a, DatLegacyArg) and a.map_ is not None and not group and \
+                a.access in (Access.READ, Access.INC):
+            m = a.map_.map_ if isinstance(a.map_, PermutedMap) else a.map_
+            if m._serial in plans:
+                smem += (plans[m._serial].max_unique * a.data.cdim * a.data.dtype.itemsize
+                         + 15) // 16 * 16
+    if smem > _STAGE_SMEM_LIMIT:
+        return None
+    return StagePlan(plans, block)
 
 
 # ------------------------------------------------------------ entry points

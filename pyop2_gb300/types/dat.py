@@ -216,6 +216,21 @@ class Dat(AbstractDat):
         device.require()
         return d
 
+    def _rebind(self, tensor):
+        """Make ``tensor`` (CUDA, contiguous, same element count and dtype)
+        this Dat's device storage, without copying: a loop built on this Dat
+        then runs on the tensor (it re-reads the pointer at launch)."""
+        import torch
+        if not tensor.is_cuda or not tensor.is_contiguous():
+            raise ValueError("_rebind needs a contiguous CUDA tensor")
+        if tensor.numel() != int(np.prod(self._shape)) or \
+                tensor.element_size() != self._dtype.itemsize:
+            raise ValueError("tensor does not match the Dat's shape and dtype")
+        self._m._dev = tensor.view(-1).view(torch.uint8)
+        self._m._host = None
+        self._m.state = "device"
+        self.increment_dat_version()
+
     # ---- operations
     def zero(self, subset=None):
         self.increment_dat_version()

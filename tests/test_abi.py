@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib):
     L = lib.lib()
     for name in declared_functions():
         assert hasattr(L, name), name
-    assert L.op2g_abi_version() == 3
+    assert L.op2g_abi_version() == lib.ABI_VERSION == 4
     assert L.op2g_last_error() is not None
 
 
@@ -48,7 +48,8 @@ STRUCTS = {
                                     "block_size", "debug_checks", "batched", "prefetch",
                                     "nc_reads"]),
     "op2g_launch_desc": ("LaunchDesc", ["start", "end", "layers", "indices", "err", "ptrs",
-                                        "map_toset", "layers_per_entity", "grid"]),
+                                        "map_toset", "layers_per_entity", "grid", "stage"]),
+    "op2g_stage_desc": ("StageDesc", ["block", "ind_map", "ind_off", "loc_map", "max_unique"]),
     "op2g_sparsity_pair": ("SparsityPair", ["rmap", "cmap", "rarity", "carity", "nent", "region",
                                             "nrcomposed", "nccomposed", "rcomposed", "ccomposed",
                                             "roffset", "coffset", "roffset_quotient",

@@ -24,7 +24,8 @@ def compile_loop(pl, scatter=_lib.SCATTER_ATOMIC, bs=256):
                              table.key(), arch="sm_103a")
 
 
-@pytest.mark.parametrize("scatter", [_lib.SCATTER_ATOMIC, _lib.SCATTER_WARP, _lib.SCATTER_PLAIN])
+@pytest.mark.parametrize("scatter", [_lib.SCATTER_ATOMIC, _lib.SCATTER_WARP, _lib.SCATTER_PLAIN,
+                                     _lib.SCATTER_STAGED])
 @pytest.mark.parametrize("dtype,ctype", [(np.float64, "double"), (np.float32, "float"),
                                          (np.int32, "int"), (np.uint32, "unsigned int"),
                                          (np.int64, "long long")])
@@ -45,6 +46,30 @@ def test_all_access_modes(op2, scatter, dtype, ctype):
     assert "op2g_wrap" in s and "op2g_wrap_batched" in s
     if scatter == _lib.SCATTER_WARP:
         assert "warp_agg_inc" in s
+    if scatter == _lib.SCATTER_STAGED:
+        # READ (no written Dat is read) and INC are staged, nothing else
+        assert "op2g_run_staged" in s and "sv0[" in s and "sv3[" in s
+        assert not any("sv%d[" % a in s for a in (1, 2, 4, 5, 6))
+        assert "op2g_wrap_chunked" not in s
+
+
+def test_staged_wrapper_stages_reads_and_incs(op2):
+    """A staged gather/scatter loop through a plain and a permuted map: READ
+    and INC values come from and go to shared memory at local indices."""
+    cells, verts = op2.Set(8), op2.Set(10)
+    m = op2.Map(cells, verts, 4, np.arange(32) % 10)
+    pm = op2.PermutedMap(m, [1, 0, 3, 2])
+    x = op2.Dat(verts ** 3, dtype=np.float64)
+    y = op2.Dat(verts, dtype=np.float64)
+    z = op2.Dat(verts, dtype=np.float32)
+    w = op2.Dat(cells, dtype=np.float64)
+    k = op2.Kernel("static void k(double *y, const double *x, float *z, const double *w) {}", "k")
+    pl = LegacyParloop(k, cells, y(op2.INC, m), x(op2.READ, pm), z(op2.INC, pm), w(op2.READ))
+    s = compile_loop(pl, _lib.SCATTER_STAGED).source()
+    assert "op2g_run_staged" in s
+    for a in (0, 1, 2):
+        assert "sv%d[" % a in s
+    assert "op2g_perm1" in s and "lv0[" in s and "ushort4" in s
 
 
 @pytest.mark.parametrize("region", [1, 2, 3, 4])

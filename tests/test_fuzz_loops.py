@@ -13,7 +13,7 @@ import fuzz_loops as F
 
 CPU_SEEDS = range(48)
 GPU_SEEDS = range(48)
-STRATEGIES = ["atomic", "warp", "colour", "shared"]
+STRATEGIES = ["atomic", "warp", "colour", "shared", "staged"]
 
 
 def _equal(got, want):

@@ -8,7 +8,7 @@ from pyop2_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
 
-STRATEGIES = ["atomic", "warp", "colour", "shared"]
+STRATEGIES = ["atomic", "warp", "colour", "shared", "staged"]
 
 
 @pytest.fixture(params=STRATEGIES)

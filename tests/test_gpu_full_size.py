@@ -30,14 +30,29 @@ def rel(a, b):
     return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
 
 
+@pytest.fixture(scope="module")
+def c2a_oracle(oracle_op2):
+    out = {}
+    for permute in (False, True):
+        o = W.build_p1_3d(oracle_op2, n=128, permute=permute, seed=0)
+        o["run"]()
+        out[permute] = o["y"].data.copy()
+    return out
+
+
+@pytest.mark.parametrize("scatter", ["atomic", "staged"])
 @pytest.mark.parametrize("permute", [False, True])
-def test_config2a_full_size_vs_oracle(gpu_op2, oracle_op2, permute):
+def test_config2a_full_size_vs_oracle(gpu_op2, c2a_oracle, permute, scatter):
+    from pyop2_gb300.configuration import configuration
     g = W.build_p1_3d(gpu_op2, n=128, permute=permute, seed=0)
-    o = W.build_p1_3d(oracle_op2, n=128, permute=permute, seed=0)
     assert g["cells"].size == 12582912 and g["verts"].size == 2146689
-    g["run"]()
-    o["run"]()
-    assert rel(g["y"].data_ro, o["y"].data) <= 1e-12
+    old = configuration["scatter"]
+    configuration["scatter"] = scatter
+    try:
+        g["run"]()
+    finally:
+        configuration["scatter"] = old
+    assert rel(g["y"].data_ro, c2a_oracle[permute]) <= 1e-12
 
 
 def _pattern(op2, p):

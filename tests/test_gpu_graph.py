@@ -7,7 +7,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-STRATEGIES = ["atomic", "warp", "colour", "shared"]
+STRATEGIES = ["atomic", "warp", "colour", "shared", "staged"]
 
 
 def _problem(op2, seed):

@@ -7,7 +7,7 @@ import scenarios as S
 
 pytestmark = pytest.mark.gpu
 
-STRATEGIES = ["atomic", "warp", "colour", "shared"]
+STRATEGIES = ["atomic", "warp", "colour", "shared", "staged"]
 
 
 @pytest.fixture(params=STRATEGIES)

@@ -11,7 +11,7 @@ from test_oracle_golden import ALL_SIMPLE, SIZED, UNSIZED
 
 pytestmark = pytest.mark.gpu
 
-STRATEGIES = ["atomic", "warp", "colour", "shared"]
+STRATEGIES = ["atomic", "warp", "colour", "shared", "staged"]
 
 
 @pytest.fixture(params=STRATEGIES)

@@ -173,7 +173,7 @@ class TestDatViewInLoops:
         mask[1, 2] = False
         assert np.array_equal(full[:, mask], ref[:, mask])
 
-    @pytest.mark.parametrize("scatter", ["atomic", "warp", "colour", "shared"])
+    @pytest.mark.parametrize("scatter", ["atomic", "warp", "colour", "shared", "staged"])
     def test_indirect_view_inc_and_read(self, gpu_op2, scatter):
         from pyop2_gb300.configuration import configuration
         old = configuration["scatter"]
