@@ -97,11 +97,12 @@ enum {
                                   target once with a global atomic (non-extruded loops;
                                   atomics elsewhere)                                    */
     OP2G_SCATTER_STAGED = 4    /* the loop runs on a staging plan (op2g_stage_plan_*):
-                                  per mini-partition, the data of READ and INC Dat
-                                  arguments through plain or permuted maps are staged in
-                                  shared memory at the partition's distinct targets, INC
-                                  contributions are summed there, and each distinct
-                                  target receives one global atomic per partition
+                                  per mini-partition, the data of READ Dat arguments
+                                  through plain or permuted maps are staged in shared
+                                  memory once per distinct target, INC contributions
+                                  are stored at their entries' slots there, summed per
+                                  target in slot order, and each distinct target
+                                  receives one global atomic per partition
                                   (non-extruded, non-indexed loops; the launch passes the
                                   plan in op2g_launch_desc.stage)                        */
 };
@@ -202,18 +203,23 @@ int32_t op2g_kernel_num_regs(const op2g_kernel *k);
 
 /* The staging plan of a launch of a wrapper built with OP2G_SCATTER_STAGED:
  * the iteration range is cut into mini-partitions of `block` iterations
- * (partition p = [p * block, (p + 1) * block)); for every map of the map table
- * that the plan covers (entry m; a permuted map uses its base map's entry),
- * ind_map[m] + ind_off[m][p] .. ind_off[m][p + 1] lists the distinct targets
- * of partition p in ascending order and loc_map[m][i * arity + j] is the
- * position of entry (i, j) in its partition's list (0xFFFF for a negative
- * entry).  Built by op2g_stage_plan_count / _fill; all arrays on the device. */
+ * (partition p = [p * block, (p + 1) * block)).  For every map of the map
+ * table that the plan covers (entry m; a permuted map uses its base map's
+ * entry), partition p's segment starts at ind_off[m][p] (a multiple of 8)
+ * and holds ind_num[m][p] distinct targets in ascending order
+ * (ind_map[m] + ind_off[m][p] ...) with the first slot of each in
+ * run_off[m] + ind_off[m][p] (followed by the partition's count of valid
+ * entries); loc_map[m][i * arity + j] is entry (i, j)'s slot: its rank in the
+ * partition's entries sorted by (target, position), 0xFFFF for a negative
+ * entry.  Built by op2g_stage_plan_count / _fill; all arrays on the device. */
 typedef struct op2g_stage_desc {
     int64_t block;
     const int32_t *ind_map[OP2G_MAX_MAPS];
     const int64_t *ind_off[OP2G_MAX_MAPS];
+    const int32_t *ind_num[OP2G_MAX_MAPS];
+    const uint16_t *run_off[OP2G_MAX_MAPS];
     const uint16_t *loc_map[OP2G_MAX_MAPS];
-    int32_t max_unique[OP2G_MAX_MAPS];  /* largest distinct count of a partition; 0 = no plan */
+    int32_t max_unique[OP2G_MAX_MAPS];  /* largest distinct count of a partition */
 } op2g_stage_desc;
 
 typedef struct op2g_launch_desc {
@@ -323,19 +329,23 @@ op2g_status op2g_sparsity_fill(const op2g_sparsity_desc *d, void *workspace, siz
 /* The staging plan of one map over n iterations in partitions of `block`
  * iterations (block * arity <= 4096): the local renumbering of the
  * historical OP2 execution plan, doc/sphinx/source/plan.rst:21-39 (no code
- * counterpart in this checkout).  `map` is the device int32 [n, arity]
- * array.  op2g_stage_plan_count writes ind_off[nblocks + 1] (device int64,
- * exclusive prefix sums of the per-partition distinct counts) and returns the
- * total and the largest count (synchronises `stream`); op2g_stage_plan_fill
- * then writes ind_map[total] and loc_map[n * arity] (device).  workspace:
+ * counterpart in this checkout), with one slot per map entry in place of that
+ * plan's thread colouring.  `map` is the device int32 [n, arity] array.
+ * op2g_stage_plan_count writes ind_off[nblocks + 1] (device int64, exclusive
+ * prefix sums of the segment lengths: distinct count + 1 rounded up to 8) and
+ * ind_num[nblocks] (device int32, distinct counts), and returns the total
+ * segment length and the largest distinct count (synchronises `stream`);
+ * op2g_stage_plan_fill then writes ind_map[total] (int32), run_off[total]
+ * (uint16) and loc_map[n * arity] (uint16), all device arrays.  workspace:
  * op2g_stage_plan_workspace bytes of device memory. */
 op2g_status op2g_stage_plan_workspace(int64_t n, int32_t arity, int64_t block, size_t *bytes);
 op2g_status op2g_stage_plan_count(int64_t n, int32_t arity, const int32_t *map, int64_t block,
                                   void *workspace, size_t ws_bytes, int64_t *ind_off,
-                                  int64_t *total, int32_t *max_unique, void *stream);
+                                  int32_t *ind_num, int64_t *total, int32_t *max_unique,
+                                  void *stream);
 op2g_status op2g_stage_plan_fill(int64_t n, int32_t arity, const int32_t *map, int64_t block,
-                                 const int64_t *ind_off, int32_t *ind_map, uint16_t *loc_map,
-                                 void *stream);
+                                 const int64_t *ind_off, int32_t *ind_map, uint16_t *run_off,
+                                 uint16_t *loc_map, void *stream);
 
 /* ----------------------------------------------------------- matrices */
 /* Block-CSR matrix with rdim x cdim row-major blocks (rdim = cdim = 1 is CSR). */

@@ -53,6 +53,7 @@ class LoopDesc(ctypes.Structure):
 
 class StageDesc(ctypes.Structure):
     _fields_ = [("block", _i64), ("ind_map", _p * MAX_MAPS), ("ind_off", _p * MAX_MAPS),
+                ("ind_num", _p * MAX_MAPS), ("run_off", _p * MAX_MAPS),
                 ("loc_map", _p * MAX_MAPS), ("max_unique", _i32 * MAX_MAPS)]
 
 
@@ -120,9 +121,9 @@ SIGNATURES = {
                                    _i32, _p, _p, _p, _pi32, _p]),
     "op2g_probe_fp64_peak": (_i32, [ctypes.POINTER(ctypes.c_double), _p]),
     "op2g_stage_plan_workspace": (_i32, [_i64, _i32, _i64, ctypes.POINTER(ctypes.c_size_t)]),
-    "op2g_stage_plan_count": (_i32, [_i64, _i32, _p, _i64, _p, ctypes.c_size_t, _p,
+    "op2g_stage_plan_count": (_i32, [_i64, _i32, _p, _i64, _p, ctypes.c_size_t, _p, _p,
                                      ctypes.POINTER(_i64), _pi32, _p]),
-    "op2g_stage_plan_fill": (_i32, [_i64, _i32, _p, _i64, _p, _p, _p, _p]),
+    "op2g_stage_plan_fill": (_i32, [_i64, _i32, _p, _i64, _p, _p, _p, _p, _p]),
 }
 
 _lib = None

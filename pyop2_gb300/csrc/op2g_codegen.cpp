@@ -133,23 +133,31 @@ static size_t elt_size(int dt) {
     }
 }
 
-// Bytes of dynamic shared memory a staged wrapper takes for partitions whose
-// largest distinct-target counts are max_unique[m] (the layout the generated
-// code computes: per staged map its target list, per staged argument its
-// values, each region rounded up to 16 bytes).
-size_t staged_smem_bytes(const Signature &S, const int32_t *max_unique) {
+// Bytes of dynamic shared memory a staged wrapper takes for partitions of
+// `block` iterations whose largest distinct-target counts are max_unique[m]
+// (the layout the generated code computes, each region rounded up to 16
+// bytes): per staged map its target list (int), run offsets and per-slot
+// target table (uint16); per staged READ argument its values per target;
+// per staged INC argument its contributions per slot.
+size_t staged_smem_bytes(const Signature &S, int64_t block, const int32_t *max_unique) {
     std::vector<int> st = staged_args(S);
     auto r16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
     size_t bytes = 0;
     std::vector<bool> seen(S.maps.size(), false);
     for (size_t a = 0; a < st.size(); ++a)
         if (st[a] >= 0 && !seen[st[a]]) {
-            seen[st[a]] = true;
-            bytes += r16((size_t)max_unique[st[a]] * 4);
+            const int m = st[a];
+            seen[m] = true;
+            const size_t mu = (size_t)max_unique[m];
+            bytes += r16(mu * 4) + r16((mu + 1) * 2) + r16((size_t)block * S.maps[m].arity * 2);
         }
-    for (size_t a = 0; a < st.size(); ++a)
-        if (st[a] >= 0)
-            bytes += r16((size_t)max_unique[st[a]] * S.args[a].d.dim * elt_size(S.args[a].d.dtype));
+    for (size_t a = 0; a < st.size(); ++a) {
+        if (st[a] < 0) continue;
+        const op2g_arg_desc &d = S.args[a].d;
+        const size_t rows = d.access == OP2G_READ ? (size_t)max_unique[st[a]]
+                                                  : (size_t)block * S.maps[st[a]].arity;
+        bytes += r16(rows * d.dim * elt_size(d.dtype));
+    }
     return bytes;
 }
 
@@ -435,9 +443,10 @@ struct Gen {
         }
     }
 
-    // Staged row of plain map m at entity n: local indices lv<m> from the
-    // plan's loc_map (16-bit, read as vectors when the arity allows) and the
-    // global targets mv<m> from the partition's target list in shared memory.
+    // Staged row of plain map m at entity n: the entries' slots lv<m> from
+    // the plan's loc_map (16-bit, read as vectors when the arity allows) and
+    // the global targets mv<m> through the partition's slot -> target table
+    // and target list in shared memory.
     void emit_staged_row(int m, const std::string &ind) {
         const int ar = S.maps[m].arity;
         const std::string lv = "lv" + std::to_string(m), mv = base_row(m);
@@ -459,12 +468,12 @@ struct Gen {
         }
         o << ind << "#pragma unroll\n";
         o << ind << "  for (int i = 0; i < " << ar << "; ++i) " << mv << "[i] = " << lv
-          << "[i] == 0xFFFF ? -1 : si" << m << "[" << lv << "[i]];\n";
+          << "[i] == 0xFFFF ? -1 : si" << m << "[tg" << m << "[" << lv << "[i]]];\n";
         o << ind << "}\n";
     }
 
-    // Local index (in its partition's target list) of entry `i` of staged
-    // argument a's map: the plain map's own entry, or the permuted one.
+    // Slot of entry `i` of staged argument a's map (the plain map's own
+    // entry, or the permuted one); 0xFFFF for a negative entry.
     std::string local_index(size_t a, const std::string &i) const {
         const int m = S.args[a].d.map;
         const int r = st_arg[a];
@@ -472,11 +481,13 @@ struct Gen {
         return "(int)lv" + std::to_string(r) + "[op2g_perm" + std::to_string(m) + "[" + i + "]]";
     }
 
-    // The staged run function: CTAs take mini-partitions of the plan in turn;
-    // per partition the target lists of the staged maps and the values of
-    // staged READ arguments are loaded into shared memory (each distinct
-    // target once), staged INC arguments are summed there, and every
-    // distinct target gets one global atomic when the partition is done.
+    // The staged run function: CTAs take mini-partitions of the plan in turn.
+    // Per partition: the target lists and run offsets of the staged maps and
+    // the values of staged READ arguments (each distinct target once) are
+    // loaded into shared memory, and a slot -> target table is filled; the
+    // partition's iterations run with READ packs from shared memory and INC
+    // contributions stored at their slots; then each target's run of slots is
+    // summed in slot order and added to the target with one global atomic.
     void emit_staged_run() {
         std::ostringstream &O = o;
         const int BS = S.block_size;
@@ -487,15 +498,24 @@ struct Gen {
         O << "  size_t so_ = 0;\n";
         for (size_t m = 0; m < S.maps.size(); ++m)
             if (st_map[m]) {
+                const int ar = S.maps[m].arity;
                 O << "  int *si" << m << " = (int *)(op2g_smem + so_); so_ += ((size_t)p.smax[" << m
                   << "] * 4 + 15) & ~(size_t)15;\n";
+                O << "  unsigned short *ro" << m << " = (unsigned short *)(op2g_smem + so_); so_ += "
+                  << "((size_t)(p.smax[" << m << "] + 1) * 2 + 15) & ~(size_t)15;\n";
+                O << "  unsigned short *tg" << m << " = (unsigned short *)(op2g_smem + so_); so_ += "
+                  << "((size_t)p.sblock * " << ar << " * 2 + 15) & ~(size_t)15;\n";
             }
         for (size_t a = 0; a < S.args.size(); ++a)
             if (st_arg[a] >= 0) {
-                const char *T = ctype_of(S.args[a].d.dtype);
-                O << "  " << T << " *sv" << a << " = (" << T << " *)(op2g_smem + so_); so_ += ((size_t)p.smax["
-                  << st_arg[a] << "] * " << S.args[a].d.dim << " * sizeof(" << T
-                  << ") + 15) & ~(size_t)15;\n";
+                const op2g_arg_desc &d = S.args[a].d;
+                const char *T = ctype_of(d.dtype);
+                const std::string rows = d.access == OP2G_READ
+                                             ? "(size_t)p.smax[" + std::to_string(st_arg[a]) + "]"
+                                             : "(size_t)p.sblock * " +
+                                                   std::to_string(S.maps[st_arg[a]].arity);
+                O << "  " << T << " *sv" << a << " = (" << T << " *)(op2g_smem + so_); so_ += ("
+                  << rows << " * " << d.dim << " * sizeof(" << T << ") + 15) & ~(size_t)15;\n";
             }
         O << "  const long long pb0_ = p.start / p.sblock, pb1_ = (p.end + p.sblock - 1) / p.sblock;\n";
         O << "  for (long long pb_ = pb0_ + blockIdx.x; pb_ < pb1_; pb_ += gridDim.x) {\n";
@@ -504,26 +524,39 @@ struct Gen {
         for (size_t m = 0; m < S.maps.size(); ++m)
             if (st_map[m]) {
                 O << "    const long long so" << m << "_ = p.soff[" << m << "][pb_];\n";
-                O << "    const int nu" << m << "_ = (int)(p.soff[" << m << "][pb_ + 1] - so" << m << "_);\n";
-                O << "    for (int k_ = threadIdx.x; k_ < nu" << m << "_; k_ += " << BS << ") si" << m
-                  << "[k_] = __ldg(p.sind[" << m << "] + so" << m << "_ + k_);\n";
+                O << "    const int nu" << m << "_ = p.snum[" << m << "][pb_];\n";
+                O << "    for (int k_ = threadIdx.x; k_ <= nu" << m << "_; k_ += " << BS << ") {\n";
+                O << "      if (k_ < nu" << m << "_) si" << m << "[k_] = __ldg(p.sind[" << m << "] + so"
+                  << m << "_ + k_);\n";
+                O << "      ro" << m << "[k_] = __ldg(p.sruns[" << m << "] + so" << m << "_ + k_);\n";
+                O << "    }\n";
             }
         O << "    __syncthreads();\n";
+        for (size_t m = 0; m < S.maps.size(); ++m)
+            if (st_map[m]) {
+                O << "    for (int k_ = threadIdx.x; k_ < nu" << m << "_; k_ += " << BS << ")\n";
+                O << "      for (int s_ = ro" << m << "[k_]; s_ < ro" << m << "[k_ + 1]; ++s_) tg" << m
+                  << "[s_] = (unsigned short)k_;\n";
+            }
         for (size_t a = 0; a < S.args.size(); ++a) {
-            if (st_arg[a] < 0) continue;
+            if (st_arg[a] < 0 || S.args[a].d.access != OP2G_INC) continue;
+            // slots of entries outside [start, end) are never stored: they add 0
+            const int D = S.args[a].d.dim, r = st_arg[a];
+            O << "    for (int k_ = threadIdx.x; k_ < (int)ro" << r << "[nu" << r << "_] * " << D
+              << "; k_ += " << BS << ") sv" << a << "[k_] = (" << ctype_of(S.args[a].d.dtype)
+              << ")0;\n";
+        }
+        for (size_t a = 0; a < S.args.size(); ++a) {
+            if (st_arg[a] < 0 || S.args[a].d.access != OP2G_READ) continue;
             const op2g_arg_desc &d = S.args[a].d;
             const char *T = ctype_of(d.dtype);
             const int D = d.dim, r = st_arg[a];
             O << "    for (int k_ = threadIdx.x; k_ < nu" << r << "_ * " << D << "; k_ += " << BS
               << ") {\n";
-            if (d.access == OP2G_READ) {
-                O << "      const int v_ = k_ / " << D << ";\n";
-                O << "      sv" << a << "[k_] = __ldg((const " << T << " *)p.ptr[" << S.args[a].slot
-                  << "] + (long long)si" << r << "[v_] * " << gstride(a) << " + (k_ - v_ * " << D
-                  << "));\n";
-            } else {
-                O << "      sv" << a << "[k_] = (" << T << ")0;\n";
-            }
+            O << "      const int v_ = k_ / " << D << ";\n";
+            O << "      sv" << a << "[k_] = __ldg((const " << T << " *)p.ptr[" << S.args[a].slot
+              << "] + (long long)si" << r << "[v_] * " << gstride(a) << " + (k_ - v_ * " << D
+              << "));\n";
             O << "    }\n";
         }
         O << "    __syncthreads();\n";
@@ -539,9 +572,12 @@ struct Gen {
             const int D = d.dim, r = st_arg[a];
             O << "    for (int k_ = threadIdx.x; k_ < nu" << r << "_ * " << D << "; k_ += " << BS
               << ") {\n";
-            O << "      const int v_ = k_ / " << D << ";\n";
+            O << "      const int v_ = k_ / " << D << ", j_ = k_ - v_ * " << D << ";\n";
+            O << "      " << T << " s_ = (" << T << ")0;\n";
+            O << "      for (int q_ = ro" << r << "[v_]; q_ < ro" << r << "[v_ + 1]; ++q_) s_ += sv" << a
+              << "[q_ * " << D << " + j_];\n";
             O << "      op2g::atomic_inc((" << T << " *)p.ptr[" << S.args[a].slot << "] + (long long)si"
-              << r << "[v_] * " << gstride(a) << " + (k_ - v_ * " << D << "), sv" << a << "[k_]);\n";
+              << r << "[v_] * " << gstride(a) << " + j_, s_);\n";
             O << "    }\n";
         }
         O << "    __syncthreads();\n";
@@ -620,6 +656,8 @@ struct Gen {
               << "  long long smax[" << nm << "];\n"
               << "  const int *sind[" << nm << "];\n"
               << "  const long long *soff[" << nm << "];\n"
+              << "  const int *snum[" << nm << "];\n"
+              << "  const unsigned short *sruns[" << nm << "];\n"
               << "  const unsigned short *sloc[" << nm << "];\n";
         }
         O << "};\n";
@@ -936,13 +974,14 @@ struct Gen {
                           << T << ")0;\n";
                     }
                 } else if (staging && st_arg[a] >= 0) {
-                    // staged: the partition's values sit at the entry's local index
+                    // staged: the partition's values sit at the entry's target
                     O << J << "#pragma unroll\n";
                     O << J << "for (int i = 0; i < " << ar << "; ++i) {\n";
                     O << J << "  const int l_ = " << local_index(a, "i") << ";\n";
+                    O << J << "  const int q_ = l_ != 0xFFFF ? (int)tg" << st_arg[a] << "[l_] : -1;\n";
                     O << J << "#pragma unroll\n";
                     O << J << "  for (int j = 0; j < " << D << "; ++j) " << tn << "[" << po
-                      << "i * " << D << " + j] = l_ != 0xFFFF ? sv" << a << "[l_ * " << D
+                      << "i * " << D << " + j] = q_ >= 0 ? sv" << a << "[q_ * " << D
                       << " + j] : (" << T << ")0;\n";
                     O << J << "}\n";
                 } else {
@@ -1005,15 +1044,15 @@ struct Gen {
                     continue;  // scattered after the active block
                 }
                 if (staging && st_arg[a] >= 0) {
-                    // staged INC: summed in shared memory, flushed per partition
+                    // staged INC: each entry owns its slot (plain store); the
+                    // slots of one target are summed when the partition is done
                     O << J << "#pragma unroll\n";
                     O << J << "for (int i = 0; i < " << ar << "; ++i) {\n";
                     O << J << "  const int l_ = " << local_index(a, "i") << ";\n";
                     O << J << "  if (l_ == 0xFFFF) continue;\n";
                     O << J << "#pragma unroll\n";
-                    O << J << "  for (int j = 0; j < " << D << "; ++j) op2g::atomic_inc(&sv" << a
-                      << "[l_ * " << D << " + j], t" << first[a] << "[" << poff[a] << " + i * " << D
-                      << " + j]);\n";
+                    O << J << "  for (int j = 0; j < " << D << "; ++j) sv" << a << "[l_ * " << D
+                      << " + j] = t" << first[a] << "[" << poff[a] << " + i * " << D << " + j];\n";
                     O << J << "}\n";
                     continue;
                 }

@@ -373,7 +373,7 @@ op2g_status op2g_kernel_create(const char *user_src, const char *kernel_name,
     k->param_bytes = 8 * (5 + (S.nptrs > 0 ? S.nptrs : 1) + (nmaps > 0 ? nmaps : 1));
     for (int r : staged_args(S))
         if (r >= 0) k->staged = true;
-    if (k->staged) k->param_bytes += 8 * (1 + 4 * (nmaps > 0 ? nmaps : 1));
+    if (k->staged) k->param_bytes += 8 * (1 + 6 * (nmaps > 0 ? nmaps : 1));
     op2g_status st = OP2G_OK;
     k->arch = (arch && *arch) ? std::string(arch) : current_arch(&st);
     if (st != OP2G_OK) {
@@ -446,7 +446,7 @@ op2g_status op2g_kernel_pack_params(const op2g_kernel *k, const op2g_launch_desc
     for (size_t m = 0; m < S.maps.size(); ++m)
         w[5 + np + m] = d->map_toset ? d->map_toset[m] : INT64_MAX;
     if (k->staged) {
-        // sblock, smax[nm], sind[nm], soff[nm], sloc[nm]
+        // sblock, smax[nm], sind[nm], soff[nm], snum[nm], sruns[nm], sloc[nm]
         const op2g_stage_desc *g = d->stage;
         if (!g || g->block <= 0) return fail(OP2G_ERR_INVALID, "staged wrapper launched without a plan");
         const int nm = S.maps.empty() ? 1 : (int)S.maps.size();
@@ -456,8 +456,11 @@ op2g_status op2g_kernel_pack_params(const op2g_kernel *k, const op2g_launch_desc
         for (size_t a = 0; a < st.size(); ++a) {
             const int m = st[a];
             if (m < 0) continue;
-            if (!g->ind_map[m] || !g->ind_off[m] || !g->loc_map[m] || g->max_unique[m] < 0)
+            if (!g->ind_map[m] || !g->ind_off[m] || !g->ind_num[m] || !g->run_off[m] ||
+                !g->loc_map[m] || g->max_unique[m] < 0)
                 return fail(OP2G_ERR_INVALID, "staging plan lacks map " + std::to_string(m));
+            if (g->block * S.maps[m].arity > 65535)
+                return fail(OP2G_ERR_INVALID, "staging plan partitions are too large");
             if ((uintptr_t)g->loc_map[m] % 8)
                 return fail(OP2G_ERR_INVALID, "loc_map array is not 8-byte aligned");
         }
@@ -465,7 +468,9 @@ op2g_status op2g_kernel_pack_params(const op2g_kernel *k, const op2g_launch_desc
             x[1 + m] = g->max_unique[m];
             x[1 + nm + m] = (int64_t)(intptr_t)g->ind_map[m];
             x[1 + 2 * nm + m] = (int64_t)(intptr_t)g->ind_off[m];
-            x[1 + 3 * nm + m] = (int64_t)(intptr_t)g->loc_map[m];
+            x[1 + 3 * nm + m] = (int64_t)(intptr_t)g->ind_num[m];
+            x[1 + 4 * nm + m] = (int64_t)(intptr_t)g->run_off[m];
+            x[1 + 5 * nm + m] = (int64_t)(intptr_t)g->loc_map[m];
         }
     }
     // Every slot the generated code dereferences must be non-NULL.
@@ -512,7 +517,7 @@ op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *
         // one CTA per mini-partition, up to 4 waves of resident CTAs (CTAs
         // then take partitions in turn); the partitions' target lists and
         // staged values take dynamic shared memory
-        const size_t smem = staged_smem_bytes(k->sig, d->stage->max_unique);
+        const size_t smem = staged_smem_bytes(k->sig, d->stage->block, d->stage->max_unique);
         Driver &D = driver();
         {
             std::lock_guard<std::mutex> g(k->mu);

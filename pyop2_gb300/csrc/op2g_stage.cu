@@ -1,18 +1,24 @@
 // op2g_stage.cu -- the staging plan of a par_loop: mini-partitions of the
 // iteration set with, per partition and map, the sorted list of distinct
-// targets and the local (partition-relative) index of every map entry.
+// targets, and per map entry its slot in the partition's entries sorted by
+// target.
 //
 // This is the "local renumbering and staging" part of the execution plan of
 // the historical OP2 GPU backends (doc/sphinx/source/plan.rst:11-39; the
 // generated CUDA stub that used it is shown in
 // doc/sphinx/source/backends.rst:262-319): a partition's indirectly accessed
 // data are staged once into shared memory through the distinct-target list
-// (ind_map), and the kernel addresses them through the local map (loc_map).
-// Here both are built on the GPU, one CTA per partition: the partition's map
-// entries are sorted in shared memory as (value, position) keys, distinct
-// values get consecutive local indices, and every entry's local index is
-// written back at its position.  Entries with negative values (PyOP2's
-// "no target") get the local index 0xFFFF.
+// (ind_map).  Where that backend coloured the threads of a partition to add
+// INC contributions without conflicts, here every map entry owns one slot:
+// the entries of a partition sorted by (target, position) are numbered
+// 0 .. nvalid-1, the entries of one target form the run
+// run_off[k] .. run_off[k + 1], and loc_map holds each entry's slot.  A
+// kernel stores each contribution at its slot, then sums every run in slot
+// order and adds the sum to the target once.  The plan is built on the GPU,
+// one CTA per partition (a bitonic sort of (value, position) keys in shared
+// memory).  Entries with negative values (PyOP2's "no target") get the slot
+// 0xFFFF.  Each partition's segment of ind_map / run_off starts at a
+// multiple of 8 entries (16-byte aligned), so segments can be bulk-copied.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -36,17 +42,22 @@ __device__ __forceinline__ unsigned long long key_of(int v, int pos) {
     return ((unsigned long long)(unsigned)v << 32) | (unsigned)pos;
 }
 
-// One CTA per partition.  pass 0: count[b] = distinct non-negative values;
-// pass 1: ind_map[ind_off[b] + k] = k-th distinct value (ascending) and
-// loc_map[entry] = local index of the entry's value.
+// One CTA per partition.  pass 0: seg[b] = the partition's segment length
+// (distinct count + 1, rounded up to 8) and num[b] = the distinct count;
+// pass 1: the segment at ind_off[b] gets the distinct values (ind_map) and
+// the first slot of each (run_off, plus the number of valid entries after
+// the last), and loc_map[entry] = the entry's slot.
 __global__ void __launch_bounds__(PT) k_stage_plan(long long n, int arity, const int *__restrict__ map,
                                                    long long block, int pass,
-                                                   long long *__restrict__ count,
+                                                   long long *__restrict__ seg,
+                                                   int *__restrict__ num,
                                                    const long long *__restrict__ ind_off,
                                                    int *__restrict__ ind_map,
+                                                   unsigned short *__restrict__ run_off,
                                                    unsigned short *__restrict__ loc_map) {
     __shared__ unsigned long long key[PMAX];
     __shared__ int tsum[PT];
+    __shared__ int nvalid;
     const long long b = blockIdx.x;
     const long long c0 = b * block;
     const long long c1 = c0 + block < n ? c0 + block : n;
@@ -54,17 +65,25 @@ __global__ void __launch_bounds__(PT) k_stage_plan(long long n, int arity, const
     int np = 1;
     while (np < ne) np <<= 1;
     const int *src = map + c0 * arity;
+    if (threadIdx.x == 0) nvalid = 0;
+    __syncthreads();
+    int myvalid = 0;
     for (int i = threadIdx.x; i < np; i += PT) {
         unsigned long long k = ~0ull;
         if (i < ne) {
             const int v = src[i];
-            if (v >= 0) k = key_of(v, i);
-            else if (pass == 1) loc_map[c0 * arity + i] = NOLOC;
+            if (v >= 0) {
+                k = key_of(v, i);
+                ++myvalid;
+            } else if (pass == 1) {
+                loc_map[c0 * arity + i] = NOLOC;
+            }
         }
         key[i] = k;
     }
+    atomicAdd(&nvalid, myvalid);
     __syncthreads();
-    // bitonic sort of np keys, ascending
+    // bitonic sort of np keys, ascending (invalid keys last)
     for (int size = 2; size <= np; size <<= 1) {
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
             for (int t = threadIdx.x; t < np / 2; t += PT) {
@@ -97,30 +116,35 @@ __global__ void __launch_bounds__(PT) k_stage_plan(long long n, int arity, const
         tsum[threadIdx.x] += y;
         __syncthreads();
     }
+    const int nu = tsum[PT - 1];
     if (pass == 0) {
-        if (threadIdx.x == PT - 1) count[b] = tsum[PT - 1];
+        if (threadIdx.x == 0) {
+            seg[b] = (nu + 1 + 7) / 8 * 8;
+            num[b] = nu;
+        }
         return;
     }
     int local = (threadIdx.x ? tsum[threadIdx.x - 1] : 0) - 1;
     int *out = ind_map + ind_off[b];
+    unsigned short *ro = run_off + ind_off[b];
     for (int k = k0; k < k0 + per && k < np; ++k) {
         const unsigned long long x = key[k];
         if (x == ~0ull) continue;
-        const int v = (int)(x >> 32);
         if (k == 0 || (key[k - 1] >> 32) != (x >> 32)) {
             ++local;
-            out[local] = v;
+            out[local] = (int)(x >> 32);
+            ro[local] = (unsigned short)k;
         }
-        loc_map[c0 * arity + (int)(x & 0xffffffffu)] = (unsigned short)local;
+        loc_map[c0 * arity + (int)(x & 0xffffffffu)] = (unsigned short)k;
     }
+    if (threadIdx.x == 0) ro[nu] = (unsigned short)nvalid;
 }
 
-__global__ void k_max_count(const long long *__restrict__ c, long long n,
-                            unsigned long long *__restrict__ mx) {
+__global__ void k_max_count(const int *__restrict__ c, long long n, unsigned *__restrict__ mx) {
     const long long stride = (long long)gridDim.x * blockDim.x;
-    unsigned long long m = 0;
+    unsigned m = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride)
-        m = c[i] > (long long)m ? (unsigned long long)c[i] : m;
+        m = (unsigned)c[i] > m ? (unsigned)c[i] : m;
     atomicMax(mx, m);
 }
 
@@ -150,32 +174,33 @@ op2g_status op2g_stage_plan_workspace(int64_t n, int32_t arity, int64_t block, s
 }
 
 op2g_status op2g_stage_plan_count(int64_t n, int32_t arity, const int32_t *map, int64_t block,
-                                  void *ws, size_t ws_bytes, int64_t *ind_off, int64_t *total,
-                                  int32_t *max_unique, void *stream) {
+                                  void *ws, size_t ws_bytes, int64_t *ind_off, int32_t *ind_num,
+                                  int64_t *total, int32_t *max_unique, void *stream) {
     op2g_status s = check_args(n, arity, block);
     if (s != OP2G_OK) return s;
     size_t need = 0;
     op2g_stage_plan_workspace(n, arity, block, &need);
     if (!ws || ws_bytes < need) return op2g::fail(OP2G_ERR_INVALID, "workspace too small");
-    if (!ind_off || (n > 0 && !map)) return op2g::fail(OP2G_ERR_INVALID, "NULL argument");
-    cudaStream_t st = (cudaStream_t)stream;
     const long long nb = (n + block - 1) / block;
+    if (!ind_off || (nb > 0 && (!map || !ind_num)))
+        return op2g::fail(OP2G_ERR_INVALID, "NULL argument");
+    cudaStream_t st = (cudaStream_t)stream;
     long long *tmp = (long long *)ws;
-    unsigned long long *mx =
-        (unsigned long long *)((char *)ws + a256(sizeof(long long) * op2g::scan_tmp_elems(nb + 1)));
+    unsigned *mx =
+        (unsigned *)((char *)ws + a256(sizeof(long long) * op2g::scan_tmp_elems(nb + 1)));
     CK(cudaMemsetAsync(ind_off, 0, sizeof(long long) * (nb + 1), st));
-    CK(cudaMemsetAsync(mx, 0, sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(mx, 0, sizeof(unsigned), st));
     if (nb > 0) {
         k_stage_plan<<<(unsigned)nb, PT, 0, st>>>(n, arity, map, block, 0, (long long *)ind_off,
-                                                  nullptr, nullptr, nullptr);
+                                                  ind_num, nullptr, nullptr, nullptr, nullptr);
         CK(cudaGetLastError());
-        k_max_count<<<nb < 1024 ? 1 : 152, 256, 0, st>>>((const long long *)ind_off, nb, mx);
+        k_max_count<<<nb < 1024 ? 1 : 152, 256, 0, st>>>(ind_num, nb, mx);
         CK(cudaGetLastError());
     }
     s = op2g::scan_exclusive((long long *)ind_off, nb + 1, tmp, st);
     if (s != OP2G_OK) return s;
     long long tot = 0;
-    unsigned long long m = 0;
+    unsigned m = 0;
     CK(cudaMemcpyAsync(&tot, ind_off + nb, sizeof tot, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&m, mx, sizeof m, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -185,17 +210,18 @@ op2g_status op2g_stage_plan_count(int64_t n, int32_t arity, const int32_t *map, 
 }
 
 op2g_status op2g_stage_plan_fill(int64_t n, int32_t arity, const int32_t *map, int64_t block,
-                                 const int64_t *ind_off, int32_t *ind_map, uint16_t *loc_map,
-                                 void *stream) {
+                                 const int64_t *ind_off, int32_t *ind_map, uint16_t *run_off,
+                                 uint16_t *loc_map, void *stream) {
     op2g_status s = check_args(n, arity, block);
     if (s != OP2G_OK) return s;
     if (n == 0) return OP2G_OK;
-    if (!map || !ind_off || !ind_map || !loc_map)
+    if (!map || !ind_off || !ind_map || !run_off || !loc_map)
         return op2g::fail(OP2G_ERR_INVALID, "NULL argument");
     cudaStream_t st = (cudaStream_t)stream;
     const long long nb = (n + block - 1) / block;
-    k_stage_plan<<<(unsigned)nb, PT, 0, st>>>(n, arity, map, block, 1, nullptr,
-                                              (const long long *)ind_off, ind_map, loc_map);
+    k_stage_plan<<<(unsigned)nb, PT, 0, st>>>(n, arity, map, block, 1, nullptr, nullptr,
+                                              (const long long *)ind_off, ind_map, run_off,
+                                              loc_map);
     CK(cudaGetLastError());
     return OP2G_OK;
 }

@@ -942,14 +942,17 @@ def colour_plan(loop, max_colours=256):
 
 # ---------------------------------------------------------- staging plans
 class MapStagePlan:
-    """The staging plan of one map: partitions of ``block`` iterations; per
-    partition the sorted distinct targets (``ind_map[ind_off[p]:ind_off[p+1]]``)
-    and per map entry its local index (``loc_map``, uint16, 0xFFFF for a
-    negative entry) -- the local renumbering of the historical OP2 execution
-    plan (doc/sphinx/source/plan.rst:21-39), built on the device."""
+    """The staging plan of one map over its iteration set's ``size`` entities:
+    partitions of ``block`` iterations; per partition a segment (at
+    ``ind_off[p]``, 16-byte aligned) of its ``ind_num[p]`` sorted distinct
+    targets (``ind_map``) with the first slot of each (``run_off``), and per
+    map entry its slot (``loc_map``, uint16: its rank in the partition's
+    entries sorted by target; 0xFFFF for a negative entry) -- the local
+    renumbering of the historical OP2 execution plan
+    (doc/sphinx/source/plan.rst:21-39), built on the device."""
 
     def __init__(self, m, block):
-        n, ar = m.iterset.total_size, m.arity
+        n, ar = m.iterset.size, m.arity
         dev = device.device()
         nb = (n + block - 1) // block
         st = device.stream_handle()
@@ -958,14 +961,19 @@ class MapStagePlan:
         _lib.call("op2g_stage_plan_workspace", n, ar, block, ctypes.byref(ws))
         work = device.empty_bytes(ws.value)
         self.ind_off = torch.empty(nb + 1, dtype=torch.int64, device=dev)
+        self.ind_num = torch.empty(max(nb, 1), dtype=torch.int32, device=dev)
         total = ctypes.c_int64()
         mx = ctypes.c_int32()
         _lib.call("op2g_stage_plan_count", n, ar, vals.data_ptr(), block, work.data_ptr(),
-                  ws.value, self.ind_off.data_ptr(), ctypes.byref(total), ctypes.byref(mx), st)
-        self.ind_map = torch.empty(max(total.value, 1), dtype=torch.int32, device=dev)
+                  ws.value, self.ind_off.data_ptr(), self.ind_num.data_ptr(), ctypes.byref(total),
+                  ctypes.byref(mx), st)
+        self.ind_map = torch.empty(max(total.value, 8), dtype=torch.int32, device=dev)
+        self.run_off = torch.empty(max(total.value, 8), dtype=torch.int16, device=dev)
         self.loc_map = torch.empty(max(n * ar, 4), dtype=torch.int16, device=dev)
         _lib.call("op2g_stage_plan_fill", n, ar, vals.data_ptr(), block,
-                  self.ind_off.data_ptr(), self.ind_map.data_ptr(), self.loc_map.data_ptr(), st)
+                  self.ind_off.data_ptr(), self.ind_map.data_ptr(), self.run_off.data_ptr(),
+                  self.loc_map.data_ptr(), st)
+        self.n = n
         self.block = block
         self.max_unique = mx.value
         self.total = total.value
@@ -993,6 +1001,8 @@ class StagePlan:
                     continue
                 d.ind_map[i] = mp.ind_map.data_ptr()
                 d.ind_off[i] = mp.ind_off.data_ptr()
+                d.ind_num[i] = mp.ind_num.data_ptr()
+                d.run_off[i] = mp.run_off.data_ptr()
                 d.loc_map[i] = mp.loc_map.data_ptr()
                 d.max_unique[i] = mp.max_unique
             self._descs[key] = d
@@ -1017,24 +1027,29 @@ def stage_plan(loop):
         return None
     plans = {}
     for m in roots:
-        key = ("stage", block)
+        key = ("stage", block, m.iterset.size)
         mp = m._cache.get(key)
         if mp is None:
             mp = MapStagePlan(m, block)
             m._cache[key] = mp
         plans[m._serial] = mp
-    # shared memory of the staged wrapper: each staged map's target list and
-    # each staged argument's values at the largest partition
+    # shared memory of the staged wrapper (an upper bound of what it takes):
+    # per staged map its target list, run offsets and slot -> target table;
+    # per READ argument its values per target, per INC one value per slot
+    def r16(x):
+        return (x + 15) // 16 * 16
     smem = 0
     for m in roots:
-        smem += (plans[m._serial].max_unique * 4 + 15) // 16 * 16
+        mu = plans[m._serial].max_unique
+        smem += r16(mu * 4) + r16((mu + 1) * 2) + r16(block * m.arity * 2)
     for a, group, _ in loop._flat:
         if isinstance(a, DatLegacyArg) and a.map_ is not None and not group and \
                 a.access in (Access.READ, Access.INC):
             m = a.map_.map_ if isinstance(a.map_, PermutedMap) else a.map_
             if m._serial in plans:
-                smem += (plans[m._serial].max_unique * a.data.cdim * a.data.dtype.itemsize
-                         + 15) // 16 * 16
+                rows = plans[m._serial].max_unique if a.access is Access.READ \
+                    else block * m.arity
+                smem += r16(rows * a.data.cdim * a.data.dtype.itemsize)
     if smem > _STAGE_SMEM_LIMIT:
         return None
     return StagePlan(plans, block)

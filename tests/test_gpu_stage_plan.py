@@ -10,17 +10,24 @@ pytestmark = pytest.mark.gpu
 
 
 def plan_model(vals, block):
+    """Per partition: the padded segment, the sorted distinct targets, the
+    first slot of each and the number of valid entries, and every entry's
+    slot (its rank among the partition's valid entries sorted by (target,
+    position))."""
     n, ar = vals.shape
-    off, ind, loc = [0], [], np.full(n * ar, 0xFFFF, dtype=np.int64)
+    off, num, ind, runs = [0], [], [], []
+    loc = np.full(n * ar, 0xFFFF, dtype=np.int64)
     for c0 in range(0, n, block):
         v = vals[c0:c0 + block].reshape(-1)
-        u = np.unique(v[v >= 0])
-        ind.append(u)
-        off.append(off[-1] + len(u))
-        pos = np.searchsorted(u, v)
-        ok = v >= 0
-        loc[c0 * ar:c0 * ar + len(v)][ok] = pos[ok]
-    return np.array(off), (np.concatenate(ind) if ind else np.zeros(0, np.int32)), loc
+        valid = np.nonzero(v >= 0)[0]
+        order = valid[np.lexsort((valid, v[valid]))]       # by target, then position
+        loc[c0 * ar + order] = np.arange(len(order))
+        u, first = np.unique(v[order], return_index=True)
+        seg = (len(u) + 1 + 7) // 8 * 8
+        ind.append((u, np.append(first, len(order)), seg))
+        num.append(len(u))
+        off.append(off[-1] + seg)
+    return np.array(off), np.array(num), ind, loc
 
 
 @pytest.mark.parametrize("n,arity,block,ntargets", [
@@ -35,13 +42,18 @@ def test_plan_matches_model(gpu_op2, n, arity, block, ntargets):
     src, dst = op2.Set(n), op2.Set(ntargets)
     m = op2.Map(src, dst, arity, vals)
     p = MapStagePlan(m, block)
-    off, ind, loc = plan_model(vals, block)
+    off, num, segs, loc = plan_model(vals, block)
     assert np.array_equal(p.ind_off.cpu().numpy(), off)
+    assert np.array_equal(p.ind_num.cpu().numpy()[:len(num)], num)
     assert p.total == off[-1]
-    assert np.array_equal(p.ind_map.cpu().numpy()[:off[-1]], ind)
+    ind = p.ind_map.cpu().numpy()
+    runs = p.run_off.cpu().numpy().astype(np.int64) & 0xFFFF
+    for b, (u, first, seg) in enumerate(segs):
+        assert np.array_equal(ind[off[b]:off[b] + len(u)], u)
+        assert np.array_equal(runs[off[b]:off[b] + len(u) + 1], first)
     got = p.loc_map.cpu().numpy()[:n * arity].astype(np.int64) & 0xFFFF
     assert np.array_equal(got, loc)
-    assert p.max_unique == int(np.max(np.diff(off)))
+    assert p.max_unique == int(np.max(num))
 
 
 def test_staged_loop_equals_atomic_loop_with_negative_entries(gpu_op2):
