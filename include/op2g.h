@@ -57,7 +57,8 @@ enum {
 enum {
     OP2G_DEVERR_MAP_BOUNDS = 1,   /* map value >= toset size (debug builds)  */
     OP2G_DEVERR_NEW_NONZERO = 2,  /* (row, col) not in the Mat's pattern     */
-    OP2G_DEVERR_CAPACITY = 4      /* row candidate list above the capacity   */
+    OP2G_DEVERR_CAPACITY = 4,     /* row candidate list above the capacity   */
+    OP2G_DEVERR_TIMEOUT = 8       /* a bounded wait of a staged wrapper gave up */
 };
 
 /* Thread-local description of the last failure (never NULL). */

@@ -100,30 +100,6 @@ static bool declared_without_parameters(const std::string &src, const std::strin
 // with an element type shared-memory atomics support.  Entry a is the plain
 // map whose plan the argument uses, or -1.  Non-extruded, non-indexed loops
 // only; an empty result means the wrapper runs as OP2G_SCATTER_ATOMIC.
-std::vector<int> staged_args(const Signature &S) {
-    std::vector<int> st(S.args.size(), -1);
-    if (S.loop.scatter != OP2G_SCATTER_STAGED || S.loop.extruded || S.loop.indexed) return st;
-    bool any = false;
-    for (size_t a = 0; a < S.args.size(); ++a) {
-        const op2g_arg_desc &d = S.args[a].d;
-        if (d.kind != OP2G_ARG_DAT || d.map < 0 || d.group != 0) continue;
-        const MapInfo &mi = S.maps[d.map];
-        int root = -1;
-        if (mi.kind == OP2G_MAP_PLAIN) root = d.map;
-        else if (mi.kind == OP2G_MAP_PERMUTED) root = mi.base;
-        if (root < 0) continue;
-        const bool inc_ok = d.access == OP2G_INC &&
-                            (d.dtype == OP2G_F64 || d.dtype == OP2G_F32 || d.dtype == OP2G_I32 ||
-                             d.dtype == OP2G_U32 || d.dtype == OP2G_U64 || d.dtype == OP2G_I64);
-        const bool read_ok = d.access == OP2G_READ && S.loop.nc_reads;
-        if (!inc_ok && !read_ok) continue;
-        st[a] = root;
-        any = true;
-    }
-    (void)any;
-    return st;
-}
-
 static size_t elt_size(int dt) {
     switch (dt) {
         case OP2G_F64: case OP2G_I64: case OP2G_U64: return 8;
@@ -133,30 +109,77 @@ static size_t elt_size(int dt) {
     }
 }
 
+std::vector<int> staged_args(const Signature &S) {
+    std::vector<int> st(S.args.size(), -1);
+    if (S.loop.scatter != OP2G_SCATTER_STAGED || S.loop.extruded || S.loop.indexed) return st;
+    for (size_t a = 0; a < S.args.size(); ++a) {
+        const op2g_arg_desc &d = S.args[a].d;
+        if (d.kind != OP2G_ARG_DAT || d.map < 0 || d.group != 0) continue;
+        const MapInfo &mi = S.maps[d.map];
+        int root = -1;
+        if (mi.kind == OP2G_MAP_PLAIN) root = d.map;
+        else if (mi.kind == OP2G_MAP_PERMUTED) root = mi.base;
+        if (root < 0) continue;
+        const size_t e = elt_size(d.dtype);
+        const bool inc_ok = d.access == OP2G_INC &&
+                            (d.dtype == OP2G_F64 || d.dtype == OP2G_F32 || d.dtype == OP2G_I32 ||
+                             d.dtype == OP2G_U32 || d.dtype == OP2G_U64 || d.dtype == OP2G_I64);
+        const bool read_ok = d.access == OP2G_READ && S.loop.nc_reads && (e == 4 || e == 8);
+        if (!inc_ok && !read_ok) continue;
+        st[a] = root;
+    }
+    return st;
+}
+
+// Direct READ arguments a staged wrapper fetches ahead into shared memory
+// (4- or 8-byte elements, not parts of a mixed argument); only when the
+// wrapper stages at least one argument.
+std::vector<bool> staged_direct(const Signature &S) {
+    std::vector<bool> out(S.args.size(), false);
+    std::vector<int> st = staged_args(S);
+    bool any = false;
+    for (int r : st) any = any || r >= 0;
+    if (!any) return out;
+    for (size_t a = 0; a < S.args.size(); ++a) {
+        const op2g_arg_desc &d = S.args[a].d;
+        const size_t e = elt_size(d.dtype);
+        out[a] = d.kind == OP2G_ARG_DAT && d.map < 0 && d.access == OP2G_READ && d.group == 0 &&
+                 (e == 4 || e == 8);
+    }
+    return out;
+}
+
 // Bytes of dynamic shared memory a staged wrapper takes for partitions of
 // `block` iterations whose largest distinct-target counts are max_unique[m]
-// (the layout the generated code computes, each region rounded up to 16
-// bytes): per staged map its target list (int), run offsets and per-slot
-// target table (uint16); per staged READ argument its values per target;
-// per staged INC argument its contributions per slot.
+// -- the layout the generated code computes, every region rounded up to 16
+// bytes: per staged map, three plan buffers (target list, run offsets, the
+// partition's slots) and the slot -> target table; per staged READ argument
+// two value buffers (one value per target); per staged INC argument one
+// value per slot; per fetched direct argument two buffers of the
+// partition's values.
 size_t staged_smem_bytes(const Signature &S, int64_t block, const int32_t *max_unique) {
     std::vector<int> st = staged_args(S);
+    std::vector<bool> dr = staged_direct(S);
     auto r16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
     size_t bytes = 0;
     std::vector<bool> seen(S.maps.size(), false);
     for (size_t a = 0; a < st.size(); ++a)
-        if (st[a] >= 0 && !seen[st[a]]) {
-            const int m = st[a];
-            seen[m] = true;
-            const size_t mu = (size_t)max_unique[m];
-            bytes += r16(mu * 4) + r16((mu + 1) * 2) + r16((size_t)block * S.maps[m].arity * 2);
+        if (st[a] >= 0) seen[st[a]] = true;
+    for (size_t m = 0; m < S.maps.size(); ++m)
+        if (seen[m]) {
+            const size_t seg = ((size_t)max_unique[m] + 1 + 7) / 8 * 8;
+            const size_t slots = (size_t)block * S.maps[m].arity;
+            bytes += 3 * (r16(seg * 4) + r16(seg * 2) + r16(slots * 2)) + r16(slots * 2);
         }
     for (size_t a = 0; a < st.size(); ++a) {
-        if (st[a] < 0) continue;
         const op2g_arg_desc &d = S.args[a].d;
-        const size_t rows = d.access == OP2G_READ ? (size_t)max_unique[st[a]]
-                                                  : (size_t)block * S.maps[st[a]].arity;
-        bytes += r16(rows * d.dim * elt_size(d.dtype));
+        const size_t e = elt_size(d.dtype);
+        if (st[a] >= 0 && d.access == OP2G_READ)
+            bytes += 2 * r16((size_t)max_unique[st[a]] * d.dim * e);
+        else if (st[a] >= 0)
+            bytes += r16((size_t)block * S.maps[st[a]].arity * d.dim * e);
+        else if (dr[a])
+            bytes += 2 * r16((size_t)block * d.dim * e);
     }
     return bytes;
 }
@@ -180,13 +203,14 @@ struct Gen {
     // or -1; per map whether the wrapper loads its plan; set while the
     // staged run function is written.
     std::vector<int> st_arg;
-    std::vector<bool> st_map;
+    std::vector<bool> st_map, st_dir;
     bool any_staged = false, staging = false;
 
     explicit Gen(const Signature &s) : S(s) {
         nf = (S.loop.extruded && S.loop.iteration_region == OP2G_ON_INTERIOR_FACETS) ? 2 : 1;
         layout();
         st_arg = staged_args(S);
+        st_dir = staged_direct(S);
         st_map.assign(S.maps.size(), false);
         for (int r : st_arg)
             if (r >= 0) {
@@ -452,23 +476,23 @@ struct Gen {
         const std::string lv = "lv" + std::to_string(m), mv = base_row(m);
         o << ind << "unsigned short " << lv << "[" << ar << "];\n";
         o << ind << "int " << mv << "[" << ar << "];\n";
-        o << ind << "{ const unsigned short *r_ = p.sloc[" << m << "] + n * " << ar << ";\n";
+        o << ind << "{ const unsigned short *r_ = lc" << m << "[mb_] + (n - pbase_) * " << ar << ";\n";
         if (ar % 4 == 0) {
             for (int q = 0; q < ar / 4; ++q)
-                o << ind << "  { const ushort4 v_ = __ldg((const ushort4 *)r_ + " << q << "); " << lv
+                o << ind << "  { const ushort4 v_ = ((const ushort4 *)r_)[" << q << "]; " << lv
                   << "[" << 4 * q << "] = v_.x; " << lv << "[" << 4 * q + 1 << "] = v_.y; " << lv
                   << "[" << 4 * q + 2 << "] = v_.z; " << lv << "[" << 4 * q + 3 << "] = v_.w; }\n";
         } else if (ar % 2 == 0) {
             for (int q = 0; q < ar / 2; ++q)
-                o << ind << "  { const ushort2 v_ = __ldg((const ushort2 *)r_ + " << q << "); " << lv
+                o << ind << "  { const ushort2 v_ = ((const ushort2 *)r_)[" << q << "]; " << lv
                   << "[" << 2 * q << "] = v_.x; " << lv << "[" << 2 * q + 1 << "] = v_.y; }\n";
         } else {
             o << ind << "#pragma unroll\n";
-            o << ind << "  for (int i = 0; i < " << ar << "; ++i) " << lv << "[i] = __ldg(r_ + i);\n";
+            o << ind << "  for (int i = 0; i < " << ar << "; ++i) " << lv << "[i] = r_[i];\n";
         }
         o << ind << "#pragma unroll\n";
         o << ind << "  for (int i = 0; i < " << ar << "; ++i) " << mv << "[i] = " << lv
-          << "[i] == 0xFFFF ? -1 : si" << m << "[tg" << m << "[" << lv << "[i]]];\n";
+          << "[i] == 0xFFFF ? -1 : si" << m << "[mb_][tg" << m << "[" << lv << "[i]]];\n";
         o << ind << "}\n";
     }
 
@@ -481,83 +505,191 @@ struct Gen {
         return "(int)lv" + std::to_string(r) + "[op2g_perm" + std::to_string(m) + "[" + i + "]]";
     }
 
-    // The staged run function: CTAs take mini-partitions of the plan in turn.
-    // Per partition: the target lists and run offsets of the staged maps and
-    // the values of staged READ arguments (each distinct target once) are
-    // loaded into shared memory, and a slot -> target table is filled; the
-    // partition's iterations run with READ packs from shared memory and INC
-    // contributions stored at their slots; then each target's run of slots is
-    // summed in slot order and added to the target with one global atomic.
+    // The staged run function.  CTAs take mini-partitions of the plan in turn
+    // and pipeline them: the plan segments of partition q + 2 (target list,
+    // run offsets, the partition's slots) arrive by bulk copy (one thread
+    // issues them; they complete on one of three mbarriers) and the staged
+    // READ values and fetched direct arguments of partition q + 1 by
+    // per-element asynchronous copies, while partition q computes.  Per
+    // partition: a slot -> target table is filled, the iterations run with
+    // READ packs from shared memory and INC contributions stored at their
+    // slots, then each target's run of slots is summed in slot order and
+    // added to the target with one global atomic.  Every mbarrier wait is
+    // bounded; when one gives up, the CTA sets OP2G_DEVERR_TIMEOUT in the
+    // error word (when there is one), waits (bounded) for its copies in
+    // flight and stops.
     void emit_staged_run() {
         std::ostringstream &O = o;
         const int BS = S.block_size;
         staging = true;
+        std::vector<int> ms;   // staged maps
+        for (size_t m = 0; m < S.maps.size(); ++m)
+            if (st_map[m]) ms.push_back((int)m);
+        const int NSM = (int)ms.size();
         O << "__device__ __forceinline__ void op2g_run_staged(const op2g_params_t &p) {\n";
         O << "  extern __shared__ __align__(16) unsigned char op2g_smem[];\n";
+        O << "  __shared__ __align__(8) unsigned long long bar_[3];\n";
+        O << "  __shared__ int snu_[3][" << NSM << "];\n";
         emit_global_init();
+        // layout (mirrored by staged_smem_bytes on the host)
         O << "  size_t so_ = 0;\n";
-        for (size_t m = 0; m < S.maps.size(); ++m)
-            if (st_map[m]) {
-                const int ar = S.maps[m].arity;
-                O << "  int *si" << m << " = (int *)(op2g_smem + so_); so_ += ((size_t)p.smax[" << m
-                  << "] * 4 + 15) & ~(size_t)15;\n";
-                O << "  unsigned short *ro" << m << " = (unsigned short *)(op2g_smem + so_); so_ += "
-                  << "((size_t)(p.smax[" << m << "] + 1) * 2 + 15) & ~(size_t)15;\n";
-                O << "  unsigned short *tg" << m << " = (unsigned short *)(op2g_smem + so_); so_ += "
-                  << "((size_t)p.sblock * " << ar << " * 2 + 15) & ~(size_t)15;\n";
+        for (int m : ms) {
+            const int ar = S.maps[m].arity;
+            O << "  const int seg" << m << "_ = (int)((p.smax[" << m << "] + 1 + 7) / 8 * 8);\n";
+            O << "  int *si" << m << "[3]; unsigned short *ro" << m << "[3], *lc" << m << "[3];\n";
+            O << "  for (int b_ = 0; b_ < 3; ++b_) {\n";
+            O << "    si" << m << "[b_] = (int *)(op2g_smem + so_); so_ += ((size_t)seg" << m
+              << "_ * 4 + 15) & ~(size_t)15;\n";
+            O << "    ro" << m << "[b_] = (unsigned short *)(op2g_smem + so_); so_ += ((size_t)seg" << m
+              << "_ * 2 + 15) & ~(size_t)15;\n";
+            O << "    lc" << m << "[b_] = (unsigned short *)(op2g_smem + so_); so_ += ((size_t)p.sblock * "
+              << ar << " * 2 + 15) & ~(size_t)15;\n";
+            O << "  }\n";
+            O << "  unsigned short *tg" << m << " = (unsigned short *)(op2g_smem + so_); so_ += "
+              << "((size_t)p.sblock * " << ar << " * 2 + 15) & ~(size_t)15;\n";
+        }
+        for (size_t a = 0; a < S.args.size(); ++a) {
+            const op2g_arg_desc &d = S.args[a].d;
+            const char *T = ctype_of(d.dtype);
+            if (st_arg[a] >= 0 && d.access == OP2G_READ) {
+                O << "  " << T << " *sv" << a << "[2];\n";
+                O << "  for (int b_ = 0; b_ < 2; ++b_) { sv" << a << "[b_] = (" << T
+                  << " *)(op2g_smem + so_); so_ += ((size_t)p.smax[" << st_arg[a] << "] * " << d.dim
+                  << " * sizeof(" << T << ") + 15) & ~(size_t)15; }\n";
+            } else if (st_arg[a] >= 0) {
+                O << "  " << T << " *sv" << a << " = (" << T << " *)(op2g_smem + so_); so_ += ((size_t)p.sblock * "
+                  << S.maps[st_arg[a]].arity << " * " << d.dim << " * sizeof(" << T
+                  << ") + 15) & ~(size_t)15;\n";
+            } else if (st_dir[a]) {
+                O << "  " << T << " *dv" << a << "[2];\n";
+                O << "  for (int b_ = 0; b_ < 2; ++b_) { dv" << a << "[b_] = (" << T
+                  << " *)(op2g_smem + so_); so_ += ((size_t)p.sblock * " << d.dim << " * sizeof(" << T
+                  << ") + 15) & ~(size_t)15; }\n";
             }
-        for (size_t a = 0; a < S.args.size(); ++a)
-            if (st_arg[a] >= 0) {
-                const op2g_arg_desc &d = S.args[a].d;
-                const char *T = ctype_of(d.dtype);
-                const std::string rows = d.access == OP2G_READ
-                                             ? "(size_t)p.smax[" + std::to_string(st_arg[a]) + "]"
-                                             : "(size_t)p.sblock * " +
-                                                   std::to_string(S.maps[st_arg[a]].arity);
-                O << "  " << T << " *sv" << a << " = (" << T << " *)(op2g_smem + so_); so_ += ("
-                  << rows << " * " << d.dim << " * sizeof(" << T << ") + 15) & ~(size_t)15;\n";
-            }
-        O << "  const long long pb0_ = p.start / p.sblock, pb1_ = (p.end + p.sblock - 1) / p.sblock;\n";
-        O << "  for (long long pb_ = pb0_ + blockIdx.x; pb_ < pb1_; pb_ += gridDim.x) {\n";
-        O << "    const long long c0_ = pb_ * p.sblock > p.start ? pb_ * p.sblock : p.start;\n";
-        O << "    const long long c1_ = (pb_ + 1) * p.sblock < p.end ? (pb_ + 1) * p.sblock : p.end;\n";
-        for (size_t m = 0; m < S.maps.size(); ++m)
-            if (st_map[m]) {
-                O << "    const long long so" << m << "_ = p.soff[" << m << "][pb_];\n";
-                O << "    const int nu" << m << "_ = p.snum[" << m << "][pb_];\n";
-                O << "    for (int k_ = threadIdx.x; k_ <= nu" << m << "_; k_ += " << BS << ") {\n";
-                O << "      if (k_ < nu" << m << "_) si" << m << "[k_] = __ldg(p.sind[" << m << "] + so"
-                  << m << "_ + k_);\n";
-                O << "      ro" << m << "[k_] = __ldg(p.sruns[" << m << "] + so" << m << "_ + k_);\n";
+        }
+        O << "  (void)so_;\n";
+        O << "  const long long pb1_ = (p.end + p.sblock - 1) / p.sblock;\n";
+        O << "  const long long first_ = p.start / p.sblock + blockIdx.x, step_ = gridDim.x;\n";
+        O << "  if (threadIdx.x == 0) {\n";
+        O << "    for (int b_ = 0; b_ < 3; ++b_) op2g::mbar_init(&bar_[b_], 1);\n";
+        O << "    op2g::fence_mbar_init();\n";
+        O << "  }\n";
+        O << "  __syncthreads();\n";
+        O << "  unsigned ph_[3] = {0u, 0u, 0u};   // parity of each plan buffer's next phase\n";
+        O << "  bool pend_[3] = {false, false, false};   // a bulk copy into the buffer is in flight\n";
+        // thread 0 holds the plan offsets of the next partition to issue
+        O << "  long long po_[" << NSM << "], pl_[" << NSM << "]; int pn_[" << NSM << "];\n";
+        O << "  auto load_next_ = [&](long long q_) {\n";
+        O << "    if (threadIdx.x != 0 || q_ >= pb1_) return;\n";
+        for (int i = 0; i < NSM; ++i) {
+            const int m = ms[i];
+            O << "    po_[" << i << "] = p.soff[" << m << "][q_]; pl_[" << i << "] = p.soff[" << m
+              << "][q_ + 1] - po_[" << i << "]; pn_[" << i << "] = p.snum[" << m << "][q_];\n";
+        }
+        O << "  };\n";
+        // the plan segments of partition q into plan buffer b (thread 0 issues)
+        O << "  auto issue_meta_ = [&](long long q_, int b_) {\n";
+        O << "    if (q_ >= pb1_) return;\n";
+        O << "    pend_[b_] = true;\n";
+        O << "    if (threadIdx.x != 0) return;\n";
+        O << "    const long long qb_ = q_ * p.sblock;\n";
+        O << "    const long long qe_ = qb_ + p.sblock < p.end ? qb_ + p.sblock : p.end;\n";
+        O << "    unsigned bytes_ = 0;\n";
+        for (int i = 0; i < NSM; ++i) {
+            const int m = ms[i], ar = S.maps[m].arity;
+            O << "    const unsigned lb" << i << "_ = (unsigned)(((qe_ - qb_) * " << ar
+              << " * 2 + 15) & ~15LL);\n";
+            O << "    bytes_ += (unsigned)pl_[" << i << "] * 6u + lb" << i << "_;\n";
+            O << "    snu_[b_][" << i << "] = pn_[" << i << "];\n";
+        }
+        O << "    op2g::mbar_expect_tx(&bar_[b_], bytes_);\n";
+        for (int i = 0; i < NSM; ++i) {
+            const int m = ms[i], ar = S.maps[m].arity;
+            O << "    op2g::bulk_g2s(si" << m << "[b_], p.sind[" << m << "] + po_[" << i
+              << "], (unsigned)pl_[" << i << "] * 4u, &bar_[b_]);\n";
+            O << "    op2g::bulk_g2s(ro" << m << "[b_], p.sruns[" << m << "] + po_[" << i
+              << "], (unsigned)pl_[" << i << "] * 2u, &bar_[b_]);\n";
+            O << "    op2g::bulk_g2s(lc" << m << "[b_], p.sloc[" << m << "] + qb_ * " << ar << ", lb"
+              << i << "_, &bar_[b_]);\n";
+        }
+        O << "    load_next_(q_ + step_);\n";
+        O << "  };\n";
+        // the value copies of partition q (plan buffer mb, value buffer vb)
+        O << "  auto issue_vals_ = [&](long long q_, int qm_, int qv_) {\n";
+        O << "    if (q_ >= pb1_) return;\n";
+        O << "    const long long q0_ = q_ * p.sblock > p.start ? q_ * p.sblock : p.start;\n";
+        O << "    const long long q1_ = (q_ + 1) * p.sblock < p.end ? (q_ + 1) * p.sblock : p.end;\n";
+        O << "    (void)q0_; (void)q1_; (void)qm_; (void)qv_;\n";
+        for (size_t a = 0; a < S.args.size(); ++a) {
+            const op2g_arg_desc &d = S.args[a].d;
+            const char *T = ctype_of(d.dtype);
+            const size_t e = elt_size(d.dtype);
+            if (st_arg[a] >= 0 && d.access == OP2G_READ) {
+                const int r = st_arg[a];
+                int qi = 0;
+                while (ms[qi] != r) ++qi;
+                O << "    for (int k_ = threadIdx.x; k_ < snu_[qm_][" << qi << "] * " << d.dim << "; k_ += "
+                  << BS << ") {\n";
+                O << "      const int v_ = k_ / " << d.dim << ";\n";
+                O << "      op2g::cp_async<" << e << ">(sv" << a << "[qv_] + k_, (const " << T
+                  << " *)p.ptr[" << S.args[a].slot << "] + (long long)si" << r << "[qm_][v_] * "
+                  << gstride(a) << " + (k_ - v_ * " << d.dim << "));\n";
+                O << "    }\n";
+            } else if (st_arg[a] < 0 && st_dir[a]) {
+                O << "    for (int k_ = threadIdx.x; k_ < (int)(q1_ - q0_) * " << d.dim << "; k_ += " << BS
+                  << ") {\n";
+                O << "      const int v_ = k_ / " << d.dim << ";\n";
+                O << "      op2g::cp_async<" << e << ">(dv" << a << "[qv_] + k_, (const " << T << " *)p.ptr["
+                  << S.args[a].slot << "] + (q0_ + v_) * " << gstride(a) << " + (k_ - v_ * " << d.dim
+                  << "));\n";
                 O << "    }\n";
             }
+        }
+        O << "  };\n";
+        O << "  bool ok_ = true;\n";
+        // prologue: plan segments of the first two partitions, values of the first
+        O << "  load_next_(first_);\n";
+        O << "  issue_meta_(first_, 0);\n";
+        O << "  issue_meta_(first_ + step_, 1);\n";
+        O << "  if (first_ < pb1_) {\n";
+        O << "    ok_ = op2g::mbar_wait(&bar_[0], ph_[0]);\n";
+        O << "    if (ok_) { ph_[0] ^= 1u; pend_[0] = false; }\n";
+        O << "    ok_ = __syncthreads_and(ok_);\n";
+        O << "    if (ok_) issue_vals_(first_, 0, 0);\n";
+        O << "  }\n";
+        O << "  op2g::cp_async_commit();\n";
+        O << "  int mb_ = 0, vb_ = 0;\n";
+        O << "  for (long long pb_ = first_; ok_ && pb_ < pb1_; pb_ += step_) {\n";
+        O << "    const int mbn_ = mb_ == 2 ? 0 : mb_ + 1, mbn2_ = mbn_ == 2 ? 0 : mbn_ + 1;\n";
+        O << "    if (pb_ + step_ < pb1_) {\n";
+        O << "      ok_ = op2g::mbar_wait(&bar_[mbn_], ph_[mbn_]);\n";
+        O << "      if (ok_) { ph_[mbn_] ^= 1u; pend_[mbn_] = false; }\n";
+        O << "      if (!__syncthreads_and(ok_)) { ok_ = false; break; }\n";
+        O << "      issue_vals_(pb_ + step_, mbn_, vb_ ^ 1);\n";
+        O << "    }\n";
+        O << "    op2g::cp_async_commit();\n";
+        O << "    op2g::cp_async_wait<1>();   // this partition's values\n";
         O << "    __syncthreads();\n";
-        for (size_t m = 0; m < S.maps.size(); ++m)
-            if (st_map[m]) {
-                O << "    for (int k_ = threadIdx.x; k_ < nu" << m << "_; k_ += " << BS << ")\n";
-                O << "      for (int s_ = ro" << m << "[k_]; s_ < ro" << m << "[k_ + 1]; ++s_) tg" << m
-                  << "[s_] = (unsigned short)k_;\n";
-            }
+        // buffer mbn2_ was last read by the previous partition, whose final
+        // barrier (with the proxy fence before it) ordered those reads
+        O << "    issue_meta_(pb_ + 2 * step_, mbn2_);\n";
+        O << "    const long long pbase_ = pb_ * p.sblock;\n";
+        O << "    const long long c0_ = pbase_ > p.start ? pbase_ : p.start;\n";
+        O << "    const long long c1_ = pbase_ + p.sblock < p.end ? pbase_ + p.sblock : p.end;\n";
+        for (int i = 0; i < NSM; ++i) {
+            const int m = ms[i];
+            O << "    const int nu" << m << "_ = snu_[mb_][" << i << "];\n";
+            O << "    for (int k_ = threadIdx.x; k_ < nu" << m << "_; k_ += " << BS << ")\n";
+            O << "      for (int s_ = ro" << m << "[mb_][k_]; s_ < ro" << m << "[mb_][k_ + 1]; ++s_) tg" << m
+              << "[s_] = (unsigned short)k_;\n";
+        }
         for (size_t a = 0; a < S.args.size(); ++a) {
             if (st_arg[a] < 0 || S.args[a].d.access != OP2G_INC) continue;
             // slots of entries outside [start, end) are never stored: they add 0
             const int D = S.args[a].d.dim, r = st_arg[a];
-            O << "    for (int k_ = threadIdx.x; k_ < (int)ro" << r << "[nu" << r << "_] * " << D
+            O << "    for (int k_ = threadIdx.x; k_ < (int)ro" << r << "[mb_][nu" << r << "_] * " << D
               << "; k_ += " << BS << ") sv" << a << "[k_] = (" << ctype_of(S.args[a].d.dtype)
               << ")0;\n";
-        }
-        for (size_t a = 0; a < S.args.size(); ++a) {
-            if (st_arg[a] < 0 || S.args[a].d.access != OP2G_READ) continue;
-            const op2g_arg_desc &d = S.args[a].d;
-            const char *T = ctype_of(d.dtype);
-            const int D = d.dim, r = st_arg[a];
-            O << "    for (int k_ = threadIdx.x; k_ < nu" << r << "_ * " << D << "; k_ += " << BS
-              << ") {\n";
-            O << "      const int v_ = k_ / " << D << ";\n";
-            O << "      sv" << a << "[k_] = __ldg((const " << T << " *)p.ptr[" << S.args[a].slot
-              << "] + (long long)si" << r << "[v_] * " << gstride(a) << " + (k_ - v_ * " << D
-              << "));\n";
-            O << "    }\n";
         }
         O << "    __syncthreads();\n";
         O << "    for (long long it = c0_ + threadIdx.x; it < c1_; it += " << BS << ") {\n";
@@ -574,13 +706,25 @@ struct Gen {
               << ") {\n";
             O << "      const int v_ = k_ / " << D << ", j_ = k_ - v_ * " << D << ";\n";
             O << "      " << T << " s_ = (" << T << ")0;\n";
-            O << "      for (int q_ = ro" << r << "[v_]; q_ < ro" << r << "[v_ + 1]; ++q_) s_ += sv" << a
+            O << "      for (int q_ = ro" << r << "[mb_][v_]; q_ < ro" << r << "[mb_][v_ + 1]; ++q_) s_ += sv" << a
               << "[q_ * " << D << " + j_];\n";
             O << "      op2g::atomic_inc((" << T << " *)p.ptr[" << S.args[a].slot << "] + (long long)si"
-              << r << "[v_] * " << gstride(a) << " + j_, s_);\n";
+              << r << "[mb_][v_] * " << gstride(a) << " + j_, s_);\n";
             O << "    }\n";
         }
+        // this partition's plan buffer is refilled by bulk copy two partitions on
+        O << "    op2g::fence_proxy_async_smem();\n";
         O << "    __syncthreads();\n";
+        O << "    mb_ = mbn_;\n";
+        O << "    vb_ ^= 1;\n";
+        O << "  }\n";
+        O << "  op2g::cp_async_wait<0>();\n";
+        O << "  if (!ok_) {\n";
+        O << "    if (threadIdx.x == 0) op2g::set_err(p.err, OP2G_DEVERR_TIMEOUT);\n";
+        O << "    for (int b_ = 0; b_ < 3; ++b_)\n";
+        O << "      if (pend_[b_]) (void)op2g::mbar_wait(&bar_[b_], ph_[b_]);\n";
+        O << "    __syncthreads();\n";
+        O << "    return;\n";
         O << "  }\n";
         emit_global_reductions();
         O << "}\n\n";
@@ -633,6 +777,7 @@ struct Gen {
         O << "#include \"op2g_device.cuh\"\n";
         O << "#define OP2G_DEVERR_MAP_BOUNDS " << OP2G_DEVERR_MAP_BOUNDS << "\n";
         O << "#define OP2G_DEVERR_NEW_NONZERO " << OP2G_DEVERR_NEW_NONZERO << "\n";
+        O << "#define OP2G_DEVERR_TIMEOUT " << OP2G_DEVERR_TIMEOUT << "\n";
         O << "namespace op2g { __device__ __forceinline__ int rem(int a, int b) { return a < b ? a : a - b; } }\n";
         O << "#define restrict __restrict__\n";
         O << "// ---- user kernel ----\n";
@@ -954,10 +1099,16 @@ struct Gen {
             } else if (A.d.kind == OP2G_ARG_DAT) {
                 const int D = A.d.dim;
                 if (A.d.map < 0) {
-                    // direct: pointer into the Dat (pyop2/codegen/builder.py:367-377)
-                    kargs.push_back("op2g::ptr((" + std::string(T) + " *)p.ptr[" +
-                                    std::to_string(A.slot) + "] + n * " +
-                                    std::to_string(gstride(a)) + ")");
+                    // direct: pointer into the Dat (pyop2/codegen/builder.py:367-377);
+                    // in a staged wrapper a fetched READ argument is read from
+                    // its partition buffer in shared memory
+                    if (staging && st_dir[a])
+                        kargs.push_back("op2g::ptr((" + std::string(T) + " *)dv" + an +
+                                        "[vb_] + (n - c0_) * " + std::to_string(A.d.dim) + ")");
+                    else
+                        kargs.push_back("op2g::ptr((" + std::string(T) + " *)p.ptr[" +
+                                        std::to_string(A.slot) + "] + n * " +
+                                        std::to_string(gstride(a)) + ")");
                     continue;
                 }
                 const int ar = S.maps[A.d.map].arity;
@@ -981,7 +1132,7 @@ struct Gen {
                     O << J << "  const int q_ = l_ != 0xFFFF ? (int)tg" << st_arg[a] << "[l_] : -1;\n";
                     O << J << "#pragma unroll\n";
                     O << J << "  for (int j = 0; j < " << D << "; ++j) " << tn << "[" << po
-                      << "i * " << D << " + j] = q_ >= 0 ? sv" << a << "[q_ * " << D
+                      << "i * " << D << " + j] = q_ >= 0 ? sv" << a << "[vb_][q_ * " << D
                       << " + j] : (" << T << ")0;\n";
                     O << J << "}\n";
                 } else {

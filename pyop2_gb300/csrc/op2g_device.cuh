@@ -196,4 +196,67 @@ __device__ __forceinline__ long long bcsr_find(const long long *__restrict__ row
     return -1;
 }
 
+// ------------------------------------------------- asynchronous staging copies
+// Used by staged wrappers (OP2G_SCATTER_STAGED) to fetch the next
+// partitions' data while the current one computes: bulk copies (the TMA's
+// one-dimensional form) of contiguous plan segments completing on an
+// mbarrier, and per-element asynchronous copies (cp.async) of gathered
+// values, waited for by commit groups.
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Order this thread's earlier generic-proxy accesses of shared memory before
+// later asynchronous-proxy (bulk copy) accesses.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+// dst, src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                        unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+// Wait for phase `parity` of the mbarrier to complete, giving up after a
+// bounded number of tries (returns false then).
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+    const unsigned a = smem_addr(bar);
+    for (int it = 0; it < (1 << 20); ++it) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p_;\n mbarrier.try_wait.parity.shared::cta.b64 p_, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p_;\n}" : "=r"(done) : "r"(a), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *dst, const void *src) {
+    static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async moves 4, 8 or 16 bytes");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_addr(dst)), "l"(src),
+                 "n"(BYTES)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 }  // namespace op2g

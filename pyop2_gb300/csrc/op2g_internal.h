@@ -43,6 +43,7 @@ std::string generate_source(const Signature &S);
 // Staged wrappers (OP2G_SCATTER_STAGED): per argument the plain map whose
 // staging plan it uses, or -1; and the dynamic shared memory they take.
 std::vector<int> staged_args(const Signature &S);
+std::vector<bool> staged_direct(const Signature &S);
 size_t staged_smem_bytes(const Signature &S, int64_t block, const int32_t *max_unique);
 
 // Exclusive in-place prefix sum of d[0..n) on `st` (device memory); tmp holds

@@ -514,8 +514,7 @@ op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *
     if (st != OP2G_OK) return st;
     if (k->staged) {
         if (d->end <= d->start) return OP2G_OK;
-        // one CTA per mini-partition, up to 4 waves of resident CTAs (CTAs
-        // then take partitions in turn); the partitions' target lists and
+        // CTAs take mini-partitions in turn; the partitions' plan segments and
         // staged values take dynamic shared memory
         const size_t smem = staged_smem_bytes(k->sig, d->stage->block, d->stage->max_unique);
         Driver &D = driver();
@@ -541,7 +540,8 @@ op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *
         }
         const int64_t B = d->stage->block;
         const int64_t nparts = (d->end + B - 1) / B - d->start / B;
-        int64_t grid = d->grid > 0 ? d->grid : (int64_t)L->occ_at_smem * L->sms * 4;
+        // one resident wave: each CTA pipelines its partitions
+        int64_t grid = d->grid > 0 ? d->grid : (int64_t)L->occ_at_smem * L->sms;
         if (grid > nparts) grid = nparts;
         if (grid < 1) grid = 1;
         void *params[] = {buf};

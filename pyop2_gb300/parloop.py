@@ -969,7 +969,9 @@ class MapStagePlan:
                   ctypes.byref(mx), st)
         self.ind_map = torch.empty(max(total.value, 8), dtype=torch.int32, device=dev)
         self.run_off = torch.empty(max(total.value, 8), dtype=torch.int16, device=dev)
-        self.loc_map = torch.empty(max(n * ar, 4), dtype=torch.int16, device=dev)
+        # 16-byte bulk copies of a partition's slots may read up to 7 entries
+        # past the last one
+        self.loc_map = torch.empty(n * ar + 8, dtype=torch.int16, device=dev)
         _lib.call("op2g_stage_plan_fill", n, ar, vals.data_ptr(), block,
                   self.ind_off.data_ptr(), self.ind_map.data_ptr(), self.run_off.data_ptr(),
                   self.loc_map.data_ptr(), st)
@@ -1034,22 +1036,30 @@ def stage_plan(loop):
             m._cache[key] = mp
         plans[m._serial] = mp
     # shared memory of the staged wrapper (an upper bound of what it takes):
-    # per staged map its target list, run offsets and slot -> target table;
-    # per READ argument its values per target, per INC one value per slot
+    # per staged map three plan buffers (target list, run offsets, slots) and
+    # the slot -> target table; per READ argument two buffers of values per
+    # target, per INC argument one value per slot; per direct READ argument
+    # two buffers of the partition's values
     def r16(x):
         return (x + 15) // 16 * 16
     smem = 0
     for m in roots:
         mu = plans[m._serial].max_unique
-        smem += r16(mu * 4) + r16((mu + 1) * 2) + r16(block * m.arity * 2)
+        seg = (mu + 1 + 7) // 8 * 8
+        smem += 3 * (r16(seg * 4) + r16(seg * 2) + r16(block * m.arity * 2)) + \
+            r16(block * m.arity * 2)
     for a, group, _ in loop._flat:
-        if isinstance(a, DatLegacyArg) and a.map_ is not None and not group and \
-                a.access in (Access.READ, Access.INC):
-            m = a.map_.map_ if isinstance(a.map_, PermutedMap) else a.map_
-            if m._serial in plans:
-                rows = plans[m._serial].max_unique if a.access is Access.READ \
-                    else block * m.arity
-                smem += r16(rows * a.data.cdim * a.data.dtype.itemsize)
+        if not isinstance(a, DatLegacyArg) or group:
+            continue
+        size = a.data.cdim * a.data.dtype.itemsize
+        if a.map_ is None:
+            if a.access is Access.READ:
+                smem += 2 * r16(block * size)
+            continue
+        m = a.map_.map_ if isinstance(a.map_, PermutedMap) else a.map_
+        if m._serial in plans and a.access in (Access.READ, Access.INC):
+            smem += 2 * r16(plans[m._serial].max_unique * size) if a.access is Access.READ \
+                else r16(block * m.arity * size)
     if smem > _STAGE_SMEM_LIMIT:
         return None
     return StagePlan(plans, block)
