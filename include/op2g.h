@@ -105,7 +105,9 @@ enum {
                                   target in slot order, and each distinct target
                                   receives one global atomic per partition
                                   (non-extruded, non-indexed loops; the launch passes the
-                                  plan in op2g_launch_desc.stage)                        */
+                                  plan in op2g_launch_desc.stage; grid 0 = one resident
+                                  wave whose CTAs pipeline their partitions, -1 = one
+                                  CTA per partition)                                   */
 };
 
 #define OP2G_MAX_ARGS 32
@@ -215,6 +217,7 @@ int32_t op2g_kernel_num_regs(const op2g_kernel *k);
  * entry.  Built by op2g_stage_plan_count / _fill; all arrays on the device. */
 typedef struct op2g_stage_desc {
     int64_t block;
+    int64_t n;                          /* iterations the plan covers: [0, n)      */
     const int32_t *ind_map[OP2G_MAX_MAPS];
     const int64_t *ind_off[OP2G_MAX_MAPS];
     const int32_t *ind_num[OP2G_MAX_MAPS];

@@ -52,7 +52,7 @@ class LoopDesc(ctypes.Structure):
 
 
 class StageDesc(ctypes.Structure):
-    _fields_ = [("block", _i64), ("ind_map", _p * MAX_MAPS), ("ind_off", _p * MAX_MAPS),
+    _fields_ = [("block", _i64), ("n", _i64), ("ind_map", _p * MAX_MAPS), ("ind_off", _p * MAX_MAPS),
                 ("ind_num", _p * MAX_MAPS), ("run_off", _p * MAX_MAPS),
                 ("loc_map", _p * MAX_MAPS), ("max_unique", _i32 * MAX_MAPS)]
 

@@ -526,6 +526,31 @@ struct Gen {
         for (size_t m = 0; m < S.maps.size(); ++m)
             if (st_map[m]) ms.push_back((int)m);
         const int NSM = (int)ms.size();
+        // the slot -> target table of a staged map is filled only when an
+        // argument other than a staged INC goes through it (a staged READ
+        // needs its targets' values, any other argument the global targets)
+        std::vector<bool> need_tg(S.maps.size(), false);
+        for (size_t a = 0; a < S.args.size(); ++a) {
+            const op2g_arg_desc &d = S.args[a].d;
+            if (d.kind == OP2G_ARG_DAT && st_arg[a] >= 0 && d.access == OP2G_INC) continue;
+            auto mark = [&](int m) {
+                if (m < 0) return;
+                const int r = S.maps[m].kind == OP2G_MAP_PERMUTED ? S.maps[m].base : m;
+                if (st_map[r]) need_tg[r] = true;
+            };
+            if (d.kind == OP2G_ARG_DAT) mark(d.map);
+            if (d.kind == OP2G_ARG_MAT) {
+                mark(d.map);
+                mark(d.cmap);
+            }
+        }
+        for (size_t m = 0; m < S.maps.size(); ++m)
+            if (S.maps[m].kind == OP2G_MAP_COMPOSED)
+                for (int k = 0; k < S.maps[m].ncomposed; ++k) {
+                    const int c = S.maps[m].composed[k];
+                    const int r = S.maps[c].kind == OP2G_MAP_PERMUTED ? S.maps[c].base : c;
+                    if (st_map[r]) need_tg[r] = true;
+                }
         O << "__device__ __forceinline__ void op2g_run_staged(const op2g_params_t &p) {\n";
         O << "  extern __shared__ __align__(16) unsigned char op2g_smem[];\n";
         O << "  __shared__ __align__(8) unsigned long long bar_[3];\n";
@@ -676,22 +701,34 @@ struct Gen {
         O << "    const long long pbase_ = pb_ * p.sblock;\n";
         O << "    const long long c0_ = pbase_ > p.start ? pbase_ : p.start;\n";
         O << "    const long long c1_ = pbase_ + p.sblock < p.end ? pbase_ + p.sblock : p.end;\n";
+        bool fill = false;
         for (int i = 0; i < NSM; ++i) {
             const int m = ms[i];
             O << "    const int nu" << m << "_ = snu_[mb_][" << i << "];\n";
+            if (!need_tg[m]) continue;
+            fill = true;
             O << "    for (int k_ = threadIdx.x; k_ < nu" << m << "_; k_ += " << BS << ")\n";
             O << "      for (int s_ = ro" << m << "[mb_][k_]; s_ < ro" << m << "[mb_][k_ + 1]; ++s_) tg" << m
               << "[s_] = (unsigned short)k_;\n";
         }
-        for (size_t a = 0; a < S.args.size(); ++a) {
-            if (st_arg[a] < 0 || S.args[a].d.access != OP2G_INC) continue;
-            // slots of entries outside [start, end) are never stored: they add 0
-            const int D = S.args[a].d.dim, r = st_arg[a];
-            O << "    for (int k_ = threadIdx.x; k_ < (int)ro" << r << "[mb_][nu" << r << "_] * " << D
-              << "; k_ += " << BS << ") sv" << a << "[k_] = (" << ctype_of(S.args[a].d.dtype)
-              << ")0;\n";
+        bool zero = false;
+        for (size_t a = 0; a < S.args.size(); ++a)
+            zero = zero || (st_arg[a] >= 0 && S.args[a].d.access == OP2G_INC);
+        if (zero) {
+            // a partition cut by [start, end) leaves the slots of the entries
+            // outside unstored: they must add 0
+            O << "    const long long pe_ = pbase_ + p.sblock < p.sn ? pbase_ + p.sblock : p.sn;\n";
+            O << "    if (c0_ != pbase_ || c1_ != pe_) {\n";
+            for (size_t a = 0; a < S.args.size(); ++a) {
+                if (st_arg[a] < 0 || S.args[a].d.access != OP2G_INC) continue;
+                const int D = S.args[a].d.dim, r = st_arg[a];
+                O << "      for (int k_ = threadIdx.x; k_ < (int)ro" << r << "[mb_][nu" << r << "_] * " << D
+                  << "; k_ += " << BS << ") sv" << a << "[k_] = (" << ctype_of(S.args[a].d.dtype)
+                  << ")0;\n";
+            }
+            O << "    }\n";
         }
-        O << "    __syncthreads();\n";
+        if (fill || zero) O << "    __syncthreads();\n";
         O << "    for (long long it = c0_ + threadIdx.x; it < c1_; it += " << BS << ") {\n";
         O << "      const long long n = it;\n";
         emit_body("      ", false, false);
@@ -797,7 +834,7 @@ struct Gen {
         if (any_staged) {
             // the staging plan (op2g_stage_desc), one entry per map
             const int nm = nmaps > 0 ? nmaps : 1;
-            O << "  long long sblock;\n"
+            O << "  long long sblock, sn;\n"
               << "  long long smax[" << nm << "];\n"
               << "  const int *sind[" << nm << "];\n"
               << "  const long long *soff[" << nm << "];\n"

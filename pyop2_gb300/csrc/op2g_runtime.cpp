@@ -373,7 +373,7 @@ op2g_status op2g_kernel_create(const char *user_src, const char *kernel_name,
     k->param_bytes = 8 * (5 + (S.nptrs > 0 ? S.nptrs : 1) + (nmaps > 0 ? nmaps : 1));
     for (int r : staged_args(S))
         if (r >= 0) k->staged = true;
-    if (k->staged) k->param_bytes += 8 * (1 + 6 * (nmaps > 0 ? nmaps : 1));
+    if (k->staged) k->param_bytes += 8 * (2 + 6 * (nmaps > 0 ? nmaps : 1));
     op2g_status st = OP2G_OK;
     k->arch = (arch && *arch) ? std::string(arch) : current_arch(&st);
     if (st != OP2G_OK) {
@@ -446,12 +446,14 @@ op2g_status op2g_kernel_pack_params(const op2g_kernel *k, const op2g_launch_desc
     for (size_t m = 0; m < S.maps.size(); ++m)
         w[5 + np + m] = d->map_toset ? d->map_toset[m] : INT64_MAX;
     if (k->staged) {
-        // sblock, smax[nm], sind[nm], soff[nm], snum[nm], sruns[nm], sloc[nm]
+        // sblock, sn, smax[nm], sind[nm], soff[nm], snum[nm], sruns[nm], sloc[nm]
         const op2g_stage_desc *g = d->stage;
         if (!g || g->block <= 0) return fail(OP2G_ERR_INVALID, "staged wrapper launched without a plan");
         const int nm = S.maps.empty() ? 1 : (int)S.maps.size();
-        int64_t *x = w + 5 + np + nm;
-        x[0] = g->block;
+        if (d->end > g->n) return fail(OP2G_ERR_INVALID, "launch range beyond the staging plan");
+        int64_t *x = w + 5 + np + nm + 1;
+        x[-1] = g->block;
+        x[0] = g->n;
         std::vector<int> st = staged_args(S);
         for (size_t a = 0; a < st.size(); ++a) {
             const int m = st[a];
@@ -541,7 +543,8 @@ op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *
         const int64_t B = d->stage->block;
         const int64_t nparts = (d->end + B - 1) / B - d->start / B;
         // one resident wave: each CTA pipelines its partitions
-        int64_t grid = d->grid > 0 ? d->grid : (int64_t)L->occ_at_smem * L->sms;
+        int64_t grid = d->grid > 0 ? d->grid
+                       : d->grid < 0 ? nparts : (int64_t)L->occ_at_smem * L->sms;
         if (grid > nparts) grid = nparts;
         if (grid < 1) grid = 1;
         void *params[] = {buf};

@@ -985,9 +985,10 @@ class MapStagePlan:
 class StagePlan:
     """The staging plans of a loop's maps, all with one partition size."""
 
-    def __init__(self, plans, block):
+    def __init__(self, plans, block, n):
         self.plans = plans          # map serial -> MapStagePlan
         self.block = block
+        self.n = n                  # iterations covered
         self._descs = {}
 
     def desc(self, table):
@@ -997,6 +998,7 @@ class StagePlan:
         if d is None:
             d = _lib.StageDesc()
             d.block = self.block
+            d.n = self.n
             for i, obj in enumerate(table.objs):
                 mp = self.plans.get(obj._serial) if obj is not None else None
                 if mp is None:
@@ -1062,7 +1064,7 @@ def stage_plan(loop):
                 else r16(block * m.arity * size)
     if smem > _STAGE_SMEM_LIMIT:
         return None
-    return StagePlan(plans, block)
+    return StagePlan(plans, block, loop.iterset.size)
 
 
 # ------------------------------------------------------------ entry points

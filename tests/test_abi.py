@@ -49,7 +49,7 @@ STRUCTS = {
                                     "nc_reads"]),
     "op2g_launch_desc": ("LaunchDesc", ["start", "end", "layers", "indices", "err", "ptrs",
                                         "map_toset", "layers_per_entity", "grid", "stage"]),
-    "op2g_stage_desc": ("StageDesc", ["block", "ind_map", "ind_off", "ind_num", "run_off",
+    "op2g_stage_desc": ("StageDesc", ["block", "n", "ind_map", "ind_off", "ind_num", "run_off",
                                       "loc_map", "max_unique"]),
     "op2g_sparsity_pair": ("SparsityPair", ["rmap", "cmap", "rarity", "carity", "nent", "region",
                                             "nrcomposed", "nccomposed", "rcomposed", "ccomposed",
