@@ -1075,6 +1075,33 @@ def run_ours(args):
     return 0
 
 
+def scatter_pair(op2, n=N_CUBE, launches=2):
+    """The INC scatter loop y[map(e, i)] += w_e on the n^3 x 6 tet mesh,
+    `launches` times with hardware atomics, then `launches` times on the
+    staging plan (plan built before the first staged launch).  For one-kernel
+    profiler captures of the two forms."""
+    import torch
+    from pyop2_gb300 import _lib
+    from pyop2_gb300 import workloads as W
+    from pyop2_gb300.parloop import LegacyParloop
+    p = W.build_p1_3d(op2, n=n, seed=0)
+    cells, c2v, y = p["cells"], p["c2v"], p["y"]
+    w = op2.Dat(cells, np.random.default_rng(3).uniform(0, 1, cells.size))
+    K = op2.Kernel("static void sc(double *y, const double *w) "
+                   "{ for (int i = 0; i < 4; ++i) y[i] += w[0]; }", "sc")
+    la = LegacyParloop(K, cells, y(op2.INC, c2v), w(op2.READ))
+    la.build(_lib.SCATTER_ATOMIC)
+    ls = LegacyParloop(K, cells, y(op2.INC, c2v), w(op2.READ))
+    ls.build(_lib.SCATTER_STAGED)
+    ls.launch_desc()
+    torch.cuda.synchronize()
+    for lp in [la] * launches + [ls] * launches:
+        lp.compute()
+    torch.cuda.synchronize()
+    return {"cells": cells.size, "launches": 2 * launches,
+            "y_checksum": float(y.data_ro.sum())}
+
+
 def run_only(args):
     """One secondary measurement on its own (used for ncu captures); prints
     its JSON object."""
@@ -1093,6 +1120,8 @@ def run_only(args):
         out = measure_small(op2, with_cpu=False)
     elif args.only == "prism_assembly":
         out = measure_prism_assembly(op2, n=args.size or 256)
+    elif args.only == "scatter":
+        out = scatter_pair(op2, n=args.size or N_CUBE)
     else:
         out = measure_prisms(op2, args.steps, args.warmup, n=args.size or 256)
     print(json.dumps({"only": args.only, "result": out}), flush=True)
@@ -1112,7 +1141,7 @@ def main():
                     help="only the headline action (no adjoint / batch measurements)")
     ap.add_argument("--only", default=None,
                     choices=["sparsity", "adjoint", "batch", "prisms", "small",
-                             "prism_assembly"],
+                             "prism_assembly", "scatter"],
                     help="run one secondary measurement alone (profiling runs)")
     ap.add_argument("--size", type=int, default=None,
                     help="with --only: mesh size (cube edge / prism base edge)")
