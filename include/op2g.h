@@ -172,6 +172,12 @@ typedef struct op2g_loop_desc {
     int32_t nc_reads;          /* 1: READ Dat gathers use the read-only data path; the
                                   caller guarantees that no argument of the loop writes
                                   a Dat that a READ argument reads                      */
+    int32_t cells_per_thread;  /* > 1: each thread runs that many iterations per sweep
+                                  step, their gathers and arithmetic interleaved (an
+                                  iteration past the end recomputes the last one and
+                                  skips its unpack); loops with written direct or
+                                  passthrough arguments, warp or shared-memory scatter
+                                  or prefetch run one                                  */
 } op2g_loop_desc;
 
 typedef struct op2g_kernel op2g_kernel;

@@ -48,7 +48,8 @@ class LoopDesc(ctypes.Structure):
     _fields_ = [("extruded", _i32), ("constant_layers", _i32), ("extruded_periodic", _i32),
                 ("indexed", _i32), ("iteration_region", _i32), ("pass_layer_arg", _i32),
                 ("scatter", _i32), ("block_size", _i32), ("debug_checks", _i32),
-                ("batched", _i32), ("prefetch", _i32), ("nc_reads", _i32)]
+                ("batched", _i32), ("prefetch", _i32), ("nc_reads", _i32),
+                ("cells_per_thread", _i32)]
 
 
 class StageDesc(ctypes.Structure):

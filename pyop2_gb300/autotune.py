@@ -11,7 +11,7 @@ _CHOICES = {}
 
 
 def candidates(loop):
-    """(scatter, block size, prefetch, grid) tuples worth timing for this
+    """(scatter, block size, prefetch, grid[, cells per thread]) tuples worth timing for this
     loop: every INC strategy that applies (atomics, warp aggregation,
     shared-memory hash tables, colouring, a staging plan), three CTA sizes,
     for non-extruded
@@ -26,6 +26,9 @@ def candidates(loop):
             # staged partitions take their partition in turn; prefetch and the
             # grid policy do not apply
             out.append((_lib.SCATTER_STAGED, bs, 0, 0))
+        for grid in (0, -1):
+            # two cells per thread, interleaved (no prefetch)
+            out.append((_lib.SCATTER_ATOMIC, bs, 0, grid, 2))
         for pf in pfs:
             for grid in (0, -1):
                 out.append((_lib.SCATTER_ATOMIC, bs, pf, grid))
@@ -75,8 +78,8 @@ def choose(loop, reps=3):
         return cands[0]
     snaps = _snapshot(_written(loop))
     best = None
-    for sc, bs, pf, grid in cands:
-        loop.build(sc, bs, pf, grid)
+    for cand in cands:
+        loop.build(*cand)
         loop.compute()   # warm-up (and compilation, colouring plan)
         _restore(snaps)
         ev0 = torch.cuda.Event(enable_timing=True)
@@ -91,7 +94,7 @@ def choose(loop, reps=3):
             _restore(snaps)
         t = min(times)
         if best is None or t < best[0]:
-            best = (t, (sc, bs, pf, grid))
+            best = (t, tuple(cand))
     loop._built = None
     for o, t, s in snaps:
         if hasattr(o, "_m"):

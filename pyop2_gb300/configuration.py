@@ -32,6 +32,9 @@ class Configuration(dict):
         # staging plan: READ and INC data of each mini-partition in shared
         # memory at its distinct targets) or "auto" (autotuner)
         "scatter": ("OP2G_SCATTER", str, "atomic"),
+        # iterations each thread runs per sweep step, their gathers and
+        # arithmetic interleaved (1 or 2)
+        "cells_per_thread": ("OP2G_CELLS_PER_THREAD", int, 1),
         # iterations per mini-partition of a staging plan (at most 4096 / arity)
         "stage_cells": ("OP2G_STAGE_CELLS", int, 512),
         # threads per CTA of generated wrappers

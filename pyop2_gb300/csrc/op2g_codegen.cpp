@@ -205,6 +205,10 @@ struct Gen {
     std::vector<int> st_arg;
     std::vector<bool> st_map, st_dir;
     bool any_staged = false, staging = false;
+    // Several cells per thread per sweep step: iterations past the end run
+    // on a clamped (valid) iteration and only their unpack is skipped, so the
+    // cells' gathers and arithmetic can be interleaved by the compiler.
+    bool guard_unpack = false;
 
     explicit Gen(const Signature &s) : S(s) {
         nf = (S.loop.extruded && S.loop.iteration_region == OP2G_ON_INTERIOR_FACETS) ? 2 : 1;
@@ -920,9 +924,28 @@ struct Gen {
                 }
             O << "  __syncthreads();\n";
         }
-        O << "  for (long long base_ = i0_ + first; base_ < i1_; base_ += stride) {\n";
-        O << "    const long long it = base_ + threadIdx.x;\n";
-        O << "    const bool active = it < i1_;\n";
+        // Cells per thread: loops without written direct arguments (a clamped
+        // iteration would write them twice), passthrough arguments, warp or
+        // shared-memory scatter or map-row prefetch.
+        bool has_pass = false;
+        for (const ArgInfo &A : S.args) has_pass = has_pass || A.d.kind == OP2G_ARG_PASSTHROUGH;
+        const int cpt = (S.loop.cells_per_thread > 1 && !warp && !any_shared && !pf && !varlay &&
+                         !direct_written && !has_pass)
+                            ? S.loop.cells_per_thread
+                            : 1;
+        if (cpt > 1) {
+            guard_unpack = true;
+            O << "  for (long long base_ = i0_ + first; base_ < i1_; base_ += stride * " << cpt << ") {\n";
+            O << "#pragma unroll\n";
+            O << "   for (int c_ = 0; c_ < " << cpt << "; ++c_) {\n";
+            O << "    const long long ic_ = base_ + c_ * stride + threadIdx.x;\n";
+            O << "    const bool active = ic_ < i1_;\n";
+            O << "    const long long it = active ? ic_ : i1_ - 1;\n";
+        } else {
+            O << "  for (long long base_ = i0_ + first; base_ < i1_; base_ += stride) {\n";
+            O << "    const long long it = base_ + threadIdx.x;\n";
+            O << "    const bool active = it < i1_;\n";
+        }
         if (pf) {
             for (size_t m = 0; m < S.maps.size(); ++m)
                 if (rows[m])
@@ -947,7 +970,7 @@ struct Gen {
                 }
             }
         }
-        O << I << "if (active) {\n";
+        O << I << (cpt > 1 ? "{\n" : "if (active) {\n");
         std::string J = "      ";
         // entity / layer
         if (extr && !varlay) {
@@ -1024,7 +1047,9 @@ struct Gen {
             O << "    __syncthreads();\n";
             O << "    par_ ^= 1;\n";
         }
+        if (cpt > 1) O << "   }\n";  // cells of the step
         O << "  }\n";  // sweep loop
+        guard_unpack = false;
         emit_global_reductions();
         O << "}\n\n";
 
@@ -1208,6 +1233,7 @@ struct Gen {
         O << ");\n";
 
         // Unpacks (pyop2/codegen/builder.py:283-300, 386-410, 554-606)
+        if (guard_unpack) O << J << "if (active) {\n";
         for (size_t a = 0; a < S.args.size(); ++a) {
             const ArgInfo &A = S.args[a];
             const char *T = ctype_of(A.d.dtype);
@@ -1336,6 +1362,7 @@ struct Gen {
                 O << J << "}\n";
             }
         }
+        if (guard_unpack) O << J << "}\n";
     }
 };
 

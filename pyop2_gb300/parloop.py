@@ -547,10 +547,12 @@ class Parloop:
                 (read if a.access is Access.READ else written).add(id(owner))
         return not (read & written)
 
-    def _loop_desc(self, scatter, block_size, prefetch=None):
+    def _loop_desc(self, scatter, block_size, prefetch=None, cells=None):
         it = self.iterset
         if prefetch is None:
             prefetch = int(configuration["prefetch"])
+        if cells is None:
+            cells = int(configuration["cells_per_thread"])
         return dict(extruded=int(it._extruded),
                     constant_layers=int(bool(it._extruded and it.constant_layers)),
                     extruded_periodic=int(bool(it._extruded_periodic)),
@@ -560,7 +562,8 @@ class Parloop:
                     scatter=scatter, block_size=block_size,
                     debug_checks=int(bool(configuration["debug"])), batched=0,
                     prefetch=int(bool(prefetch) and not it._extruded),
-                    nc_reads=int(self._nc_reads()))
+                    nc_reads=int(self._nc_reads()),
+                    cells_per_thread=max(1, int(cells)))
 
     def _needs_conflict_handling(self):
         return any(isinstance(a, (DatLegacyArg, MatLegacyArg)) and
@@ -640,16 +643,20 @@ class Parloop:
         return signature_key(self.local_kernel.source, self.local_kernel.name,
                              self._loop_desc(scatter, block_size), argdescs, table.key())
 
-    def build(self, scatter=None, block_size=None, prefetch=None, grid=None):
+    def build(self, scatter=None, block_size=None, prefetch=None, grid=None, cells=None):
         """Compile the wrapper for this loop (idempotent per strategy).
-        ``grid`` is the launch's CTA policy (``op2g_launch_desc.grid``)."""
+        ``grid`` is the launch's CTA policy (``op2g_launch_desc.grid``),
+        ``cells`` the iterations a thread runs per sweep step."""
         if scatter is None:
-            scatter, block_size, prefetch, grid = self._choose_strategy()
+            choice = self._choose_strategy()
+            scatter, block_size, prefetch, grid = choice[:4]
+            if len(choice) > 4:
+                cells = choice[4]
         if block_size is None:
             block_size = int(configuration["block_size"])
         self._grid = int(configuration["grid"]) if grid is None else int(grid)
         table, argdescs = self._signature()
-        loop = self._loop_desc(scatter, block_size, prefetch)
+        loop = self._loop_desc(scatter, block_size, prefetch, cells)
         k = compile_signature(self.local_kernel.source, self.local_kernel.name, loop, argdescs,
                               table.key())
         device.require()

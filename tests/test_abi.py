@@ -46,7 +46,7 @@ STRUCTS = {
     "op2g_loop_desc": ("LoopDesc", ["extruded", "constant_layers", "extruded_periodic", "indexed",
                                     "iteration_region", "pass_layer_arg", "scatter",
                                     "block_size", "debug_checks", "batched", "prefetch",
-                                    "nc_reads"]),
+                                    "nc_reads", "cells_per_thread"]),
     "op2g_launch_desc": ("LaunchDesc", ["start", "end", "layers", "indices", "err", "ptrs",
                                         "map_toset", "layers_per_entity", "grid", "stage"]),
     "op2g_stage_desc": ("StageDesc", ["block", "n", "ind_map", "ind_off", "ind_num", "run_off",

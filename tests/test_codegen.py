@@ -204,3 +204,30 @@ def test_kernel_with_empty_parameter_list(op2, decl):
     assert "k();" in compile_loop(pl).source()
     pl2 = LegacyParloop(op2.Kernel("static void kk(double *x) { }", "kk"), cells, d(op2.READ, m))
     assert "kk(op2g::ptr(t0));" in compile_loop(pl2).source()
+
+
+@pytest.mark.parametrize("cells", [1, 2, 3])
+def test_cells_per_thread(op2, cells):
+    """Several cells per thread: the unpack (INC, Globals) is guarded,
+    the gathers and the call are not; loops with written direct arguments
+    fall back to one cell per thread."""
+    cells_, verts = op2.Set(8), op2.Set(10)
+    m = op2.Map(cells_, verts, 3, np.arange(24) % 10)
+    x, y = op2.Dat(verts ** 2), op2.Dat(verts)
+    g = op2.Global(1, 0.0)
+    k = op2.Kernel("static void k(double *y, const double *x, double *g) {}", "k")
+    pl = LegacyParloop(k, cells_, y(op2.INC, m), x(op2.READ, m), g(op2.MIN))
+    table, argdescs = pl._signature()
+    src = compile_signature(pl.local_kernel.source, "k", pl._loop_desc(_lib.SCATTER_ATOMIC, 256, 0, cells),
+                            argdescs, table.key(), arch="sm_103a").source()
+    if cells > 1:
+        assert "stride * %d" % cells in src and "i1_ - 1" in src and "if (active) {" in src
+    else:
+        assert "stride * " not in src
+    d = op2.Dat(cells_)
+    pl2 = LegacyParloop(op2.Kernel("static void k2(double *y, double *d) {}", "k2"), cells_,
+                        y(op2.INC, m), d(op2.WRITE))
+    table, argdescs = pl2._signature()
+    src2 = compile_signature(pl2.local_kernel.source, "k2", pl2._loop_desc(_lib.SCATTER_ATOMIC, 256, 0, cells),
+                             argdescs, table.key(), arch="sm_103a").source()
+    assert "stride * " not in src2

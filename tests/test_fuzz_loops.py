@@ -13,7 +13,7 @@ import fuzz_loops as F
 
 CPU_SEEDS = range(48)
 GPU_SEEDS = range(48)
-STRATEGIES = ["atomic", "warp", "colour", "shared", "staged"]
+STRATEGIES = ["atomic", "warp", "colour", "shared", "staged", "atomic_cells2"]
 
 
 def _equal(got, want):
@@ -58,10 +58,12 @@ def test_specs_cover_every_access_and_shape():
 @pytest.fixture(params=STRATEGIES)
 def strategy(request, gpu_op2):
     from pyop2_gb300.configuration import configuration
-    old = configuration["scatter"]
-    configuration["scatter"] = request.param
+    old = configuration["scatter"], configuration["cells_per_thread"]
+    # "atomic_cells2": hardware atomics, two cells per thread per sweep step
+    configuration["scatter"] = request.param.split("_")[0]
+    configuration["cells_per_thread"] = 2 if request.param.endswith("cells2") else 1
     yield request.param
-    configuration["scatter"] = old
+    configuration["scatter"], configuration["cells_per_thread"] = old
 
 
 @pytest.mark.gpu

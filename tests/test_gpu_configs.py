@@ -8,16 +8,18 @@ from pyop2_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
 
-STRATEGIES = ["atomic", "warp", "colour", "shared", "staged"]
+STRATEGIES = ["atomic", "warp", "colour", "shared", "staged", "atomic_cells2"]
 
 
 @pytest.fixture(params=STRATEGIES)
 def strategy(request, gpu_op2):
     from pyop2_gb300.configuration import configuration
-    old = configuration["scatter"]
-    configuration["scatter"] = request.param
+    old = configuration["scatter"], configuration["cells_per_thread"]
+    # "atomic_cells2": hardware atomics, two cells per thread per sweep step
+    configuration["scatter"] = request.param.split("_")[0]
+    configuration["cells_per_thread"] = 2 if request.param.endswith("cells2") else 1
     yield request.param
-    configuration["scatter"] = old
+    configuration["scatter"], configuration["cells_per_thread"] = old
 
 
 def relerr(a, b):
