@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <climits>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -997,6 +998,124 @@ unsigned grid_for(long long n, int bs) {
 
 // Launch k_spmv_bsr with more than the default 48 KB of dynamic shared
 // memory (the attribute is set once per instantiation and size).
+// Asynchronous global -> shared copies of 4 or 8 bytes (cp.async), waited
+// for by commit groups.
+template <int BYTES>
+__device__ __forceinline__ void cpa(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src), "n"(BYTES)
+                 : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Blocks of R x C (R, C > 1): one lane per block row.  A warp owns 32
+// consecutive block rows and walks them in column slices of K blocks: for
+// slice k every row's blocks [k K, k K + K) (a contiguous run of K R C
+// values) are copied into the warp's shared memory with cp.async -- one run
+// per instruction, 32 consecutive doubles per instruction -- while the lanes
+// sum the previous slice from the other buffer.  Each lane then reads its own
+// run (row stride ST, odd, so the 32 lanes hit distinct banks) and does R C
+// FMAs per block into R accumulators: every FMA instruction is a full warp
+// of useful work, the FP64 pipe's measure on this GPU.
+template <int R, int C, int K>
+__global__ void __launch_bounds__(256)
+    k_spmv_bsr_lane(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
+    constexpr int BS = R * C;
+    constexpr int ST = (K * BS) | 1;
+    extern __shared__ double sbuf[];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    double *vb = sbuf + (size_t)wib * (2 * 32 * ST + 32 * K);  // [2][32][ST] values
+    int *cb = (int *)(vb + 2 * 32 * ST);                       // [2][32][K] columns
+    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long r0 = ((long long)blockIdx.x * (blockDim.x >> 5) + wib) * 32; r0 < m.nrows;
+         r0 += nwarps * 32) {
+        const long long r = r0 + lane;
+        long long q0 = 0, q1 = 0;
+        if (r < m.nrows) {
+            q0 = __ldg(m.rowptr + r);
+            q1 = __ldg(m.rowptr + r + 1);
+        }
+        const int len = (int)(q1 - q0);
+        const int nsteps = ((int)__reduce_max_sync(full, (unsigned)len) + K - 1) / K;
+        double acc[R];
+#pragma unroll
+        for (int i = 0; i < R; ++i) acc[i] = 0.0;
+        auto issue = [&](int k, int buf) {
+            double *dv = vb + buf * 32 * ST;
+            int *dc = cb + buf * 32 * K;
+            for (int sg = 0; sg < 32; ++sg) {
+                const long long b0 = __shfl_sync(full, q0, sg) + (long long)k * K;
+                const long long e0 = __shfl_sync(full, q1, sg);
+                const int ns = e0 - b0 >= K ? K : (e0 > b0 ? (int)(e0 - b0) : 0);
+                const double *src = m.values + b0 * BS;
+                for (int j = lane; j < ns * BS; j += 32) cpa<8>(dv + sg * ST + j, src + j);
+                if (lane < ns) cpa<4>(dc + sg * K + lane, m.colidx + b0 + lane);
+            }
+        };
+        if (nsteps > 0) issue(0, 0);
+        cpa_commit();
+        for (int k = 0; k < nsteps; ++k) {
+            if (k + 1 < nsteps) issue(k + 1, (k + 1) & 1);
+            cpa_commit();
+            cpa_wait<1>();  // slice k has landed
+            __syncwarp();
+            const double *sv = vb + (k & 1) * 32 * ST + lane * ST;
+            const int *sc = cb + (k & 1) * 32 * K + lane * K;
+            const int rest = len - k * K;
+            const int nb = rest >= K ? K : (rest > 0 ? rest : 0);
+            for (int b = 0; b < nb; ++b) {
+                const long long col = sc[b];
+                double xv[C];
+#pragma unroll
+                for (int j = 0; j < C; ++j) xv[j] = __ldg(x + col * C + j);
+#pragma unroll
+                for (int i = 0; i < R; ++i)
+#pragma unroll
+                    for (int j = 0; j < C; ++j) acc[i] = fma(sv[b * BS + i * C + j], xv[j], acc[i]);
+            }
+            __syncwarp();  // buffer k & 1 is refilled for slice k + 2
+        }
+        cpa_wait<0>();
+        if (r < m.nrows) {
+#pragma unroll
+            for (int i = 0; i < R; ++i) y[r * R + i] = acc[i];
+        }
+    }
+}
+
+template <int R, int C, int K>
+cudaError_t spmv_lane_launch(cudaStream_t st, const op2g_bcsr &m, const double *x, double *y) {
+    constexpr int BS = R * C, ST = (K * BS) | 1, T = 256;
+    const size_t smem = (size_t)(T / 32) * (2 * 32 * ST + 32 * K) * sizeof(double);
+    static int granted = -1;   // device whose attribute is set
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (granted != dev) {
+        e = cudaFuncSetAttribute(k_spmv_bsr_lane<R, C, K>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        granted = dev;
+    }
+    int occ = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_spmv_bsr_lane<R, C, K>, T, smem);
+    if (e != cudaSuccess) return e;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long warps = (m.nrows + 31) / 32;
+    long long g = (long long)(occ > 0 ? occ : 1) * (sms > 0 ? sms : 1);
+    const long long need = (warps + T / 32 - 1) / (T / 32);
+    if (g > need) g = need;
+    if (g < 1) g = 1;
+    k_spmv_bsr_lane<R, C, K><<<(unsigned)g, T, smem, st>>>(m, x, y);
+    return cudaGetLastError();
+}
+
 template <int RT, int CT>
 cudaError_t spmv_launch(unsigned grid, size_t smem, cudaStream_t st, const op2g_bcsr &m,
                         const double *x, double *y) {
@@ -1062,7 +1181,19 @@ op2g_status op2g_mat_spmv(const op2g_bcsr *m, const double *x, double *y, int32_
         const long long ctas = (m->nrows + SPMV_T / r - 1) / (SPMV_T / r);
         const unsigned g = grid_for(ctas * SPMV_T, SPMV_T);
         cudaError_t e;
-        if (r == 2 && c == 2)
+        static const int lane_k = [] {
+            const char *v = getenv("OP2G_SPMV_K");
+            return v ? atoi(v) : 2;
+        }();
+        if (r == 3 && c == 3 && lane_k == 1)
+            e = spmv_lane_launch<3, 3, 1>(st, *m, x, y);
+        else if (r == 3 && c == 3 && lane_k == 2)
+            e = spmv_lane_launch<3, 3, 2>(st, *m, x, y);
+        else if (r == 3 && c == 3 && lane_k == 4)
+            e = spmv_lane_launch<3, 3, 4>(st, *m, x, y);
+        else if (r == 2 && c == 2 && lane_k > 0)
+            e = spmv_lane_launch<2, 2, 4>(st, *m, x, y);
+        else if (r == 2 && c == 2)
             e = spmv_launch<2, 2>(g, smem, st, *m, x, y);
         else if (r == 3 && c == 3)
             e = spmv_launch<3, 3>(g, smem, st, *m, x, y);
