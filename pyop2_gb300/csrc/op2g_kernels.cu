@@ -15,7 +15,6 @@
 #include <cuda_runtime.h>
 
 #include <climits>
-#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -1013,16 +1012,17 @@ __device__ __forceinline__ void cpa_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Blocks of R x C (R, C > 1): one lane per block row.  A warp owns 32
-// consecutive block rows and walks them in column slices of K blocks: for
-// slice k every row's blocks [k K, k K + K) (a contiguous run of K R C
-// values) are copied into the warp's shared memory with cp.async -- one run
-// per instruction, 32 consecutive doubles per instruction -- while the lanes
-// sum the previous slice from the other buffer.  Each lane then reads its own
-// run (row stride ST, odd, so the 32 lanes hit distinct banks) and does R C
-// FMAs per block into R accumulators: every FMA instruction is a full warp
-// of useful work, the FP64 pipe's measure on this GPU.
-template <int R, int C, int K>
+// Blocks of R x C: one lane per block row.  A warp owns 32 consecutive
+// block rows and walks them in column slices of K blocks: for slice k every
+// row's blocks [k K, k K + K) (a contiguous run of K R C values) are copied
+// into the warp's shared memory with cp.async -- one run per copy
+// instruction, 32 consecutive doubles each -- with NB = 2 while the lanes sum
+// the previous slice from the other buffer, with NB = 1 (less shared memory,
+// more resident warps) before they sum it.  Each lane then reads its own run
+// (row stride ST, odd, so the 32 lanes hit distinct banks) and does R C FMAs
+// per block into R accumulators: every FMA instruction is a full warp of
+// useful work, the FP64 pipe's measure on this GPU.
+template <int R, int C, int K, int NB>
 __global__ void __launch_bounds__(256)
     k_spmv_bsr_lane(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
     constexpr int BS = R * C;
@@ -1030,8 +1030,8 @@ __global__ void __launch_bounds__(256)
     extern __shared__ double sbuf[];
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    double *vb = sbuf + (size_t)wib * (2 * 32 * ST + 32 * K);  // [2][32][ST] values
-    int *cb = (int *)(vb + 2 * 32 * ST);                       // [2][32][K] columns
+    double *vb = sbuf + (size_t)wib * (NB * 32 * ST + 16 * NB * K);  // [NB][32][ST] values
+    int *cb = (int *)(vb + NB * 32 * ST);                            // [NB][32][K] columns
     const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long r0 = ((long long)blockIdx.x * (blockDim.x >> 5) + wib) * 32; r0 < m.nrows;
          r0 += nwarps * 32) {
@@ -1058,15 +1058,22 @@ __global__ void __launch_bounds__(256)
                 if (lane < ns) cpa<4>(dc + sg * K + lane, m.colidx + b0 + lane);
             }
         };
-        if (nsteps > 0) issue(0, 0);
-        cpa_commit();
+        if (NB == 2 && nsteps > 0) issue(0, 0);
+        if (NB == 2) cpa_commit();
         for (int k = 0; k < nsteps; ++k) {
-            if (k + 1 < nsteps) issue(k + 1, (k + 1) & 1);
-            cpa_commit();
-            cpa_wait<1>();  // slice k has landed
+            const int bk = NB == 2 ? (k & 1) : 0;
+            if (NB == 2) {
+                if (k + 1 < nsteps) issue(k + 1, (k + 1) & 1);
+                cpa_commit();
+                cpa_wait<1>();  // slice k has landed
+            } else {
+                issue(k, 0);
+                cpa_commit();
+                cpa_wait<0>();
+            }
             __syncwarp();
-            const double *sv = vb + (k & 1) * 32 * ST + lane * ST;
-            const int *sc = cb + (k & 1) * 32 * K + lane * K;
+            const double *sv = vb + bk * 32 * ST + lane * ST;
+            const int *sc = cb + bk * 32 * K + lane * K;
             const int rest = len - k * K;
             const int nb = rest >= K ? K : (rest > 0 ? rest : 0);
             for (int b = 0; b < nb; ++b) {
@@ -1079,7 +1086,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
                     for (int j = 0; j < C; ++j) acc[i] = fma(sv[b * BS + i * C + j], xv[j], acc[i]);
             }
-            __syncwarp();  // buffer k & 1 is refilled for slice k + 2
+            __syncwarp();  // this buffer is refilled for a later slice
         }
         cpa_wait<0>();
         if (r < m.nrows) {
@@ -1089,22 +1096,22 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-template <int R, int C, int K>
+template <int R, int C, int K, int NB>
 cudaError_t spmv_lane_launch(cudaStream_t st, const op2g_bcsr &m, const double *x, double *y) {
     constexpr int BS = R * C, ST = (K * BS) | 1, T = 256;
-    const size_t smem = (size_t)(T / 32) * (2 * 32 * ST + 32 * K) * sizeof(double);
+    const size_t smem = (size_t)(T / 32) * (NB * 32 * ST + 16 * NB * K) * sizeof(double);
     static int granted = -1;   // device whose attribute is set
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (granted != dev) {
-        e = cudaFuncSetAttribute(k_spmv_bsr_lane<R, C, K>,
+        e = cudaFuncSetAttribute(k_spmv_bsr_lane<R, C, K, NB>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         granted = dev;
     }
     int occ = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_spmv_bsr_lane<R, C, K>, T, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_spmv_bsr_lane<R, C, K, NB>, T, smem);
     if (e != cudaSuccess) return e;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long warps = (m.nrows + 31) / 32;
@@ -1112,7 +1119,7 @@ cudaError_t spmv_lane_launch(cudaStream_t st, const op2g_bcsr &m, const double *
     const long long need = (warps + T / 32 - 1) / (T / 32);
     if (g > need) g = need;
     if (g < 1) g = 1;
-    k_spmv_bsr_lane<R, C, K><<<(unsigned)g, T, smem, st>>>(m, x, y);
+    k_spmv_bsr_lane<R, C, K, NB><<<(unsigned)g, T, smem, st>>>(m, x, y);
     return cudaGetLastError();
 }
 
@@ -1181,22 +1188,13 @@ op2g_status op2g_mat_spmv(const op2g_bcsr *m, const double *x, double *y, int32_
         const long long ctas = (m->nrows + SPMV_T / r - 1) / (SPMV_T / r);
         const unsigned g = grid_for(ctas * SPMV_T, SPMV_T);
         cudaError_t e;
-        static const int lane_k = [] {
-            const char *v = getenv("OP2G_SPMV_K");
-            return v ? atoi(v) : 2;
-        }();
-        if (r == 3 && c == 3 && lane_k == 1)
-            e = spmv_lane_launch<3, 3, 1>(st, *m, x, y);
-        else if (r == 3 && c == 3 && lane_k == 2)
-            e = spmv_lane_launch<3, 3, 2>(st, *m, x, y);
-        else if (r == 3 && c == 3 && lane_k == 4)
-            e = spmv_lane_launch<3, 3, 4>(st, *m, x, y);
-        else if (r == 2 && c == 2 && lane_k > 0)
-            e = spmv_lane_launch<2, 2, 4>(st, *m, x, y);
+        // 3x3 blocks: one lane per block row, four-block slices (measured on
+        // the prism BAIJ matrix: 3.37 ms against 3.64 ms for the tiled kernel;
+        // two-buffered slices of one, two or four blocks 3.44, 5.10, 6.16 ms)
+        if (r == 3 && c == 3)
+            e = spmv_lane_launch<3, 3, 4, 1>(st, *m, x, y);
         else if (r == 2 && c == 2)
             e = spmv_launch<2, 2>(g, smem, st, *m, x, y);
-        else if (r == 3 && c == 3)
-            e = spmv_launch<3, 3>(g, smem, st, *m, x, y);
         else
             e = spmv_launch<0, 0>(g, smem, st, *m, x, y);
         CK(e);
