@@ -1012,17 +1012,16 @@ __device__ __forceinline__ void cpa_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Blocks of R x C: one lane per block row.  A warp owns 32 consecutive
-// block rows and walks them in column slices of K blocks: for slice k every
-// row's blocks [k K, k K + K) (a contiguous run of K R C values) are copied
-// into the warp's shared memory with cp.async -- one run per copy
-// instruction, 32 consecutive doubles each -- with NB = 2 while the lanes sum
-// the previous slice from the other buffer, with NB = 1 (less shared memory,
-// more resident warps) before they sum it.  Each lane then reads its own run
-// (row stride ST, odd, so the 32 lanes hit distinct banks) and does R C FMAs
-// per block into R accumulators: every FMA instruction is a full warp of
-// useful work, the FP64 pipe's measure on this GPU.
-template <int R, int C, int K, int NB>
+// Blocks of R x C: one lane per block row, so every FMA instruction is a
+// full warp of useful work (the FP64 pipe's measure on this GPU) and no
+// lanes' sums are combined.  A warp owns 32 consecutive block rows and walks
+// them in column slices of K blocks: for slice k each lane copies its own
+// row's blocks [k K, k K + K) (a contiguous run of K R C values, and their
+// column indices) into the warp's shared memory with cp.async, gathers the
+// x entries of the slice's blocks (all in flight together), then does R C
+// FMAs per block into R accumulators from its run (row stride ST, odd, so
+// the 32 lanes hit distinct banks).
+template <int R, int C, int K>
 __global__ void __launch_bounds__(256)
     k_spmv_bsr_lane(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
     constexpr int BS = R * C;
@@ -1030,8 +1029,8 @@ __global__ void __launch_bounds__(256)
     extern __shared__ double sbuf[];
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    double *vb = sbuf + (size_t)wib * (NB * 32 * ST + 16 * NB * K);  // [NB][32][ST] values
-    int *cb = (int *)(vb + NB * 32 * ST);                            // [NB][32][K] columns
+    double *sv = sbuf + (size_t)wib * (32 * ST + 16 * K) + lane * ST;  // this lane's run
+    int *sc = (int *)(sbuf + (size_t)wib * (32 * ST + 16 * K) + 32 * ST) + lane * K;
     const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long r0 = ((long long)blockIdx.x * (blockDim.x >> 5) + wib) * 32; r0 < m.nrows;
          r0 += nwarps * 32) {
@@ -1046,49 +1045,35 @@ __global__ void __launch_bounds__(256)
         double acc[R];
 #pragma unroll
         for (int i = 0; i < R; ++i) acc[i] = 0.0;
-        auto issue = [&](int k, int buf) {
-            double *dv = vb + buf * 32 * ST;
-            int *dc = cb + buf * 32 * K;
-            for (int sg = 0; sg < 32; ++sg) {
-                const long long b0 = __shfl_sync(full, q0, sg) + (long long)k * K;
-                const long long e0 = __shfl_sync(full, q1, sg);
-                const int ns = e0 - b0 >= K ? K : (e0 > b0 ? (int)(e0 - b0) : 0);
-                const double *src = m.values + b0 * BS;
-                for (int j = lane; j < ns * BS; j += 32) cpa<8>(dv + sg * ST + j, src + j);
-                if (lane < ns) cpa<4>(dc + sg * K + lane, m.colidx + b0 + lane);
-            }
-        };
-        if (NB == 2 && nsteps > 0) issue(0, 0);
-        if (NB == 2) cpa_commit();
         for (int k = 0; k < nsteps; ++k) {
-            const int bk = NB == 2 ? (k & 1) : 0;
-            if (NB == 2) {
-                if (k + 1 < nsteps) issue(k + 1, (k + 1) & 1);
-                cpa_commit();
-                cpa_wait<1>();  // slice k has landed
-            } else {
-                issue(k, 0);
-                cpa_commit();
-                cpa_wait<0>();
-            }
+            const long long b0 = q0 + (long long)k * K;
+            const int nb = q1 - b0 >= K ? K : (q1 > b0 ? (int)(q1 - b0) : 0);
+            const double *src = m.values + b0 * BS;
+            for (int j = 0; j < nb * BS; ++j) cpa<8>(sv + j, src + j);
+            for (int j = 0; j < nb; ++j) cpa<4>(sc + j, m.colidx + b0 + j);
+            cpa_commit();
+            cpa_wait<0>();
             __syncwarp();
-            const double *sv = vb + bk * 32 * ST + lane * ST;
-            const int *sc = cb + bk * 32 * K + lane * K;
-            const int rest = len - k * K;
-            const int nb = rest >= K ? K : (rest > 0 ? rest : 0);
-            for (int b = 0; b < nb; ++b) {
-                const long long col = sc[b];
-                double xv[C];
+            // the slice's x entries first (all in flight together), then the FMAs
+            double xv[K][C];
 #pragma unroll
-                for (int j = 0; j < C; ++j) xv[j] = __ldg(x + col * C + j);
+            for (int b = 0; b < K; ++b) {
+                const long long col = b < nb ? sc[b] : 0;
 #pragma unroll
-                for (int i = 0; i < R; ++i)
-#pragma unroll
-                    for (int j = 0; j < C; ++j) acc[i] = fma(sv[b * BS + i * C + j], xv[j], acc[i]);
+                for (int j = 0; j < C; ++j) xv[b][j] = b < nb ? __ldg(x + col * C + j) : 0.0;
             }
-            __syncwarp();  // this buffer is refilled for a later slice
+#pragma unroll
+            for (int b = 0; b < K; ++b) {
+                if (b < nb) {
+#pragma unroll
+                    for (int i = 0; i < R; ++i)
+#pragma unroll
+                        for (int j = 0; j < C; ++j)
+                            acc[i] = fma(sv[b * BS + i * C + j], xv[b][j], acc[i]);
+                }
+            }
+            __syncwarp();  // the run is refilled for the next slice
         }
-        cpa_wait<0>();
         if (r < m.nrows) {
 #pragma unroll
             for (int i = 0; i < R; ++i) y[r * R + i] = acc[i];
@@ -1096,22 +1081,22 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-template <int R, int C, int K, int NB>
+template <int R, int C, int K>
 cudaError_t spmv_lane_launch(cudaStream_t st, const op2g_bcsr &m, const double *x, double *y) {
     constexpr int BS = R * C, ST = (K * BS) | 1, T = 256;
-    const size_t smem = (size_t)(T / 32) * (NB * 32 * ST + 16 * NB * K) * sizeof(double);
+    const size_t smem = (size_t)(T / 32) * (32 * ST + 16 * K) * sizeof(double);
     static int granted = -1;   // device whose attribute is set
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (granted != dev) {
-        e = cudaFuncSetAttribute(k_spmv_bsr_lane<R, C, K, NB>,
+        e = cudaFuncSetAttribute(k_spmv_bsr_lane<R, C, K>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         granted = dev;
     }
     int occ = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_spmv_bsr_lane<R, C, K, NB>, T, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_spmv_bsr_lane<R, C, K>, T, smem);
     if (e != cudaSuccess) return e;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long warps = (m.nrows + 31) / 32;
@@ -1119,7 +1104,7 @@ cudaError_t spmv_lane_launch(cudaStream_t st, const op2g_bcsr &m, const double *
     const long long need = (warps + T / 32 - 1) / (T / 32);
     if (g > need) g = need;
     if (g < 1) g = 1;
-    k_spmv_bsr_lane<R, C, K, NB><<<(unsigned)g, T, smem, st>>>(m, x, y);
+    k_spmv_bsr_lane<R, C, K><<<(unsigned)g, T, smem, st>>>(m, x, y);
     return cudaGetLastError();
 }
 
@@ -1188,11 +1173,10 @@ op2g_status op2g_mat_spmv(const op2g_bcsr *m, const double *x, double *y, int32_
         const long long ctas = (m->nrows + SPMV_T / r - 1) / (SPMV_T / r);
         const unsigned g = grid_for(ctas * SPMV_T, SPMV_T);
         cudaError_t e;
-        // 3x3 blocks: one lane per block row, four-block slices (measured on
-        // the prism BAIJ matrix: 3.37 ms against 3.64 ms for the tiled kernel;
-        // two-buffered slices of one, two or four blocks 3.44, 5.10, 6.16 ms)
+        // 3x3 blocks: one lane per block row, four-block slices (prism BAIJ
+        // matrix: 2.02 ms, against 3.64 ms for the tiled kernel)
         if (r == 3 && c == 3)
-            e = spmv_lane_launch<3, 3, 4, 1>(st, *m, x, y);
+            e = spmv_lane_launch<3, 3, 4>(st, *m, x, y);
         else if (r == 2 && c == 2)
             e = spmv_launch<2, 2>(g, smem, st, *m, x, y);
         else
