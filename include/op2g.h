@@ -175,9 +175,9 @@ typedef struct op2g_loop_desc {
     int32_t cells_per_thread;  /* > 1: each thread runs that many iterations per sweep
                                   step, their gathers and arithmetic interleaved (an
                                   iteration past the end recomputes the last one and
-                                  skips its unpack); loops with written direct or
-                                  passthrough arguments, warp or shared-memory scatter
-                                  or prefetch run one                                  */
+                                  skips its unpack); loops with direct RW/INC/MIN/MAX
+                                  or passthrough arguments, warp or shared-memory
+                                  scatter or prefetch run one                          */
 } op2g_loop_desc;
 
 typedef struct op2g_kernel op2g_kernel;

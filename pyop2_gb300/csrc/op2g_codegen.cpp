@@ -924,13 +924,19 @@ struct Gen {
                 }
             O << "  __syncthreads();\n";
         }
-        // Cells per thread: loops without written direct arguments (a clamped
-        // iteration would write them twice), passthrough arguments, warp or
-        // shared-memory scatter or map-row prefetch.
-        bool has_pass = false;
-        for (const ArgInfo &A : S.args) has_pass = has_pass || A.d.kind == OP2G_ARG_PASSTHROUGH;
+        // Cells per thread: loops without direct RW/INC/MIN/MAX arguments (a
+        // clamped iteration reruns the last one, which for a direct WRITE
+        // argument stores the same values again, but would apply an update
+        // twice), passthrough arguments, warp or shared-memory scatter or
+        // map-row prefetch.
+        bool has_pass = false, direct_update = false;
+        for (const ArgInfo &A : S.args) {
+            has_pass = has_pass || A.d.kind == OP2G_ARG_PASSTHROUGH;
+            direct_update = direct_update || (A.d.kind == OP2G_ARG_DAT && A.d.map < 0 &&
+                                              A.d.access != OP2G_READ && A.d.access != OP2G_WRITE);
+        }
         const int cpt = (S.loop.cells_per_thread > 1 && !warp && !any_shared && !pf && !varlay &&
-                         !direct_written && !has_pass)
+                         !direct_update && !has_pass)
                             ? S.loop.cells_per_thread
                             : 1;
         if (cpt > 1) {

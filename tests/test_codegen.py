@@ -209,8 +209,9 @@ def test_kernel_with_empty_parameter_list(op2, decl):
 @pytest.mark.parametrize("cells", [1, 2, 3])
 def test_cells_per_thread(op2, cells):
     """Several cells per thread: the unpack (INC, Globals) is guarded,
-    the gathers and the call are not; loops with written direct arguments
-    fall back to one cell per thread."""
+    the gathers and the call are not; loops that update a direct argument
+    (RW, INC) fall back to one cell per thread, direct WRITE arguments do not
+    (the rerun last iteration stores the same values)."""
     cells_, verts = op2.Set(8), op2.Set(10)
     m = op2.Map(cells_, verts, 3, np.arange(24) % 10)
     x, y = op2.Dat(verts ** 2), op2.Dat(verts)
@@ -225,9 +226,11 @@ def test_cells_per_thread(op2, cells):
     else:
         assert "stride * " not in src
     d = op2.Dat(cells_)
-    pl2 = LegacyParloop(op2.Kernel("static void k2(double *y, double *d) {}", "k2"), cells_,
-                        y(op2.INC, m), d(op2.WRITE))
-    table, argdescs = pl2._signature()
-    src2 = compile_signature(pl2.local_kernel.source, "k2", pl2._loop_desc(_lib.SCATTER_ATOMIC, 256, 0, cells),
-                             argdescs, table.key(), arch="sm_103a").source()
-    assert "stride * " not in src2
+    for acc, multi in ((op2.WRITE, cells > 1), (op2.RW, False), (op2.INC, False)):
+        pl2 = LegacyParloop(op2.Kernel("static void k2(double *y, double *d) {}", "k2"), cells_,
+                            y(op2.INC, m), d(acc))
+        table, argdescs = pl2._signature()
+        src2 = compile_signature(pl2.local_kernel.source, "k2",
+                                 pl2._loop_desc(_lib.SCATTER_ATOMIC, 256, 0, cells),
+                                 argdescs, table.key(), arch="sm_103a").source()
+        assert ("stride * " in src2) == multi
