@@ -209,6 +209,7 @@ struct Gen {
     // on a clamped (valid) iteration and only their unpack is skipped, so the
     // cells' gathers and arithmetic can be interleaved by the compiler.
     bool guard_unpack = false;
+    int cells_per_thread = 1;  // what the sweep loop was generated with
 
     explicit Gen(const Signature &s) : S(s) {
         nf = (S.loop.extruded && S.loop.iteration_region == OP2G_ON_INTERIOR_FACETS) ? 2 : 1;
@@ -939,6 +940,7 @@ struct Gen {
                          !direct_update && !has_pass)
                             ? S.loop.cells_per_thread
                             : 1;
+        cells_per_thread = cpt;
         if (cpt > 1) {
             guard_unpack = true;
             O << "  for (long long base_ = i0_ + first; base_ < i1_; base_ += stride * " << cpt << ") {\n";
@@ -1479,9 +1481,11 @@ std::string validate_signature(const Signature &S) {
     return "";
 }
 
-std::string generate_source(const Signature &S) {
+std::string generate_source(const Signature &S, int *cells_per_thread) {
     Gen g(S);
-    return g.emit();
+    std::string src = g.emit();
+    if (cells_per_thread) *cells_per_thread = g.cells_per_thread;
+    return src;
 }
 
 }  // namespace op2g

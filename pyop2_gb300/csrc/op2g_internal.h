@@ -39,7 +39,9 @@ struct Signature {
 };
 
 std::string validate_signature(const Signature &S);
-std::string generate_source(const Signature &S);
+// The wrapper's source; *cells_per_thread (may be NULL) receives the
+// iterations a thread runs per sweep step in it.
+std::string generate_source(const Signature &S, int *cells_per_thread = nullptr);
 // Staged wrappers (OP2G_SCATTER_STAGED): per argument the plain map whose
 // staging plan it uses, or -1; and the dynamic shared memory they take.
 std::vector<int> staged_args(const Signature &S);

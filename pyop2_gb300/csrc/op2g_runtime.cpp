@@ -288,6 +288,7 @@ struct op2g_kernel {
     std::map<int, Loaded> per_dev;
     int param_bytes = 0;
     bool staged = false;   // the wrapper stages arguments on a plan (OP2G_SCATTER_STAGED)
+    int cells_per_thread = 1;
 };
 
 extern "C" {
@@ -369,7 +370,7 @@ op2g_status op2g_kernel_create(const char *user_src, const char *kernel_name,
 
     op2g_kernel *k = new op2g_kernel();
     k->sig = S;
-    k->source = generate_source(S);
+    k->source = generate_source(S, &k->cells_per_thread);
     k->param_bytes = 8 * (5 + (S.nptrs > 0 ? S.nptrs : 1) + (nmaps > 0 ? nmaps : 1));
     for (int r : staged_args(S))
         if (r >= 0) k->staged = true;
@@ -555,9 +556,13 @@ op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *
     const int64_t items = (d->end - d->start) * (k->sig.loop.extruded && k->sig.loop.constant_layers &&
                                                  column_parallel(k->sig) ? per : 1);
     if (items <= 0) return OP2G_OK;
+    // a thread runs cells_per_thread iterations per sweep step: the grid is
+    // sized for the steps
+    const int64_t cpt = k->cells_per_thread > 1 ? k->cells_per_thread : 1;
     int32_t grid = 0, bs = 0, chunked = 0;
-    op2g_launch_shape(items, d->end - d->start, k->sig.block_size, L->sms, L->occ, d->grid,
-                      L->fc != nullptr, &grid, &bs, &chunked);
+    op2g_launch_shape((items + cpt - 1) / cpt, (d->end - d->start + cpt - 1) / cpt,
+                      k->sig.block_size, L->sms, L->occ, d->grid, L->fc != nullptr, &grid, &bs,
+                      &chunked);
     void *params[] = {buf};
     return launch(chunked ? L->fc : L->f, (unsigned)grid, (unsigned)bs, params, stream);
 }
