@@ -995,42 +995,20 @@ unsigned grid_for(long long n, int bs) {
     return (unsigned)(g < 1 ? 1 : g);
 }
 
-// Launch k_spmv_bsr with more than the default 48 KB of dynamic shared
-// memory (the attribute is set once per instantiation and size).
-// Asynchronous global -> shared copies of 4 or 8 bytes (cp.async), waited
-// for by commit groups.
-template <int BYTES>
-__device__ __forceinline__ void cpa(void *dst, const void *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(
-                     (unsigned)__cvta_generic_to_shared(dst)),
-                 "l"(src), "n"(BYTES)
-                 : "memory");
-}
-__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cpa_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
 // Blocks of R x C: one lane per block row, so every FMA instruction is a
 // full warp of useful work (the FP64 pipe's measure on this GPU) and no
-// lanes' sums are combined.  A warp owns 32 consecutive block rows and walks
-// them in column slices of K blocks: for slice k each lane copies its own
-// row's blocks [k K, k K + K) (a contiguous run of K R C values, and their
-// column indices) into the warp's shared memory with cp.async, gathers the
-// x entries of the slice's blocks (all in flight together), then does R C
-// FMAs per block into R accumulators from its run (row stride ST, odd, so
-// the 32 lanes hit distinct banks).
-template <int R, int C, int K>
-__global__ void __launch_bounds__(256)
+// lanes' sums are combined.  A warp owns 32 consecutive block rows; each
+// lane walks its own row one block at a time, holding the block's R C
+// values and column index in registers, with the next block's loads issued
+// before the current block's x gather and FMAs (a contiguous R C run per
+// lane: the lines a lane touches are reused by its next loads from L1).
+// 68 registers at 3 CTAs of 256 threads per SM.
+template <int R, int C>
+__global__ void __launch_bounds__(256, 3)
     k_spmv_bsr_lane(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
     constexpr int BS = R * C;
-    constexpr int ST = (K * BS) | 1;
-    extern __shared__ double sbuf[];
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    double *sv = sbuf + (size_t)wib * (32 * ST + 16 * K) + lane * ST;  // this lane's run
-    int *sc = (int *)(sbuf + (size_t)wib * (32 * ST + 16 * K) + 32 * ST) + lane * K;
     const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long r0 = ((long long)blockIdx.x * (blockDim.x >> 5) + wib) * 32; r0 < m.nrows;
          r0 += nwarps * 32) {
@@ -1040,39 +1018,33 @@ __global__ void __launch_bounds__(256)
             q0 = __ldg(m.rowptr + r);
             q1 = __ldg(m.rowptr + r + 1);
         }
-        const int len = (int)(q1 - q0);
-        const int nsteps = ((int)__reduce_max_sync(full, (unsigned)len) + K - 1) / K;
+        const int nsteps = (int)__reduce_max_sync(full, (unsigned)(q1 - q0));
         double acc[R];
 #pragma unroll
         for (int i = 0; i < R; ++i) acc[i] = 0.0;
+        double v[BS];
+        int col = 0;
+        // block q of this lane's row, or zeros past its end
+        auto load = [&](long long q) {
+            const bool ok = q < q1;
+            col = ok ? __ldg(m.colidx + q) : 0;
+#pragma unroll
+            for (int e = 0; e < BS; ++e) v[e] = ok ? __ldg(m.values + q * BS + e) : 0.0;
+        };
+        if (nsteps > 0) load(q0);
         for (int k = 0; k < nsteps; ++k) {
-            const long long b0 = q0 + (long long)k * K;
-            const int nb = q1 - b0 >= K ? K : (q1 > b0 ? (int)(q1 - b0) : 0);
-            const double *src = m.values + b0 * BS;
-            for (int j = 0; j < nb * BS; ++j) cpa<8>(sv + j, src + j);
-            for (int j = 0; j < nb; ++j) cpa<4>(sc + j, m.colidx + b0 + j);
-            cpa_commit();
-            cpa_wait<0>();
-            __syncwarp();
-            // the slice's x entries first (all in flight together), then the FMAs
-            double xv[K][C];
+            double cv[BS];
 #pragma unroll
-            for (int b = 0; b < K; ++b) {
-                const long long col = b < nb ? sc[b] : 0;
+            for (int e = 0; e < BS; ++e) cv[e] = v[e];
+            const long long cc = col;
+            if (k + 1 < nsteps) load(q0 + k + 1);
+            double xv[C];
 #pragma unroll
-                for (int j = 0; j < C; ++j) xv[b][j] = b < nb ? __ldg(x + col * C + j) : 0.0;
-            }
+            for (int j = 0; j < C; ++j) xv[j] = __ldg(x + cc * C + j);
 #pragma unroll
-            for (int b = 0; b < K; ++b) {
-                if (b < nb) {
+            for (int i = 0; i < R; ++i)
 #pragma unroll
-                    for (int i = 0; i < R; ++i)
-#pragma unroll
-                        for (int j = 0; j < C; ++j)
-                            acc[i] = fma(sv[b * BS + i * C + j], xv[b][j], acc[i]);
-                }
-            }
-            __syncwarp();  // the run is refilled for the next slice
+                for (int j = 0; j < C; ++j) acc[i] = fma(cv[i * C + j], xv[j], acc[i]);
         }
         if (r < m.nrows) {
 #pragma unroll
@@ -1081,22 +1053,13 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-template <int R, int C, int K>
+template <int R, int C>
 cudaError_t spmv_lane_launch(cudaStream_t st, const op2g_bcsr &m, const double *x, double *y) {
-    constexpr int BS = R * C, ST = (K * BS) | 1, T = 256;
-    const size_t smem = (size_t)(T / 32) * (32 * ST + 16 * K) * sizeof(double);
-    static int granted = -1;   // device whose attribute is set
-    int dev = 0;
+    constexpr int T = 256;
+    int dev = 0, occ = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (granted != dev) {
-        e = cudaFuncSetAttribute(k_spmv_bsr_lane<R, C, K>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        granted = dev;
-    }
-    int occ = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_spmv_bsr_lane<R, C, K>, T, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_spmv_bsr_lane<R, C>, T, 0);
     if (e != cudaSuccess) return e;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long warps = (m.nrows + 31) / 32;
@@ -1104,10 +1067,12 @@ cudaError_t spmv_lane_launch(cudaStream_t st, const op2g_bcsr &m, const double *
     const long long need = (warps + T / 32 - 1) / (T / 32);
     if (g > need) g = need;
     if (g < 1) g = 1;
-    k_spmv_bsr_lane<R, C, K><<<(unsigned)g, T, smem, st>>>(m, x, y);
+    k_spmv_bsr_lane<R, C><<<(unsigned)g, T, 0, st>>>(m, x, y);
     return cudaGetLastError();
 }
 
+// Launch k_spmv_bsr with more than the default 48 KB of dynamic shared
+// memory (the attribute is set once per instantiation and size).
 template <int RT, int CT>
 cudaError_t spmv_launch(unsigned grid, size_t smem, cudaStream_t st, const op2g_bcsr &m,
                         const double *x, double *y) {
@@ -1173,12 +1138,13 @@ op2g_status op2g_mat_spmv(const op2g_bcsr *m, const double *x, double *y, int32_
         const long long ctas = (m->nrows + SPMV_T / r - 1) / (SPMV_T / r);
         const unsigned g = grid_for(ctas * SPMV_T, SPMV_T);
         cudaError_t e;
-        // 3x3 blocks: one lane per block row, four-block slices (prism BAIJ
-        // matrix: 2.02 ms, against 3.64 ms for the tiled kernel)
+        // 3x3 and 2x2 blocks: one lane per block row (prism 3x3 matrix of
+        // 88.8 M blocks: 1.67 ms, against 3.64 ms for the tiled kernel; 2x2
+        // on the 128^3 tet mesh: 0.31 ms against 0.51 ms)
         if (r == 3 && c == 3)
-            e = spmv_lane_launch<3, 3, 4>(st, *m, x, y);
+            e = spmv_lane_launch<3, 3>(st, *m, x, y);
         else if (r == 2 && c == 2)
-            e = spmv_launch<2, 2>(g, smem, st, *m, x, y);
+            e = spmv_lane_launch<2, 2>(st, *m, x, y);
         else
             e = spmv_launch<0, 0>(g, smem, st, *m, x, y);
         CK(e);
