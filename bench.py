@@ -802,6 +802,10 @@ def cpu_sections(reps=2):
     return out
 
 
+GATHER_COPY = ("static void gc(double *o, const double *x) "
+               "{ o[0] = x[0]; o[1] = x[1]; o[2] = x[2]; o[3] = x[3]; }")
+
+
 def measure_data_path(op2, p, steps, warmup):
     """Loops with (almost) no arithmetic on the benchmark mesh, to show the
     wrapper's memory path against HBM where FP64 is not the limit: a direct
@@ -826,6 +830,10 @@ def measure_data_path(op2, p, steps, warmup):
                                         "{ for (int i = 0; i < 4; ++i) y[i] += w[0]; }", "sc"),
                                       cells, y(op2.INC, c2v), w(op2.READ)), 24 * C + 16 * V),
     }
+    # the gather alone: the four vertex values copied out, no FP64 arithmetic
+    out4 = op2.Dat(cells ** 4, np.zeros((C, 4)))
+    loops["gather_copy"] = (LegacyParloop(K(GATHER_COPY, "gc"), cells, out4(op2.WRITE),
+                                          x(op2.READ, c2v)), 48 * C + 8 * V)
     from pyop2_gb300 import _lib
     pl = LegacyParloop(K("static void ga(double *o, const double *x) "
                          "{ o[0] = x[0] + x[1] + x[2] + x[3]; }", "ga"),
@@ -1102,6 +1110,32 @@ def scatter_pair(op2, n=N_CUBE, launches=2):
             "y_checksum": float(y.data_ro.sum())}
 
 
+def gather_pair(op2, n=N_CUBE, permute=False, launches=2):
+    """The gather loops on the n^3 x 6 tet mesh: `launches` times the sum
+    o_e = x[map(e, 0)] + ... + x[map(e, 3)] (three FP64 adds per cell), then
+    `launches` times the copy o_e[i] = x[map(e, i)] (no arithmetic).  For
+    one-kernel profiler captures of the two forms."""
+    import torch
+    from pyop2_gb300 import workloads as W
+    from pyop2_gb300.parloop import LegacyParloop
+    p = W.build_p1_3d(op2, n=n, permute=permute, seed=0)
+    cells, c2v, x = p["cells"], p["c2v"], p["x"]
+    out = op2.Dat(cells, np.zeros(cells.size))
+    out4 = op2.Dat(cells ** 4, np.zeros((cells.size, 4)))
+    ls = LegacyParloop(op2.Kernel("static void ga(double *o, const double *x) "
+                                  "{ o[0] = x[0] + x[1] + x[2] + x[3]; }", "ga"),
+                       cells, out(op2.WRITE), x(op2.READ, c2v))
+    lc = LegacyParloop(op2.Kernel(GATHER_COPY, "gc"), cells, out4(op2.WRITE), x(op2.READ, c2v))
+    ls.launch_desc()
+    lc.launch_desc()
+    torch.cuda.synchronize()
+    for lp in [ls] * launches + [lc] * launches:
+        lp.compute()
+    torch.cuda.synchronize()
+    return {"cells": cells.size, "launches": 2 * launches,
+            "checksum": float(out.data_ro.sum() + out4.data_ro.sum())}
+
+
 def run_only(args):
     """One secondary measurement on its own (used for ncu captures); prints
     its JSON object."""
@@ -1122,6 +1156,11 @@ def run_only(args):
         out = measure_prism_assembly(op2, n=args.size or 256)
     elif args.only == "scatter":
         out = scatter_pair(op2, n=args.size or N_CUBE)
+    elif args.only == "gather":
+        out = gather_pair(op2, n=args.size or N_CUBE, permute=args.permute)
+    elif args.only == "data_path":
+        p = workloads.build_p1_3d(op2, n=args.size or N_CUBE, permute=args.permute, seed=0)
+        out = measure_data_path(op2, p, args.steps, args.warmup)
     else:
         out = measure_prisms(op2, args.steps, args.warmup, n=args.size or 256)
     print(json.dumps({"only": args.only, "result": out}), flush=True)
@@ -1141,7 +1180,7 @@ def main():
                     help="only the headline action (no adjoint / batch measurements)")
     ap.add_argument("--only", default=None,
                     choices=["sparsity", "adjoint", "batch", "prisms", "small",
-                             "prism_assembly", "scatter"],
+                             "prism_assembly", "scatter", "gather", "data_path"],
                     help="run one secondary measurement alone (profiling runs)")
     ap.add_argument("--size", type=int, default=None,
                     help="with --only: mesh size (cube edge / prism base edge)")

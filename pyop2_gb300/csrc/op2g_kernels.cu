@@ -729,70 +729,10 @@ __global__ void k_set_diag(op2g_bcsr m, const int *__restrict__ rows, long long 
 
 // y = A x on block-CSR.  GB300 issues FP64 at 2 thread-instructions per
 // clock per SM, so even a 1x1 product has as much FP64 time (one FMA per
-// entry) as HBM time; both kernels below stream the matrix with coalesced
-// loads into shared memory and spend one FMA per entry, summing each row in
-// a fixed order so that repeated products are bitwise identical.
+// entry) as HBM time; every kernel below spends one FMA per entry and sums
+// each row in a fixed order, so that repeated products are bitwise
+// identical.
 constexpr int SPMV_T = 256, SPMV_PER = 8, SPMV_TILE = SPMV_T * SPMV_PER;
-
-// 1x1 blocks (CSR).  A CTA owns SPMV_T consecutive rows, one per thread, and
-// walks their entries (contiguous) in tiles of SPMV_TILE: every thread
-// issues SPMV_PER loads of values and column indices, then the gathers of
-// x, stages value and x side by side in shared memory, and after a barrier
-// runs acc = fma(value, x, acc) over its own row's entries in column order.
-// At ~15 entries per row a CTA's rows span two tiles; 32 KB of shared
-// memory and 64 registers leave 4 CTAs per SM to overlap one another's load
-// and sum phases (measured faster than the pipelined kernel below, whose
-// double buffer allows only 3).
-__global__ void __launch_bounds__(SPMV_T, 4)
-    k_spmv_csr(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
-    __shared__ double sv[SPMV_TILE], sx[SPMV_TILE];
-    const int tid = threadIdx.x;
-    for (long long r0 = blockIdx.x * (long long)SPMV_T; r0 < m.nrows;
-         r0 += (long long)gridDim.x * SPMV_T) {
-        const long long rN = r0 + SPMV_T < m.nrows ? r0 + SPMV_T : m.nrows;
-        const long long row = r0 + tid;
-        const bool own = row < rN;
-        long long q0 = 0, q1 = 0;
-        if (own) {
-            q0 = __ldg(m.rowptr + row);
-            q1 = __ldg(m.rowptr + row + 1);
-        }
-        const long long qb = __ldg(m.rowptr + rN);
-        double acc = 0.0;
-        for (long long qa = __ldg(m.rowptr + r0); qa < qb; qa += SPMV_TILE) {
-            const int n = (int)(qa + SPMV_TILE < qb ? SPMV_TILE : qb - qa);
-            __syncthreads();  // the previous tile has been summed
-            // all loads of the tile in flight before the first use
-            double v[SPMV_PER], xv[SPMV_PER];
-            int ci[SPMV_PER];
-#pragma unroll
-            for (int k = 0; k < SPMV_PER; ++k) {
-                const int i = tid + k * SPMV_T;
-                if (i < n) {
-                    v[k] = __ldg(m.values + qa + i);
-                    ci[k] = __ldg(m.colidx + qa + i);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < SPMV_PER; ++k)
-                if (tid + k * SPMV_T < n) xv[k] = __ldg(x + ci[k]);
-#pragma unroll
-            for (int k = 0; k < SPMV_PER; ++k) {
-                const int i = tid + k * SPMV_T;
-                if (i < n) {
-                    sv[i] = v[k];
-                    sx[i] = xv[k];
-                }
-            }
-            __syncthreads();
-            if (own) {
-                const long long s0 = q0 > qa ? q0 : qa, e0 = q1 < qa + n ? q1 : qa + n;
-                for (int o = (int)(s0 - qa); o < (int)(e0 - qa); ++o) acc = fma(sv[o], sx[o], acc);
-            }
-        }
-        if (own) y[row] = acc;
-    }
-}
 
 // Blocks of R x C > 1 entries: a 3x3 block row holds ~190 entries, so one
 // thread per dof row would leave most lanes of a tile idle; instead S lanes
@@ -995,16 +935,18 @@ unsigned grid_for(long long n, int bs) {
     return (unsigned)(g < 1 ? 1 : g);
 }
 
-// Blocks of R x C: one lane per block row, so every FMA instruction is a
-// full warp of useful work (the FP64 pipe's measure on this GPU) and no
-// lanes' sums are combined.  A warp owns 32 consecutive block rows; each
-// lane walks its own row one block at a time, holding the block's R C
-// values and column index in registers, with the next block's loads issued
-// before the current block's x gather and FMAs (a contiguous R C run per
-// lane: the lines a lane touches are reused by its next loads from L1).
-// 68 registers at 3 CTAs of 256 threads per SM.
-template <int R, int C>
-__global__ void __launch_bounds__(256, 3)
+// One lane per block row, so every FMA instruction is a full warp of useful
+// work (the FP64 pipe's measure on this GPU) and no lanes' sums are
+// combined.  A warp owns 32 consecutive block rows; each lane walks its own
+// row K blocks at a time with their R C values and column indices in
+// registers, and the next K blocks' loads are issued before the current
+// ones' x gathers and FMAs.  A lane's blocks are contiguous, so its next
+// loads hit the lines its last ones brought into L1.  Lanes past the end of
+// their row skip the FMAs (their loads are of zeros and x[0..C)).
+// 3x3 and 2x2 blocks: K = 1, 3 CTAs of 256 threads per SM (68-72 registers);
+// 1x1 (CSR): K = 4, 4 CTAs per SM.
+template <int R, int C, int K, int MINB>
+__global__ void __launch_bounds__(256, MINB)
     k_spmv_bsr_lane(op2g_bcsr m, const double *__restrict__ x, double *__restrict__ y) {
     constexpr int BS = R * C;
     const unsigned full = 0xffffffffu;
@@ -1018,33 +960,47 @@ __global__ void __launch_bounds__(256, 3)
             q0 = __ldg(m.rowptr + r);
             q1 = __ldg(m.rowptr + r + 1);
         }
-        const int nsteps = (int)__reduce_max_sync(full, (unsigned)(q1 - q0));
+        const int nsteps = ((int)__reduce_max_sync(full, (unsigned)(q1 - q0)) + K - 1) / K;
         double acc[R];
 #pragma unroll
         for (int i = 0; i < R; ++i) acc[i] = 0.0;
-        double v[BS];
-        int col = 0;
-        // block q of this lane's row, or zeros past its end
+        double v[K * BS];
+        int col[K];
+        // blocks [q, q + K) of this lane's row, zeros past its end
         auto load = [&](long long q) {
-            const bool ok = q < q1;
-            col = ok ? __ldg(m.colidx + q) : 0;
 #pragma unroll
-            for (int e = 0; e < BS; ++e) v[e] = ok ? __ldg(m.values + q * BS + e) : 0.0;
+            for (int b = 0; b < K; ++b) {
+                const bool ok = q + b < q1;
+                col[b] = ok ? __ldg(m.colidx + q + b) : 0;
+#pragma unroll
+                for (int e = 0; e < BS; ++e)
+                    v[b * BS + e] = ok ? __ldg(m.values + (q + b) * BS + e) : 0.0;
+            }
         };
         if (nsteps > 0) load(q0);
         for (int k = 0; k < nsteps; ++k) {
-            double cv[BS];
+            const long long qk = q0 + (long long)k * K;
+            double cv[K * BS];
+            int cc[K];
 #pragma unroll
-            for (int e = 0; e < BS; ++e) cv[e] = v[e];
-            const long long cc = col;
-            if (k + 1 < nsteps) load(q0 + k + 1);
-            double xv[C];
+            for (int e = 0; e < K * BS; ++e) cv[e] = v[e];
 #pragma unroll
-            for (int j = 0; j < C; ++j) xv[j] = __ldg(x + cc * C + j);
+            for (int b = 0; b < K; ++b) cc[b] = col[b];
+            if (k + 1 < nsteps) load(qk + K);
+            double xv[K][C];
 #pragma unroll
-            for (int i = 0; i < R; ++i)
+            for (int b = 0; b < K; ++b)
 #pragma unroll
-                for (int j = 0; j < C; ++j) acc[i] = fma(cv[i * C + j], xv[j], acc[i]);
+                for (int j = 0; j < C; ++j) xv[b][j] = __ldg(x + (long long)cc[b] * C + j);
+#pragma unroll
+            for (int b = 0; b < K; ++b)
+                if (qk + b < q1) {
+#pragma unroll
+                    for (int i = 0; i < R; ++i)
+#pragma unroll
+                        for (int j = 0; j < C; ++j)
+                            acc[i] = fma(cv[b * BS + i * C + j], xv[b][j], acc[i]);
+                }
         }
         if (r < m.nrows) {
 #pragma unroll
@@ -1053,13 +1009,13 @@ __global__ void __launch_bounds__(256, 3)
     }
 }
 
-template <int R, int C>
+template <int R, int C, int K, int MINB>
 cudaError_t spmv_lane_launch(cudaStream_t st, const op2g_bcsr &m, const double *x, double *y) {
     constexpr int T = 256;
     int dev = 0, occ = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_spmv_bsr_lane<R, C>, T, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_spmv_bsr_lane<R, C, K, MINB>, T, 0);
     if (e != cudaSuccess) return e;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long warps = (m.nrows + 31) / 32;
@@ -1067,7 +1023,7 @@ cudaError_t spmv_lane_launch(cudaStream_t st, const op2g_bcsr &m, const double *
     const long long need = (warps + T / 32 - 1) / (T / 32);
     if (g > need) g = need;
     if (g < 1) g = 1;
-    k_spmv_bsr_lane<R, C><<<(unsigned)g, T, 0, st>>>(m, x, y);
+    k_spmv_bsr_lane<R, C, K, MINB><<<(unsigned)g, T, 0, st>>>(m, x, y);
     return cudaGetLastError();
 }
 
@@ -1131,7 +1087,9 @@ op2g_status op2g_mat_spmv(const op2g_bcsr *m, const double *x, double *y, int32_
     else if (r > SPMV_T || r * c > SPMV_TILE || m->ncols * c > INT_MAX)
         k_spmv_rows<8><<<grid_for(nr * 8, 256), 256, 0, st>>>(*m, x, y);
     else if (r == 1 && c == 1)
-        k_spmv_csr<<<grid_for(m->nrows, SPMV_T), SPMV_T, 0, st>>>(*m, x, y);
+        // tet mesh 128^3 (31.8 M entries): 0.090 ms, against 0.121 ms for a
+        // CTA-tiled kernel staging values and x in shared memory
+        CK((spmv_lane_launch<1, 1, 4, 4>(st, *m, x, y)));
     else {
         // two buffers of (SPMV_TILE / bs) * bs values and x entries
         const size_t smem = 4 * (size_t)(SPMV_TILE / (r * c)) * (r * c) * sizeof(double);
@@ -1142,9 +1100,9 @@ op2g_status op2g_mat_spmv(const op2g_bcsr *m, const double *x, double *y, int32_
         // 88.8 M blocks: 1.67 ms, against 3.64 ms for the tiled kernel; 2x2
         // on the 128^3 tet mesh: 0.31 ms against 0.51 ms)
         if (r == 3 && c == 3)
-            e = spmv_lane_launch<3, 3>(st, *m, x, y);
+            e = spmv_lane_launch<3, 3, 1, 3>(st, *m, x, y);
         else if (r == 2 && c == 2)
-            e = spmv_lane_launch<2, 2>(st, *m, x, y);
+            e = spmv_lane_launch<2, 2, 1, 3>(st, *m, x, y);
         else
             e = spmv_launch<0, 0>(g, smem, st, *m, x, y);
         CK(e);

@@ -59,6 +59,32 @@ def test_mult_matches_scipy(gpu_op2, shape):
 
 
 @pytest.mark.parametrize("shape", SHAPES, ids=["%dx%d" % s for s in SHAPES])
+def test_mult_inf_only_where_referenced(gpu_op2, shape):
+    """x's first column block is +inf: a row that stores no block in that
+    column stays finite (lanes past the end of a shorter row in the same
+    warp must not touch x), and a row that does is non-finite, as in scipy."""
+    op2 = gpu_op2
+    r, c = shape
+    A, drows, dcols, rng = _assembled(op2, r, c, seed=5 * r + c)
+    S = A.to_scipy().tocsr()
+    xv = rng.uniform(-1, 1, (193, c))
+    xv[0, :] = np.inf
+    x = op2.Dat(dcols, xv if c > 1 else xv[:, 0])
+    y = op2.Dat(drows)
+    with np.errstate(invalid="ignore"):
+        A.mult(x, y)
+        ref = S @ x.data_ro.reshape(-1)
+    got = y.data_ro.reshape(-1)
+    refers = np.zeros(257 * r, bool)
+    refers[np.unique(S[:, :c].tocoo().row)] = True
+    assert refers.any() and not refers.all()
+    assert np.all(np.isfinite(got[~refers]))
+    assert not np.any(np.isfinite(got[refers]))
+    fin = ~refers
+    assert np.abs(got[fin] - ref[fin]).max() <= 1e-12 * np.abs(ref[fin]).max()
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=["%dx%d" % s for s in SHAPES])
 def test_to_torch_export(gpu_op2, shape):
     """torch sparse export (CSR for 1x1, BSR otherwise) equals the scipy
     export entry for entry and shares the Mat's device values."""
