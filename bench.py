@@ -807,11 +807,12 @@ GATHER_COPY = ("static void gc(double *o, const double *x) "
 
 
 def measure_data_path(op2, p, steps, warmup):
-    """Loops with (almost) no arithmetic on the benchmark mesh, to show the
-    wrapper's memory path against HBM where FP64 is not the limit: a direct
-    copy, a gather through the map, an INC scatter through the map.  Bytes
-    are compulsory ones (map read once, per-cell Dats once, vertex Dats
-    once; INC targets read and written)."""
+    """Loops with little or no arithmetic on the benchmark mesh, to show the
+    wrapper's memory path against HBM: a direct copy, a gather through the
+    map that sums the four values (three FP64 adds per cell) and one that
+    copies them out, an INC scatter through the map.  Bytes are compulsory
+    ones (map read once, per-cell Dats once, vertex Dats once; INC targets
+    read and written)."""
     import numpy as np
     import torch
     from pyop2_gb300.parloop import LegacyParloop

@@ -187,19 +187,25 @@ typedef struct op2g_kernel op2g_kernel;
  * current device) and return a handle.  `cache_dir` (may be NULL) holds
  * compiled cubins keyed by a hash of source, options and arch.  No device is
  * needed unless arch is NULL.  On OP2G_ERR_COMPILE op2g_last_error() holds
- * the NVRTC log. */
+ * the NVRTC log.  When a direct DAT argument's rows are a multiple of 16
+ * bytes (stride, or dim, x element size), a second variant is compiled that
+ * declares every such row 16- or 32-byte aligned, so the kernel's accesses
+ * to adjacent components become vector loads and stores; op2g_kernel_launch
+ * runs it when all those arguments' pointers are aligned, the first variant
+ * otherwise (batched launches always run the first). */
 op2g_status op2g_kernel_create(const char *user_src, const char *kernel_name,
                                const op2g_loop_desc *loop, const op2g_arg_desc *args,
                                int32_t nargs, const op2g_map_desc *maps, int32_t nmaps,
                                const char *arch, const char *cache_dir, op2g_kernel **out);
 void op2g_kernel_destroy(op2g_kernel *k);
 
-/* Copy the generated CUDA source into buf (NUL-terminated, truncated to len);
- * *needed receives strlen+1. */
+/* Copy the generated CUDA source (the variant without alignment hints) into
+ * buf (NUL-terminated, truncated to len); *needed receives strlen+1. */
 op2g_status op2g_kernel_source(const op2g_kernel *k, char *buf, size_t len, size_t *needed);
-/* Load the compiled wrapper on the current device without launching it.
- * Launches load it on first use; call this first when the first launch will
- * happen inside a CUDA stream capture (module loading is not capturable). */
+/* Load the compiled wrapper (both variants) on the current device without
+ * launching it.  Launches load it on first use; call this first when the
+ * first launch will happen inside a CUDA stream capture (module loading is
+ * not capturable). */
 op2g_status op2g_kernel_prepare(op2g_kernel *k);
 /* Number of device-pointer slots op2g_kernel_launch expects in `ptrs`:
  *   per argument, in order: DAT 1 (data), GLOBAL 1 (data, or the zeroed

@@ -210,6 +210,8 @@ struct Gen {
     // cells' gathers and arithmetic can be interleaved by the compiler.
     bool guard_unpack = false;
     int cells_per_thread = 1;  // what the sweep loop was generated with
+    // The variant for aligned direct arguments (aligned_direct_args).
+    bool align_hints = false;
 
     explicit Gen(const Signature &s) : S(s) {
         nf = (S.loop.extruded && S.loop.iteration_region == OP2G_ON_INTERIOR_FACETS) ? 2 : 1;
@@ -1175,10 +1177,20 @@ struct Gen {
                     if (staging && st_dir[a])
                         kargs.push_back("op2g::ptr((" + std::string(T) + " *)dv" + an +
                                         "[vb_] + (n - c0_) * " + std::to_string(A.d.dim) + ")");
-                    else
-                        kargs.push_back("op2g::ptr((" + std::string(T) + " *)p.ptr[" +
-                                        std::to_string(A.slot) + "] + n * " +
-                                        std::to_string(gstride(a)) + ")");
+                    else {
+                        // in the variant launched on aligned pointers the
+                        // compiler is told each row's alignment, so the
+                        // kernel's accesses to adjacent components merge
+                        // into vector loads and stores
+                        const int al = align_hints ? direct_row_alignment(S, a) : 0;
+                        const std::string row = "(" + std::string(T) + " *)p.ptr[" +
+                                                std::to_string(A.slot) + "] + n * " +
+                                                std::to_string(gstride(a));
+                        kargs.push_back(al ? "op2g::ptr((" + std::string(T) +
+                                                 " *)__builtin_assume_aligned(" + row + ", " +
+                                                 std::to_string(al) + "))"
+                                           : "op2g::ptr(" + row + ")");
+                    }
                     continue;
                 }
                 const int ar = S.maps[A.d.map].arity;
@@ -1481,8 +1493,29 @@ std::string validate_signature(const Signature &S) {
     return "";
 }
 
-std::string generate_source(const Signature &S, int *cells_per_thread) {
+// Alignment of every row of direct Dat argument a when its array is
+// aligned to it: 32 or 16 bytes for rows of a multiple of that size, else 0.
+int direct_row_alignment(const Signature &S, size_t a) {
+    const op2g_arg_desc &d = S.args[a].d;
+    if (d.kind != OP2G_ARG_DAT || d.map >= 0) return 0;
+    const long long rb = (long long)(d.stride > 0 ? d.stride : d.dim) * (long long)elt_size(d.dtype);
+    return rb % 32 == 0 ? 32 : rb % 16 == 0 ? 16 : 0;
+}
+
+std::vector<std::pair<int, int>> aligned_direct_args(const Signature &S) {
+    std::vector<std::pair<int, int>> out;
+    for (int r : staged_args(S))
+        if (r >= 0) return out;
+    for (size_t a = 0; a < S.args.size(); ++a) {
+        const int al = direct_row_alignment(S, a);
+        if (al) out.push_back({S.args[a].slot, al});
+    }
+    return out;
+}
+
+std::string generate_source(const Signature &S, int *cells_per_thread, bool align_hints) {
     Gen g(S);
+    g.align_hints = align_hints;
     std::string src = g.emit();
     if (cells_per_thread) *cells_per_thread = g.cells_per_thread;
     return src;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/op2g.h"
@@ -40,8 +41,15 @@ struct Signature {
 
 std::string validate_signature(const Signature &S);
 // The wrapper's source; *cells_per_thread (may be NULL) receives the
-// iterations a thread runs per sweep step in it.
-std::string generate_source(const Signature &S, int *cells_per_thread = nullptr);
+// iterations a thread runs per sweep step in it.  With align_hints the
+// direct arguments of aligned_direct_args are declared aligned (the variant
+// launched only when their pointers are).
+std::string generate_source(const Signature &S, int *cells_per_thread = nullptr,
+                            bool align_hints = false);
+// Direct Dat arguments whose rows are a multiple of 16 bytes, as (pointer
+// slot, row alignment in bytes: 16 or 32); empty for staged wrappers.
+std::vector<std::pair<int, int>> aligned_direct_args(const Signature &S);
+int direct_row_alignment(const Signature &S, size_t a);
 // Staged wrappers (OP2G_SCATTER_STAGED): per argument the plain map whose
 // staging plan it uses, or -1; and the dynamic shared memory they take.
 std::vector<int> staged_args(const Signature &S);

@@ -289,7 +289,21 @@ struct op2g_kernel {
     int param_bytes = 0;
     bool staged = false;   // the wrapper stages arguments on a plan (OP2G_SCATTER_STAGED)
     int cells_per_thread = 1;
+    // Direct arguments with rows of a multiple of 16 bytes (pointer slot,
+    // alignment): a second variant of the wrapper declares their rows
+    // aligned, and a launch runs it when every such pointer is aligned.
+    std::vector<std::pair<int, int>> al_args;
+    std::string source_al, cubin_al;
+    std::map<int, Loaded> per_dev_al;
 };
+
+// Whether the launch's direct-argument pointers allow the aligned variant.
+static bool use_aligned(const op2g_kernel *k, const op2g_launch_desc *d) {
+    if (k->al_args.empty() || !d->ptrs) return false;
+    for (const auto &sa : k->al_args)
+        if ((uintptr_t)d->ptrs[sa.first] % (uintptr_t)sa.second) return false;
+    return true;
+}
 
 extern "C" {
 
@@ -382,6 +396,13 @@ op2g_status op2g_kernel_create(const char *user_src, const char *kernel_name,
         return st;
     }
     st = build_cubin(k->source, k->arch, cache_dir, k->cubin);
+    if (st == OP2G_OK) {
+        k->al_args = aligned_direct_args(S);
+        if (!k->al_args.empty()) {
+            k->source_al = generate_source(S, nullptr, true);
+            st = build_cubin(k->source_al, k->arch, cache_dir, k->cubin_al);
+        }
+    }
     if (st != OP2G_OK) {
         delete k;
         return st;
@@ -394,6 +415,8 @@ void op2g_kernel_destroy(op2g_kernel *k) {
     if (!k) return;
     if (driver().ok) {
         for (auto &kv : k->per_dev)
+            if (kv.second.mod) driver().ModuleUnload(kv.second.mod);
+        for (auto &kv : k->per_dev_al)
             if (kv.second.mod) driver().ModuleUnload(kv.second.mod);
     }
     delete k;
@@ -413,8 +436,12 @@ op2g_status op2g_kernel_source(const op2g_kernel *k, char *buf, size_t len, size
 op2g_status op2g_kernel_prepare(op2g_kernel *k) {
     if (!k) return fail(OP2G_ERR_INVALID, "NULL kernel");
     Loaded *L = nullptr;
-    return load_module(k->cubin, "op2g_wrap", "op2g_wrap_batched", k->sig.block_size, k->per_dev,
-                       k->mu, &L);
+    op2g_status st = load_module(k->cubin, "op2g_wrap", "op2g_wrap_batched", k->sig.block_size,
+                                 k->per_dev, k->mu, &L);
+    if (st == OP2G_OK && !k->cubin_al.empty())
+        st = load_module(k->cubin_al, "op2g_wrap", "op2g_wrap_batched", k->sig.block_size,
+                         k->per_dev_al, k->mu, &L);
+    return st;
 }
 
 int32_t op2g_kernel_num_ptrs(const op2g_kernel *k) { return k ? k->sig.nptrs : -1; }
@@ -512,8 +539,9 @@ op2g_status op2g_kernel_launch(op2g_kernel *k, const op2g_launch_desc *d, void *
     op2g_status st = op2g_kernel_pack_params(k, d, buf);
     if (st != OP2G_OK) return st;
     Loaded *L = nullptr;
-    st = load_module(k->cubin, "op2g_wrap", "op2g_wrap_batched", k->sig.block_size, k->per_dev,
-                     k->mu, &L);
+    const bool al = use_aligned(k, d);
+    st = load_module(al ? k->cubin_al : k->cubin, "op2g_wrap", "op2g_wrap_batched",
+                     k->sig.block_size, al ? k->per_dev_al : k->per_dev, k->mu, &L);
     if (st != OP2G_OK) return st;
     if (k->staged) {
         if (d->end <= d->start) return OP2G_OK;
