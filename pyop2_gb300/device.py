@@ -189,11 +189,10 @@ class Mirror:
 
     def zero(self):
         if self._dev is not None:
+            # the host copy goes stale (refreshed if it is read) instead of
+            # being cleared as well
             self._dev.zero_()
             self.state = "device"
-            if self._host is not None:
-                self._host[...] = 0
-                self.state = "both"
         else:
             self._host = None
             self.state = "host"
