@@ -92,14 +92,21 @@ static bool declared_without_parameters(const std::string &src, const std::strin
     return false;
 }
 
-// ---------------------------------------------------------------------------
-// Which arguments a staged wrapper (OP2G_SCATTER_STAGED) stages in shared
-// memory: Dat arguments (not parts of a mixed argument) through a plain map
-// or a permuted one, READ when no argument of the loop writes a Dat that a
-// READ argument reads (staged values are read once per partition), and INC
-// with an element type shared-memory atomics support.  Entry a is the plain
-// map whose plan the argument uses, or -1.  Non-extruded, non-indexed loops
-// only; an empty result means the wrapper runs as OP2G_SCATTER_ATOMIC.
+// Starting value of an INC accumulator (Global, Dat and Mat packs; the
+// reference zero-fills them, pyop2/codegen/builder.py:271-274, 353-356,
+// 538-541).  For floating types it is -0.0, the exact identity of IEEE
+// addition: -0.0 + w == w for every w, so the compiler drops the kernel's
+// first `+=` into each entry (a DADD per entry: 4 of the P1 tet action's 64
+// FP64 instructions per cell), whereas +0.0 + w turns w = -0.0 into +0.0.
+// The scattered value then differs from the reference's only when it is
+// -0.0, and the sum it is added to only when that sum is also -0.0 (-0.0
+// here, +0.0 in the reference; the two compare equal).
+static std::string inc_zero(int dt) {
+    if (dt == OP2G_F64) return "(-0.0)";
+    if (dt == OP2G_F32) return "(-0.0f)";
+    return std::string("(") + ctype_of(dt) + ")0";
+}
+
 static size_t elt_size(int dt) {
     switch (dt) {
         case OP2G_F64: case OP2G_I64: case OP2G_U64: return 8;
@@ -109,6 +116,14 @@ static size_t elt_size(int dt) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Which arguments a staged wrapper (OP2G_SCATTER_STAGED) stages in shared
+// memory: Dat arguments (not parts of a mixed argument) through a plain map
+// or a permuted one, READ when no argument of the loop writes a Dat that a
+// READ argument reads (staged values are read once per partition), and INC
+// with an element type shared-memory atomics support.  Entry a is the plain
+// map whose plan the argument uses, or -1.  Non-extruded, non-indexed loops
+// only; an empty result means the wrapper runs as OP2G_SCATTER_ATOMIC.
 std::vector<int> staged_args(const Signature &S) {
     std::vector<int> st(S.args.size(), -1);
     if (S.loop.scatter != OP2G_SCATTER_STAGED || S.loop.extruded || S.loop.indexed) return st;
@@ -1161,8 +1176,8 @@ struct Gen {
                 } else {
                     O << J << T << " g" << an << "[" << A.d.dim << "];\n";
                     if (A.d.access == OP2G_INC)
-                        O << J << "for (int j = 0; j < " << A.d.dim << "; ++j) g" << an << "[j] = ("
-                          << T << ")0;\n";
+                        O << J << "for (int j = 0; j < " << A.d.dim << "; ++j) g" << an << "[j] = "
+                          << inc_zero(A.d.dtype) << ";\n";
                     else
                         O << J << "for (int j = 0; j < " << A.d.dim << "; ++j) g" << an
                           << "[j] = gacc" << an << "[j];\n";
@@ -1203,8 +1218,10 @@ struct Gen {
                 if (A.d.access == OP2G_INC || A.d.access == OP2G_WRITE) {
                     if (lead) {
                         O << J << "#pragma unroll\n";
-                        O << J << "for (int k = 0; k < " << tot << "; ++k) " << tn << "[k] = ("
-                          << T << ")0;\n";
+                        O << J << "for (int k = 0; k < " << tot << "; ++k) " << tn << "[k] = "
+                          << (A.d.access == OP2G_INC ? inc_zero(A.d.dtype)
+                                                     : "(" + std::string(T) + ")0")
+                          << ";\n";
                     }
                 } else if (staging && st_arg[a] >= 0) {
                     // staged: the partition's values sit at the entry's target
@@ -1240,8 +1257,9 @@ struct Gen {
                 const int tot = psize[a];
                 O << J << T << " t" << an << "[" << tot << "];\n";
                 O << J << "#pragma unroll\n";
-                O << J << "for (int k = 0; k < " << tot << "; ++k) t" << an << "[k] = (" << T
-                  << ")0;\n";
+                O << J << "for (int k = 0; k < " << tot << "; ++k) t" << an << "[k] = "
+                  << (A.d.access == OP2G_INC ? inc_zero(A.d.dtype) : "(" + std::string(T) + ")0")
+                  << ";\n";
                 kargs.push_back("op2g::ptr(t" + an + ")");
             }
         }

@@ -257,3 +257,33 @@ def test_out_of_range_map_is_refused_before_any_launch(gpu_op2):
     ok = op2.Map(ext, nodes, 1, np.array([[0], [3]]), offset=[1])   # 3 + 2 = 5: inside
     op2.par_loop(k, ext, dn(op2.INC, ok))
     assert np.array_equal(dn.data_ro, np.ones(6))
+
+
+@pytest.mark.parametrize("scatter", ["atomic", "warp", "colour", "shared"])
+def test_inc_signed_zero(gpu_op2, oracle_op2, scatter):
+    """INC accumulators start at -0.0 (the identity of IEEE addition), so a
+    kernel's first += into an entry is exact.  Contributions of -0.0 into
+    +0.0 leave +0.0 and nonzero values are unchanged, bit for bit as in the
+    reference, whose accumulators start at +0.0."""
+    from pyop2_gb300.configuration import configuration
+    res = []
+    old = configuration["scatter"]
+    try:
+        configuration["scatter"] = scatter
+        for op2 in (gpu_op2, oracle_op2):
+            cells, verts = op2.Set(64), op2.Set(20)
+            m = op2.Map(cells, verts, 2, (np.arange(128) * 7 % 20).astype(np.int32))
+            init = np.zeros(20)
+            init[10:] = np.arange(1.0, 11.0)
+            y = op2.Dat(verts, init)
+            g = op2.Global(1, 0.0)
+            k = op2.Kernel("static void k(double *y, double *g) "
+                           "{ y[0] += -0.0; y[1] += -0.0 * 3.0; g[0] += -0.0; }", "k")
+            op2.par_loop(k, cells, y(op2.INC, m), g(op2.INC))
+            res.append((y.data_ro.copy(), g.data_ro.copy()))
+    finally:
+        configuration["scatter"] = old
+    (yg, gg), (yo, go) = res
+    assert np.array_equal(yg.view(np.int64), yo.view(np.int64))
+    assert not np.any(np.signbit(yg[:10])) and not np.signbit(gg[0])
+    assert np.array_equal(gg.view(np.int64), go.view(np.int64))
