@@ -8,7 +8,7 @@ set), and one to six arguments -- direct Dats (READ, WRITE, RW,
 INC), indirect Dats (READ, INC, MIN, MAX; WRITE and RW only through the
 bijection, where the result does not depend on the order of iteration),
 Globals (READ, INC, MIN, MAX) and sometimes a MixedDat through a MixedMap
-(READ or INC, one concatenated pack) -- of dimension 1-3 and dtype float64,
+(READ or INC, one concatenated pack) -- of dimension 1-4 and dtype float64,
 float32, int32 or int64.
 The kernel is generated C: it sums its inputs with fixed integer weights and
 writes integer-valued results into every written argument, so every
@@ -56,6 +56,9 @@ def make_spec(seed, data_seed=None):
     over different meshes (a batch)."""
     rs = np.random.default_rng(seed)
     rd = np.random.default_rng(1_000_000 + (seed if data_seed is None else data_seed))
+    # a third stream for draws added later, so that rs and rd draw what
+    # they always drew
+    rx = np.random.default_rng(2_000_000 + seed)
     want_subset = rs.random() < 0.25
     want_bij = rs.random() < 0.35
     total = int(rd.integers(1 if want_bij else 0, 160))
@@ -99,6 +102,8 @@ def make_spec(seed, data_seed=None):
         kind = rs.choice(["direct", "indirect", "global"], p=[0.3, 0.45, 0.25])
         dtype = _dtype_of(rs.random())
         dim = int(rs.integers(1, 4))
+        if dim == 3 and rx.random() < 0.5:
+            dim = 4      # rows of 16 / 32 bytes: the aligned wrapper variant
         if kind == "direct":
             acc = str(rs.choice(DIRECT_ACCESS))
             mp = None

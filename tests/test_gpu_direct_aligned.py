@@ -2,8 +2,9 @@
 wrapper variant that declares each row aligned (so the kernel's accesses to
 adjacent components become vector loads and stores) when the Dat's array is
 aligned, and through the plain wrapper when it is not.  Both must give the
-oracle's results, including PyOP2's pointer semantics for a direct WRITE
-argument: components the kernel does not write keep their values."""
+expected values, including PyOP2's pointer semantics for a direct WRITE
+argument: components the kernel does not write keep their values.  Indirect
+rows of the same sizes, from aligned and offset arrays, are checked too."""
 import numpy as np
 import pytest
 
@@ -85,3 +86,43 @@ def test_same_loop_switches_variant(gpu_op2):
     lp.compute()
     assert np.array_equal(out.data_ro, first)
     assert np.array_equal(first, 2.0 * x.data_ro[c2v.values])
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+@pytest.mark.parametrize("offset", [0, 1], ids=["aligned", "offset"])
+def test_indirect_rows(gpu_op2, case, offset):
+    """Indirect rows of 12 to 32 bytes from an aligned and from an offset
+    array: gathered (READ) through a map, and read and written back (RW)
+    through a bijection."""
+    import torch
+    op2 = gpu_op2
+    ctype, dt, dim = case
+    tdt = {np.float64: torch.float64, np.float32: torch.float32, np.int64: torch.int64}[dt]
+    n, nv = 500, 120
+    rng = np.random.default_rng(dim + offset)
+    cells, verts = op2.Set(n), op2.Set(nv)
+    c2v = op2.Map(cells, verts, 3, rng.integers(0, nv, (n, 3)).astype(np.int32))
+    vals = rng.integers(-9, 10, (nv, dim)).astype(dt)
+    base = torch.full((nv * dim + offset + 4,), -99, dtype=tdt, device="cuda")
+    base[offset:offset + nv * dim] = torch.from_numpy(vals.reshape(-1)).cuda()
+    xv = op2.Dat.from_tensor(verts ** dim, base[offset:offset + nv * dim])
+    out = op2.Dat(cells, np.zeros(n, dtype=dt), dt)
+    src = ("static void k(%(T)s *o, const %(T)s *x) {\n"
+           "  %(T)s s = 0;\n"
+           "  for (int i = 0; i < 3; ++i)\n"
+           "    for (int j = 0; j < %(D)d; ++j) s += x[i * %(D)d + j] * (%(T)s)(1 + i + 3 * j);\n"
+           "  o[0] = s;\n"
+           "}\n") % {"T": ctype, "D": dim}
+    op2.par_loop(op2.Kernel(src, "k"), cells, out(op2.WRITE), xv(op2.READ, c2v))
+    w = np.array([[1 + i + 3 * j for j in range(dim)] for i in range(3)], dtype=dt)
+    want = np.einsum("cij,ij->c", vals[c2v.values], w).astype(dt)
+    assert np.array_equal(out.data_ro, want)
+    # RW through a bijection of the vertices
+    bij = op2.Map(verts, verts, 1, rng.permutation(nv).astype(np.int32).reshape(nv, 1))
+    rw = ("static void r(%(T)s *y) {\n"
+          "  for (int j = 0; j < %(D)d; ++j) y[j] = y[j] * (%(T)s)2 + (%(T)s)j;\n"
+          "}\n") % {"T": ctype, "D": dim}
+    op2.par_loop(op2.Kernel(rw, "r"), verts, xv(op2.RW, bij))
+    assert np.array_equal(xv.data_ro.reshape(nv, dim), vals * 2 + np.arange(dim, dtype=dt))
+    rest = torch.cat([base[:offset], base[offset + nv * dim:]]).cpu().numpy()
+    assert np.all(rest == -99)
