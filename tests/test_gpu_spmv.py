@@ -1,12 +1,15 @@
 """Mat.mult (y = A x and y = A^T x) on assembled block-CSR matrices of every
-block shape the kernels specialise (1x1, 2x2, 3x3) and of shapes they do not
-(2x3, 1x2, 4x4), against scipy's product of the same assembled matrix."""
+block shape up to 4x4 (each has its own lane kernel) and of shapes beyond
+(5x2, 1x6: the tiled kernel), against scipy's product of the same assembled
+matrix."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 SHAPES = [(1, 1), (2, 2), (3, 3), (2, 3), (1, 2), (4, 4)]
+# every block shape up to 4 x 4 has a lane kernel; 5 x 2 and 1 x 6 do not
+ALL_SHAPES = [(r, c) for r in range(1, 5) for c in range(1, 5)] + [(5, 2), (1, 6)]
 
 
 def _assembled(op2, r, c, seed):
@@ -162,3 +165,35 @@ def test_torch_cg_solve_with_exported_matrix(gpu_op2):
         pdir = r + (rr_new / rr) * pdir
         rr = rr_new
     assert np.max(np.abs(x.cpu().numpy() - xs)) <= 1e-10 * np.max(np.abs(xs))
+
+
+@pytest.mark.parametrize("shape", ALL_SHAPES, ids=["%dx%d" % s for s in ALL_SHAPES])
+def test_mult_every_shape_and_unaligned_values(gpu_op2, shape):
+    """y = A x for every block shape against scipy, and through the C ABI
+    with the block values copied to an array 8 bytes past an aligned
+    address (blocks of 16 or 32 bytes are then loaded one double at a time
+    instead of as vectors): the same bits."""
+    import ctypes
+    import torch
+    from pyop2_gb300 import _lib, device
+    op2 = gpu_op2
+    r, c = shape
+    A, drows, dcols, rng = _assembled(op2, r, c, seed=7 * r + c)
+    S = A.to_scipy().tocsr()
+    x = op2.Dat(dcols, rng.uniform(-1, 1, (193, c)) if c > 1 else rng.uniform(-1, 1, 193))
+    y = op2.Dat(drows)
+    A.mult(x, y)
+    ref = S @ x.data_ro.reshape(-1)
+    got = y.data_ro.reshape(-1).copy()
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+    vals = A.tensor
+    shifted = torch.zeros(vals.numel() + 1, dtype=torch.float64, device=vals.device)
+    shifted[1:].copy_(vals)
+    b = A._bcsr()
+    b.values = shifted[1:].data_ptr()
+    assert b.values % 16 == 8
+    y2 = op2.Dat(drows)
+    _lib.call("op2g_mat_spmv", ctypes.byref(b), x._device_ptr(), y2._device_ptr(), 0,
+              device.stream_handle())
+    y2.mark_device_modified()
+    assert np.array_equal(y2.data_ro.reshape(-1), got)
