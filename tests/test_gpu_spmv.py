@@ -172,7 +172,7 @@ def test_mult_every_shape_and_unaligned_values(gpu_op2, shape):
     """y = A x for every block shape against scipy, and through the C ABI
     with the block values copied to an array 8 bytes past an aligned
     address (blocks of 16 or 32 bytes are then loaded one double at a time
-    instead of as vectors): the same bits."""
+    instead of as vectors): the same bits.  y = A^T x likewise, to rounding."""
     import ctypes
     import torch
     from pyop2_gb300 import _lib, device
@@ -197,3 +197,18 @@ def test_mult_every_shape_and_unaligned_values(gpu_op2, shape):
               device.stream_handle())
     y2.mark_device_modified()
     assert np.array_equal(y2.data_ro.reshape(-1), got)
+    # y = A^T x, from the aligned and from the shifted values (sums by
+    # atomics: equal to rounding)
+    xt = op2.Dat(drows, rng.uniform(-1, 1, (257, r)) if r > 1 else rng.uniform(-1, 1, 257))
+    reft = S.T @ xt.data_ro.reshape(-1)
+    for vals_ptr in (None, shifted[1:].data_ptr()):
+        yt = op2.Dat(dcols)
+        if vals_ptr is None:
+            A.mult(xt, yt, transpose=True)
+        else:
+            b.values = vals_ptr
+            yt.tensor.zero_()
+            _lib.call("op2g_mat_spmv", ctypes.byref(b), xt._device_ptr(), yt._device_ptr(), 1,
+                      device.stream_handle())
+            yt.mark_device_modified()
+        assert np.abs(yt.data_ro.reshape(-1) - reft).max() <= 1e-12 * np.abs(reft).max()
