@@ -987,6 +987,7 @@ __global__ void __launch_bounds__(256, MINB)
             q1 = __ldg(m.rowptr + r + 1);
         }
         const int nsteps = ((int)__reduce_max_sync(full, (unsigned)(q1 - q0)) + K - 1) / K;
+        const long long nvals = VW == -2 ? __ldg(m.rowptr + m.nrows) * BS : 0;
         double acc[R];
 #pragma unroll
         for (int i = 0; i < R; ++i) acc[i] = 0.0;
@@ -1004,7 +1005,24 @@ __global__ void __launch_bounds__(256, MINB)
             for (int b = 0; b < K; ++b) {
                 const bool ok = q + b < q1;
                 col[b] = ok ? __ldg(m.colidx + q + b) : 0;
-                if constexpr (VW == 1) {
+                if constexpr (VW == -2) {
+                    // odd block size: the 16-byte pairs covering the block
+                    // (it starts 8 bytes into a pair when its first element
+                    // is odd); the last block, whose pairs could run one
+                    // element past the array, one double at a time
+                    const long long e0 = (q + b) * BS, a0 = e0 & ~1LL;
+                    if (ok && a0 + BS + 1 <= nvals) {
+                        double w[BS + 1];
+                        ld_doubles<BS + 1, 2>(w, m.values + a0);
+                        const bool odd = e0 & 1;
+#pragma unroll
+                        for (int e = 0; e < BS; ++e) v[b * BS + e] = odd ? w[e + 1] : w[e];
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < BS; ++e)
+                            v[b * BS + e] = ok ? __ldg(m.values + e0 + e) : 0.0;
+                    }
+                } else if constexpr (VW == 1) {
 #pragma unroll
                     for (int e = 0; e < BS; ++e)
                         v[b * BS + e] = ok ? __ldg(m.values + (q + b) * BS + e) : 0.0;
@@ -1087,10 +1105,12 @@ cudaError_t spmv_lane_go(cudaStream_t st, const op2g_bcsr &m, const double *x, d
 template <int R, int C, int K, int MINB, bool TR = false>
 cudaError_t spmv_lane_launch(cudaStream_t st, const op2g_bcsr &m, const double *x, double *y) {
     constexpr int BS = R * C;
-    constexpr int VW = BS % 4 == 0 ? 4 : BS % 2 == 0 ? 2 : 1;
-    if constexpr (VW > 1) {
-        if ((uintptr_t)m.values % (8 * VW) == 0)
-            return spmv_lane_go<R, C, K, MINB, VW, TR>(st, m, x, y);
+    // 4 / 2: 256-bit / 16-byte loads; -2: odd blocks of 3 or more through
+    // the 16-byte pairs that cover them; 1: one double at a time
+    constexpr int VW = BS % 4 == 0 ? 4 : BS % 2 == 0 ? 2 : BS >= 3 ? -2 : 1;
+    if constexpr (VW != 1) {
+        const int al = VW == -2 ? 16 : 8 * VW;
+        if ((uintptr_t)m.values % al == 0) return spmv_lane_go<R, C, K, MINB, VW, TR>(st, m, x, y);
     }
     return spmv_lane_go<R, C, K, MINB, 1, TR>(st, m, x, y);
 }
@@ -1178,7 +1198,7 @@ op2g_status op2g_mat_spmv(const op2g_bcsr *m, const double *x, double *y, int32_
     cudaError_t te = cudaSuccess;
     if (transpose) {
         // blocks up to 4 x 4: the lane kernel, C atomics per block (128^3
-        // tet mesh: CSR 0.110 ms, 3x3 0.673 ms, against 0.590 / 1.692 ms for
+        // tet mesh: CSR 0.110 ms, 3x3 0.596 ms, against 0.590 / 1.692 ms for
         // a warp per row with an atomic per entry)
         if (m->ncols * c > INT_MAX || !spmv_t_lane(st, *m, x, y, &te))
             k_spmv_t<<<grid_for(m->nrows * 32, 256), 256, 0, st>>>(*m, x, y);
@@ -1199,7 +1219,7 @@ op2g_status op2g_mat_spmv(const op2g_bcsr *m, const double *x, double *y, int32_
         // Blocks up to 4 x 4: one lane per block row, K blocks per step, the
         // CTAs per SM its registers allow (measured on the 128^3 tet mesh,
         // 31.8 M blocks: 3.5-4x faster than the tiled kernel for every shape;
-        // prism 3x3 matrix of 88.8 M blocks: 1.67 ms against 3.64 ms).
+        // prism 3x3 matrix of 88.8 M blocks: 1.59 ms against 3.64 ms).
         switch (r * 10 + c) {
             case 12: e = spmv_lane_launch<1, 2, 2, 4>(st, *m, x, y); break;
             case 13: e = spmv_lane_launch<1, 3, 2, 4>(st, *m, x, y); break;
