@@ -472,6 +472,7 @@ class Parloop:
                 flat.append((a, 0, 0))
         self._flat = flat
         self._components = [c for c, _, _ in flat]
+        self._written = None
         # pyop2/parloop.py:501-511
         for a in self._components:
             if isinstance(a, DatLegacyArg) and a.data._halo_frozen and \
@@ -771,25 +772,41 @@ class Parloop:
         self._launch_cache = (ptrs, dbg, D)
         return D
 
-    def mark_written(self):
-        """State updates after a launch (pyop2/parloop.py:454-468)."""
+    def _written_lists(self):
+        """What a launch leaves changed (pyop2/parloop.py:454-468), worked out
+        once per set of arguments: Mats with their new assembly state, the
+        Dats and Globals whose device copy becomes the newer one, and the
+        Dats whose halos become stale."""
+        mats, data, halos = [], [], []
         for a in self.args:
             if isinstance(a, MixedMatLegacyArg) and a.access is not Access.READ:
-                a.data.assembly_state = (Mat.ADD_VALUES if a.access is Access.INC
-                                         else Mat.INSERT_VALUES)
-                a.data.increment_dat_version()
+                mats.append((a.data, Mat.ADD_VALUES if a.access is Access.INC
+                             else Mat.INSERT_VALUES))
         for a in self._components:
             if a.access is Access.READ or isinstance(a, PassthroughArg):
                 continue
             if isinstance(a, MatLegacyArg):
-                a.data.assembly_state = (Mat.ADD_VALUES if a.access is Access.INC
-                                         else Mat.INSERT_VALUES)
-                a.data.increment_dat_version()
+                mats.append((a.data, Mat.ADD_VALUES if a.access is Access.INC
+                             else Mat.INSERT_VALUES))
             else:
-                a.data._m.dev_modified()
-                a.data.increment_dat_version()
+                data.append(a.data)
                 if isinstance(a, DatLegacyArg):
-                    a.data.halo_valid = False
+                    halos.append(a.data)
+        return mats, data, halos
+
+    def mark_written(self):
+        """State updates after a launch (pyop2/parloop.py:454-468)."""
+        if self._written is None:
+            self._written = self._written_lists()
+        mats, data, halos = self._written
+        for m, state in mats:
+            m.assembly_state = state
+            m.increment_dat_version()
+        for d in data:
+            d._m.dev_modified()
+            d.increment_dat_version()
+        for d in halos:
+            d.halo_valid = False
 
     def compute(self):
         if configuration["profiling"]:

@@ -36,6 +36,14 @@ class DataCarrier:
         return as_cstr(self.dtype)
 
 
+def _dat_arg(*args):
+    """DatLegacyArg(*args), bound on first use (parloop imports this module)."""
+    global _dat_arg
+    from pyop2_gb300.parloop import DatLegacyArg
+    _dat_arg = DatLegacyArg
+    return DatLegacyArg(*args)
+
+
 class AbstractDat(DataCarrier):
     _modes = [Access.READ, Access.WRITE, Access.RW, Access.INC, Access.MIN, Access.MAX]
 
@@ -74,13 +82,17 @@ class Dat(AbstractDat):
         self.halo_valid = True
         self._version = 0
 
-    # ---- kernel-argument construction
-    @utils.validate_in(('access', AbstractDat._modes, ex.ModeValueError))
+    # ---- kernel-argument construction (runs for every argument of every
+    # par_loop call, so the reference's validate_in access check is written
+    # out here, with its message)
     def __call__(self, access, path=None):
-        from pyop2_gb300.parloop import DatLegacyArg
-        if configuration["type_check"] and path is not None and path.toset != self.dataset.set:
-            raise ex.MapValueError("To Set of Map does not match Set of Dat.")
-        return DatLegacyArg(self, path, access)
+        if configuration["type_check"]:
+            if access not in AbstractDat._modes:
+                raise ex.ModeValueError("access must be one of %s, not %r"
+                                        % (AbstractDat._modes, access))
+            if path is not None and path.toset != self.dataset.set:
+                raise ex.MapValueError("To Set of Map does not match Set of Dat.")
+        return _dat_arg(self, path, access)
 
     def __getitem__(self, idx):
         if idx != 0:

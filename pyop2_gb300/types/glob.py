@@ -8,9 +8,18 @@ import numpy as np
 
 from pyop2_gb300 import exceptions as ex
 from pyop2_gb300 import utils
+from pyop2_gb300.configuration import configuration
 from pyop2_gb300.device import Mirror
 from pyop2_gb300.types.access import Access
 from pyop2_gb300.types.dat import DataCarrier
+
+
+def _global_arg(*args):
+    """GlobalLegacyArg(*args), bound on first use (parloop imports this module)."""
+    global _global_arg
+    from pyop2_gb300.parloop import GlobalLegacyArg
+    _global_arg = GlobalLegacyArg
+    return GlobalLegacyArg(*args)
 
 
 class Global(DataCarrier):
@@ -39,11 +48,13 @@ class Global(DataCarrier):
         self.comm = comm
         self._version = 0
 
-    @utils.validate_in(('access', _modes, ex.ModeValueError))
+    # the reference's validate_in access check written out, with its message
+    # (this runs for every Global argument of every par_loop call)
     def __call__(self, access, map_=None):
-        from pyop2_gb300.parloop import GlobalLegacyArg
+        if configuration["type_check"] and access not in self._modes:
+            raise ex.ModeValueError("access must be one of %s, not %r" % (self._modes, access))
         assert map_ is None
-        return GlobalLegacyArg(self, access)
+        return _global_arg(self, access)
 
     def __getitem__(self, idx):
         if idx != 0:
