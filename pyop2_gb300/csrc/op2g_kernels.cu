@@ -734,9 +734,10 @@ __global__ void k_set_diag(op2g_bcsr m, const int *__restrict__ rows, long long 
 // identical.
 constexpr int SPMV_T = 256, SPMV_PER = 8, SPMV_TILE = SPMV_T * SPMV_PER;
 
-// Blocks of R x C > 1 entries: a 3x3 block row holds ~190 entries, so one
-// thread per dof row would leave most lanes of a tile idle; instead S lanes
-// share a dof row and the next tile's loads overlap the current sums.
+// Blocks with more than 4 rows or columns (smaller ones run the lane kernel
+// below): a block row holds hundreds of entries, so one thread per dof row
+// would leave most lanes of a tile idle; instead S lanes share a dof row and
+// the next tile's loads overlap the current sums.
 //
 // Work: a CTA takes slabs of NB consecutive block rows (grid-stride); NB is
 // chosen from the mean row length so that a slab's entries fill about 90 %
