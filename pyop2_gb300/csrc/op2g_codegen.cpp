@@ -1022,6 +1022,25 @@ struct Gen {
             O << J << "}\n";
         } else {
             O << J << "const long long n = " << (S.loop.indexed ? "p.indices[it]" : "it") << ";\n";
+            // The next sweep step's rows of direct arguments that are read
+            // are prefetched into L2: the kernel's loads through them cannot
+            // move above its stores through other Dat pointers (the compiler
+            // cannot prove them distinct), so each thread would otherwise
+            // keep one load in flight (a 12.58 M-cell direct copy: 0.042 ->
+            // 0.037 ms; a prefetch is a hint, nothing it reads is used).
+            if (!S.loop.indexed && cpt == 1 && !staging) {
+                bool any = false;
+                for (size_t a = 0; a < S.args.size(); ++a) {
+                    const op2g_arg_desc &d = S.args[a].d;
+                    if (d.kind != OP2G_ARG_DAT || d.map >= 0 || d.access == OP2G_WRITE) continue;
+                    if (!any) O << J << "if (it + stride < i1_) {\n";
+                    any = true;
+                    O << J << "  asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(("
+                      << ctype_of(d.dtype) << " *)p.ptr[" << S.args[a].slot << "] + (it + stride) * "
+                      << gstride(a) << "));\n";
+                }
+                if (any) O << J << "}\n";
+            }
             emit_body(J, warp, plain, pf);
         }
         O << I << "}\n";
