@@ -234,3 +234,20 @@ def test_cells_per_thread(op2, cells):
                                  pl2._loop_desc(_lib.SCATTER_ATOMIC, 256, 0, cells),
                                  argdescs, table.key(), arch="sm_103a").source()
         assert ("stride * " in src2) == multi
+
+
+def test_next_rows_of_read_direct_arguments_are_prefetched(op2):
+    """A flat loop prefetches the next sweep step's rows of the direct
+    arguments it reads (READ, RW) into L2, not of those it only writes; an
+    indexed loop (a Subset: the next entity is not known) prefetches none."""
+    cells = op2.Set(8)
+    r, w, b = op2.Dat(cells ** 2), op2.Dat(cells ** 3), op2.Dat(cells)
+    k = op2.Kernel("static void k(const double *r, double *w, double *b) {}", "k")
+    src = compile_loop(LegacyParloop(k, cells, r(op2.READ), w(op2.WRITE), b(op2.RW))).source()
+    assert src.count("prefetch.global.L2") == 2
+    assert "(double *)p.ptr[0] + (it + stride) * 2" in src
+    assert "(double *)p.ptr[2] + (it + stride) * 1" in src
+    assert "p.ptr[1] + (it + stride)" not in src
+    sub = op2.Subset(cells, [1, 3, 5])
+    src2 = compile_loop(LegacyParloop(k, sub, r(op2.READ), w(op2.WRITE), b(op2.RW))).source()
+    assert "prefetch.global.L2" not in src2
