@@ -251,3 +251,19 @@ def test_next_rows_of_read_direct_arguments_are_prefetched(op2):
     sub = op2.Subset(cells, [1, 3, 5])
     src2 = compile_loop(LegacyParloop(k, sub, r(op2.READ), w(op2.WRITE), b(op2.RW))).source()
     assert "prefetch.global.L2" not in src2
+
+
+def test_inc_packs_start_at_negative_zero(op2):
+    """INC packs of floating types (Dat, Mat, Global) start at -0.0, the
+    identity of IEEE addition; WRITE packs and integer INC packs at 0."""
+    cells, verts = op2.Set(8), op2.Set(10)
+    m = op2.Map(cells, verts, 2, np.arange(16) % 10)
+    yd, yf, yi, wd = (op2.Dat(verts, dtype=np.float64), op2.Dat(verts, dtype=np.float32),
+                      op2.Dat(verts, dtype=np.int32), op2.Dat(verts, dtype=np.float64))
+    g = op2.Global(1, 0.0)
+    k = op2.Kernel("static void k(double *a, float *b, int *c, double *d, double *g) {}", "k")
+    src = compile_loop(LegacyParloop(k, cells, yd(op2.INC, m), yf(op2.INC, m), yi(op2.INC, m),
+                                     wd(op2.WRITE, m), g(op2.INC))).source()
+    assert "t0[k] = (-0.0);" in src and "t1[k] = (-0.0f);" in src
+    assert "t2[k] = (int)0;" in src and "t3[k] = (double)0;" in src
+    assert "g4[j] = (-0.0);" in src
